@@ -1,0 +1,140 @@
+/* xrh.h - C ABI of the GB300 (sm_103a) excitonic-Hamiltonian build library, libxrh.so.
+ *
+ * Plain C types only (pointers, sizes, status codes).  Every pointer named *_dev is a
+ * device pointer (CUDA global memory) owned by the caller; the library allocates nothing
+ * on these paths.  `stream` is a cudaStream_t passed as void*.  Every call is stream
+ * ordered, does not synchronise the host, and returns XRH_OK or an error status.
+ *
+ * The entry points replace the reference's native kernels and their Python drivers:
+ *   general-XRCC/density_tensors.c   (density builder)            -> xrh_couplings_*,
+ *                                                                    xrh_density_accumulate
+ *   general-XRCC/build_density_tensors.py:122-133 (ccaa folded    -> xrh_sigma2e
+ *        with V into one number per state pair)
+ *   general-XRCC/H_contractions.c + hermitian-XRCC precontract.py  -> xrh_gemm_grouped
+ *        + diagrams/* (all density x integral contractions, batched as grouped GEMMs)
+ * The reference binds its C kernels one matrix element at a time through Qode's PyC
+ * (general-XRCC/build_H.py:20-29, build_density_tensors.py:23-26); here each call covers
+ * whole blocks of elements.  The ctypes binding is qodeapplications_gb300/_lib.py.
+ */
+#ifndef XRH_H
+#define XRH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define XRH_OK 0
+#define XRH_ERR_ARG 1          /* bad size, null pointer or unsupported combination */
+#define XRH_ERR_CUDA 2         /* a CUDA launch or API call failed (see xrh_last_cuda_error) */
+#define XRH_ERR_UNSUPPORTED 3  /* precision / feature not built for this device */
+#define XRH_ERR_TIMEOUT 4      /* a bounded device-side wait gave up (kernel returned early) */
+#define XRH_ERR_CAPACITY 5     /* a size exceeds a documented limit */
+
+/* arithmetic of a contraction */
+#define XRH_FP64 0       /* IEEE FP64 on CUDA cores (the plain drop-in path) */
+#define XRH_FP32 1       /* FP32 products, FP32 partial sums, FP64 final sums */
+#define XRH_BF16X3 2     /* tcgen05 kind::f16, operands split hi+lo in BF16, 3 products, FP32 accum */
+#define XRH_TF32X3 3     /* tcgen05 kind::tf32, operands split hi+lo in TF32, 3 products, FP32 accum */
+
+int xrh_abi_version(void);
+const char* xrh_status_string(int status);
+int xrh_last_cuda_error(void);
+
+/* Field-operator strings ("a", "c", "ca", "aa", "cc", "caa", "cca", "ccaa") are encoded
+ * as  len | (c_bits << 4)  where bit i of c_bits is set when letter i is 'c'.  Operators
+ * act right to left; operator indices are flattened row-major in string order, the
+ * layout of general-XRCC/density_tensors.c:272,319,420,480,543. */
+
+/* Coupling lists <P| op_idx |Q> = +-1 between determinant lists (uint64 occupation masks,
+ * spin orbital i<n_orbs alpha, n_orbs+i beta; N = 2*n_orbs <= 64).  Results that empty
+ * the frozen core (n_core lowest orbitals of each spin) or are not in the bra list are
+ * dropped (density_tensors.c:125-134, :49-62).  The bra list is given sorted
+ * (bra_sorted_masks) with the original position of each entry (bra_sorted_pos).
+ * count: counts_dev[Q] = number of couplings of ket Q.
+ * fill:  writes them at offsets_dev[Q] (exclusive scan of the counts), in ascending
+ *        idx order per Q: idx (flat operator index), P (bra position), Q, sign (+1/-1). */
+int xrh_couplings_count(int op_code, int n_orbs, int n_core,
+                        const uint64_t* ket_masks_dev, int n_ket,
+                        const uint64_t* bra_sorted_masks_dev, const int32_t* bra_sorted_pos_dev, int n_bra,
+                        int64_t* counts_dev, void* stream);
+int xrh_couplings_fill(int op_code, int n_orbs, int n_core,
+                       const uint64_t* ket_masks_dev, int n_ket,
+                       const uint64_t* bra_sorted_masks_dev, const int32_t* bra_sorted_pos_dev, int n_bra,
+                       const int64_t* offsets_dev, int32_t* idx_dev, int32_t* P_dev, int32_t* Q_dev,
+                       int8_t* sign_dev, void* stream);
+
+/* Transition densities from coupling lists sorted by idx (CSR, idx_ptr_dev has K+1 entries):
+ *   rhoT[idx, I, J] = sum_c sign_c * zb[I, P_c] * zk[J, Q_c]
+ * (z_contract, density_tensors.c:142-154).  zbT_dev is [n_bra_conf, n_b] (coefficients
+ * transposed, one row per determinant), zkT_dev is [n_ket_conf, n_k].  precision is
+ * XRH_FP64 or XRH_FP32.  Output rhoT_dev [K, n_b, n_k] is fully overwritten. */
+int xrh_density_accumulate(int precision, int64_t K, const int64_t* idx_ptr_dev,
+                           const int32_t* P_dev, const int32_t* Q_dev, const int8_t* sign_dev,
+                           const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
+                           double* rhoT_dev, void* stream);
+
+/* out[c, r] = in[r, c] for a row-major [rows, cols] FP64 matrix. */
+int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_dev, void* stream);
+
+/* Monomer two-electron term without the N^4 density (replaces building rho^ccaa and
+ * contracting it, general-XRCC/build_density_tensors.py:122-133 + H_contractions.c:61-78):
+ *   sigmaT[J, P] = sum_Q <P| sum_pqrs V_pqrs c+_p c+_q a_s a_r |Q> zk[J, Q]
+ * for every bra determinant P; V_dev is the fragment's antisymmetric N^4 block.  The
+ * caller finishes with E2 = Zb . sigma (one GEMM).  precision XRH_FP64 or XRH_FP32. */
+int xrh_sigma2e(int precision, int n_orbs, const double* V_dev,
+                const uint64_t* bra_masks_dev, int n_bra_conf,
+                const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev, int n_ket_conf,
+                const double* zkT_dev, int n_k, double* sigmaT_dev, void* stream);
+
+/* Grouped GEMM with K-concatenated segments and an FP64 epilogue.
+ * For each task t and each (m, n) in [0,M) x [0,N):
+ *   acc = sum over the task's segments s of alpha_s * sum_k A_s[m, k] * B_s[n, k]
+ * (A_s, B_s row-major with K contiguous, row strides lda/ldb in elements).  Then
+ *   mode 0: C[m*ldc + n]  = acc
+ *   mode 1: C[m*ldc + n] += acc   (atomic; the task may be split splitk ways along K)
+ *   mode 2: H[(rowA[m]+rowB[n])*ldc + colA[m]+colB[n]] =
+ *              acc + (diagB[n] ? DA[m] : 0) + (diagA[m] ? DB[n] : 0)
+ *           (charge-block to product-state scatter with the delta-function terms,
+ *            hermitian-XRCC/XR_term.py:36-94, get_xr_result.py:300-353)
+ * tasks_dev / segs_dev are device arrays of the structs below; tile_begin of every task
+ * and total_tiles come from the host (tiles are 64x64 for XRH_FP64, 128x128 for the
+ * tensor-core precisions, times splitk).  For XRH_BF16X3 / XRH_TF32X3 the segment
+ * operands must first be split with xrh_split_operand and described by tensor maps; see
+ * xrh_gemm_tc_grouped. */
+typedef struct {
+    const double* A;
+    const double* B;
+    int64_t lda, ldb;
+    int64_t K;
+    double alpha;
+} xrh_gemm_segment;
+
+typedef struct {
+    int64_t M, N;
+    int64_t seg_begin, seg_count;
+    int64_t mode;
+    int64_t splitk;
+    int64_t tile_begin;
+    double* C;
+    int64_t ldc;
+    const int32_t* rowA;
+    const int32_t* colA;
+    const int32_t* rowB;
+    const int32_t* colB;
+    const double* DA;
+    const double* DB;
+    const uint8_t* diagA;
+    const uint8_t* diagB;
+} xrh_gemm_task;
+
+int xrh_gemm_fp64_grouped(const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
+                          const xrh_gemm_segment* segs_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XRH_H */

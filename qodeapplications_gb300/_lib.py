@@ -1,0 +1,103 @@
+"""ctypes binding of libxrh.so (include/xrh.h).
+
+The library is built in-tree by qodeapplications_gb300/build.py.  There is no fallback:
+if the shared library is missing or a call returns an error status, an XRHError is raised.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libxrh.so")
+
+XRH_OK, XRH_ERR_ARG, XRH_ERR_CUDA, XRH_ERR_UNSUPPORTED, XRH_ERR_TIMEOUT, XRH_ERR_CAPACITY = range(6)
+FP64, FP32, BF16X3, TF32X3 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x3": BF16X3, "tf32x3": TF32X3}
+
+
+class XRHError(RuntimeError):
+    pass
+
+
+_i32, _i64, _vp, _dbl = ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_double
+
+_SIGS = {
+    "xrh_abi_version": (_i32, []),
+    "xrh_status_string": (ctypes.c_char_p, [_i32]),
+    "xrh_last_cuda_error": (_i32, []),
+    "xrh_couplings_count": (_i32, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
+    "xrh_couplings_fill": (_i32, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "xrh_density_accumulate": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
+    "xrh_transpose": (_i32, [_vp, _i64, _i64, _vp, _vp]),
+    "xrh_sigma2e": (_i32, [_i32, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
+    "xrh_gemm_fp64_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
+}
+_OPTIONAL = {}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise XRHError(f"{LIB_PATH} is missing: build it with `python -m qodeapplications_gb300.build` "
+                           "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in list(_SIGS.items()) + list(_OPTIONAL.items()):
+            if not hasattr(L, name):
+                if name in _OPTIONAL:
+                    continue
+                raise XRHError(f"{LIB_PATH} does not export {name}")
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def register(name, restype, argtypes):
+    """Declare an additional exported symbol (used by modules that add entry points)."""
+    _SIGS[name] = (restype, argtypes)
+    if _lib is not None:
+        f = getattr(_lib, name)
+        f.restype = restype
+        f.argtypes = argtypes
+
+
+def call(name, *args):
+    st = getattr(lib(), name)(*args)
+    if st != XRH_OK:
+        msg = lib().xrh_status_string(st).decode()
+        raise XRHError(f"{name} failed: {msg} (status {st}, cuda error {lib().xrh_last_cuda_error()})")
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor, or None."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def op_code(op):
+    code = len(op)
+    for i, ch in enumerate(op):
+        if ch == "c":
+            code |= 1 << (4 + i)
+    return code
+
+
+# numpy mirrors of the ABI structs (field order and sizes match include/xrh.h)
+SEGMENT_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("lda", np.int64), ("ldb", np.int64),
+                          ("K", np.int64), ("alpha", np.float64)])
+TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
+                       ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("C", np.uint64),
+                       ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64), ("rowB", np.uint64),
+                       ("colB", np.uint64), ("DA", np.uint64), ("DB", np.uint64), ("diagA", np.uint64),
+                       ("diagB", np.uint64)])
+assert SEGMENT_DTYPE.itemsize == 48 and TASK_DTYPE.itemsize == 136

@@ -1,0 +1,29 @@
+// Status helpers of the C ABI (include/xrh.h).
+#include "xrh_common.cuh"
+
+static int g_last_cuda_error = 0;
+
+extern "C" void xrh_set_last_cuda_error(int e) { g_last_cuda_error = e; }
+
+extern "C" int xrh_abi_version(void) { return 1; }
+
+extern "C" const char* xrh_status_string(int status) {
+    switch (status) {
+        case XRH_OK: return "ok";
+        case XRH_ERR_ARG: return "invalid argument";
+        case XRH_ERR_CUDA: return "CUDA error";
+        case XRH_ERR_UNSUPPORTED: return "unsupported precision or feature";
+        case XRH_ERR_TIMEOUT: return "bounded device wait timed out";
+        case XRH_ERR_CAPACITY: return "size exceeds a documented limit";
+        default: return "unknown status";
+    }
+}
+
+extern "C" int xrh_last_cuda_error(void) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) g_last_cuda_error = (int)e;
+    return g_last_cuda_error;
+}
+
+static_assert(sizeof(xrh_gemm_segment) == 48, "xrh_gemm_segment layout is part of the ABI");
+static_assert(sizeof(xrh_gemm_task) == 136, "xrh_gemm_task layout is part of the ABI");

@@ -1,0 +1,180 @@
+"""Fragment transition densities on the GPU.
+
+Mirrors the reference's density builders:
+  general-XRCC/build_density_tensors.py:57-160  build_density_tensors(z_lists, n_orbs, Vints, n_core)
+  Be-states/densities.py:236                    build_tensors(states, n_orbs, n_elec_0, ...)
+and the C kernels they drive (general-XRCC/density_tensors.c).
+
+GB300 design: the determinant lists of a fragment never change during an optimisation, so
+the integer coupling lists <P|op_idx|Q> = +-1 are built once on the device
+(FragmentSpace) and stay resident in HBM.  Each density build (DensityBuilder.build)
+is then only the floating-point gather-accumulate rho[I,J,idx] = sum s z_I[P] z_J[Q]
+plus a transpose into the reference's (n_bra, n_ket, N, ..., N) layout.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr, stream_ptr
+
+# op strings per (bra_chg - ket_chg) (general-XRCC/build_density_tensors.py:90-157); the
+# four-operator ccaa density is never stored: its only use (monomer two-electron energy)
+# goes through the sigma-vector kernel instead.
+OPS_FOR_DCHG = {+2: ("aa",), +1: ("a", "caa"), 0: ("ca",), -1: ("c", "cca"), -2: ("cc",)}
+
+
+class Couplings:
+    """Resident coupling list of one (op, bra charge, ket charge), CSR by operator index."""
+
+    def __init__(self, op, K, idx_ptr, P, Q, sign):
+        self.op, self.K = op, K
+        self.idx_ptr, self.P, self.Q, self.sign = idx_ptr, P, Q, sign
+
+    @property
+    def count(self):
+        return int(self.P.numel())
+
+
+def _sort_masks(masks_np):
+    order = np.argsort(masks_np, kind="stable")
+    return masks_np[order], order.astype(np.int32)
+
+
+class FragmentSpace:
+    """Determinant lists of one fragment (per charge) and their coupling lists on the GPU.
+
+    sectors: {charge: uint64 numpy array of occupation masks}; spin orbital i < n_orbs is
+    alpha i, n_orbs + i is beta i (general-XRCC/density_tensors.c:58-59 ordering)."""
+
+    def __init__(self, sectors, n_orbs, n_core, n_elec_ref, device="cuda", ops=None):
+        self.n_orbs, self.n_core, self.n_elec_ref = n_orbs, n_core, n_elec_ref
+        self.N = 2 * n_orbs
+        self.device = torch.device(device)
+        self.charges = list(sectors.keys())
+        self.masks_np = {c: np.ascontiguousarray(np.asarray(m, dtype=np.uint64)) for c, m in sectors.items()}
+        self.n_conf = {c: len(m) for c, m in self.masks_np.items()}
+        self.n_elec = {c: n_elec_ref - c for c in self.charges}
+        self.masks = {}
+        self.sorted_masks = {}
+        self.sorted_pos = {}
+        for c, m in self.masks_np.items():
+            sm, order = _sort_masks(m)
+            self.masks[c] = torch.from_numpy(m.view(np.int64).copy()).to(self.device)
+            self.sorted_masks[c] = torch.from_numpy(sm.view(np.int64).copy()).to(self.device)
+            self.sorted_pos[c] = torch.from_numpy(order).to(self.device)
+        self.couplings = {}
+        for bc in self.charges:
+            for kc in self.charges:
+                for op in OPS_FOR_DCHG.get(bc - kc, ()):
+                    if ops is not None and op not in ops:
+                        continue
+                    self.couplings[(op, bc, kc)] = self._build(op, bc, kc)
+
+    def _build(self, op, bc, kc):
+        n_ket, n_bra = self.n_conf[kc], self.n_conf[bc]
+        K = self.N ** len(op)
+        s = stream_ptr()
+        counts = torch.zeros(max(n_ket, 1), dtype=torch.int64, device=self.device)
+        call("xrh_couplings_count", _lib.op_code(op), self.n_orbs, self.n_core, ptr(self.masks[kc]), n_ket,
+             ptr(self.sorted_masks[bc]), ptr(self.sorted_pos[bc]), n_bra, ptr(counts), s)
+        offsets = torch.zeros_like(counts)
+        if n_ket > 1:
+            offsets[1:] = torch.cumsum(counts, 0)[:-1]
+        total = int(counts.sum().item())
+        idx = torch.empty(max(total, 1), dtype=torch.int32, device=self.device)
+        P = torch.empty_like(idx)
+        Q = torch.empty_like(idx)
+        sign = torch.empty(max(total, 1), dtype=torch.int8, device=self.device)
+        if total:
+            call("xrh_couplings_fill", _lib.op_code(op), self.n_orbs, self.n_core, ptr(self.masks[kc]), n_ket,
+                 ptr(self.sorted_masks[bc]), ptr(self.sorted_pos[bc]), n_bra, ptr(offsets), ptr(idx), ptr(P),
+                 ptr(Q), ptr(sign), s)
+        idx, P, Q, sign = idx[:total], P[:total], Q[:total], sign[:total]
+        # stable sort by operator index (Q order kept inside an index: deterministic sums)
+        order = torch.argsort(idx.to(torch.int64) * (max(n_ket, 1)) + Q.to(torch.int64))
+        idx, P, Q, sign = idx[order].contiguous(), P[order].contiguous(), Q[order].contiguous(), sign[order].contiguous()
+        idx_ptr = torch.zeros(K + 1, dtype=torch.int64, device=self.device)
+        if total:
+            idx_ptr[1:] = torch.cumsum(torch.bincount(idx.to(torch.int64), minlength=K), 0)
+        return Couplings(op, K, idx_ptr, P, Q, sign)
+
+
+class DensityBuilder:
+    """Preallocated, reusable density build for one fragment and fixed state counts.
+
+    build(coeffs, bra_coeffs=None) fills self.rho[op][(bra_chg, ket_chg)], each a CUDA
+    float64 tensor of shape (n_bra, n_ket, N, ..., N) (the reference's layout,
+    Be-states/densities.py:167-208).  Buffers are reused by every call (CUDA-graph safe)."""
+
+    def __init__(self, space, n_states, precision="fp64", n_states_bra=None):
+        self.space = space
+        self.precision = _lib.PRECISIONS[precision]
+        if self.precision not in (_lib.FP64, _lib.FP32):
+            self.precision = _lib.FP32       # tensor-core variants build densities with FP32 products
+        self.n_states = dict(n_states)
+        self.n_states_bra = dict(n_states_bra or n_states)
+        dev = space.device
+        self.rho = {}
+        self._tmp = {}
+        for (op, bc, kc), cp in space.couplings.items():
+            nb, nk = self.n_states_bra[bc], self.n_states[kc]
+            shape = (nb, nk) + (space.N,) * len(op)
+            self.rho.setdefault(op, {})[(bc, kc)] = torch.empty(shape, dtype=torch.float64, device=dev)
+            self._tmp[(op, bc, kc)] = torch.empty(cp.K * nb * nk, dtype=torch.float64, device=dev)
+        self.zT = {c: torch.empty((space.n_conf[c], self.n_states[c]), dtype=torch.float64, device=dev)
+                   for c in space.charges}
+        self.zbT = {c: torch.empty((space.n_conf[c], self.n_states_bra[c]), dtype=torch.float64, device=dev)
+                    for c in space.charges}
+
+    def build(self, coeffs, bra_coeffs=None):
+        """coeffs: {charge: CUDA float64 tensor (n_states, n_conf)}."""
+        s = stream_ptr()
+        for c in self.space.charges:
+            self.zT[c].copy_(coeffs[c].t())
+            self.zbT[c].copy_((coeffs if bra_coeffs is None else bra_coeffs)[c].t())
+        for (op, bc, kc), cp in self.space.couplings.items():
+            nb, nk = self.n_states_bra[bc], self.n_states[kc]
+            tmp = self._tmp[(op, bc, kc)]
+            call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
+                 ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
+            call("xrh_transpose", ptr(tmp), cp.K, nb * nk, ptr(self.rho[op][(bc, kc)]), s)
+        return self.rho
+
+
+def as_device_sectors(states, device="cuda"):
+    """{chg: (coeffs (n_states, n_conf), masks)} -> device coefficient tensors."""
+    return {c: torch.as_tensor(np.asarray(co), dtype=torch.float64, device=device) for c, (co, _m) in states.items()}
+
+
+def build_density_tensors(z_lists, n_orbs, Vints, n_core, n_threads=1):
+    """Drop-in for general-XRCC/build_density_tensors.py:57 (same arguments and result
+    layout): z_lists[chg].configs is (n_conf, n_e) occupied spin-orbital lists,
+    z_lists[chg].coeffs (n_states, n_conf).  Returns (densities, total_size) with
+    densities[op][(bra_chg, ket_chg)][I][J] an ndarray and densities['ccaa'][..][I][J] the
+    scalar sum V_pqrs rho^ccaa_IJ[p,q,s,r] (build_density_tensors.py:129-133).
+    n_threads is accepted for signature compatibility (the reference ignores it too)."""
+    from .hamiltonian import monomer_two_electron
+    sectors, coeffs = {}, {}
+    for chg, st in z_lists.items():
+        occ = np.asarray(st.configs, dtype=np.int64)
+        masks = np.zeros(occ.shape[0], dtype=np.uint64)
+        for col in range(occ.shape[1]):
+            masks |= np.uint64(1) << occ[:, col].astype(np.uint64)
+        sectors[chg] = masks
+        coeffs[chg] = np.asarray(list(st.coeffs), dtype=np.float64)
+    space = FragmentSpace(sectors, n_orbs, n_core, n_elec_ref=0)
+    builder = DensityBuilder(space, {c: coeffs[c].shape[0] for c in sectors})
+    rho = builder.build({c: torch.as_tensor(coeffs[c], device=space.device) for c in sectors})
+    out = {op: {} for op in ("aa", "a", "caa", "ca", "ccaa", "c", "cca", "cc")}
+    total = 0
+    for op, blocks in rho.items():
+        for key, t in blocks.items():
+            a = t.cpu().numpy()
+            out[op][key] = [[a[i, j] for j in range(a.shape[1])] for i in range(a.shape[0])]
+            total += a.size
+    V = torch.as_tensor(np.asarray(Vints, dtype=np.float64), device=space.device)
+    for c in sectors:
+        e2 = monomer_two_electron(space, {c: torch.as_tensor(coeffs[c], device=space.device)}, V, c).cpu().numpy()
+        out["ccaa"][(c, c)] = [[float(e2[i, j]) for j in range(e2.shape[1])] for i in range(e2.shape[0])]
+        total += e2.size
+    return out, total

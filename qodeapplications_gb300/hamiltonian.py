@@ -1,0 +1,333 @@
+"""Excitonic-Hamiltonian (XR-H) build on the GPU for a fragment dimer (order 0, S = 1).
+
+This is the GB300 form of hermitian-XRCC get_xr_H at xr_order 0
+(get_xr_result.py:86-132, :300-355) and of general-XRCC build_matrix_elements.dimer /
+.monomer (build_H.py:42-102).  The reference evaluates every (diagram, charge block,
+permutation) lazily in Python and calls BLAS per term; here the whole build is planned
+once into two grouped launches:
+
+1. precontractions (precontract.py:32-80): rho x integral GEMMs, one task per
+   (fragment, charge pair, family), plus the monomer one-electron GEMVs and the
+   delta-function u100 terms;
+2. final contractions: ONE task per output charge block (ci0,ci1 | cj0,cj1), whose
+   K-concatenated segments are all order-0 diagrams that land in that block
+   (t01, u001, u101, v0001, v0100, v0011, v0101 with their catalog phases and
+   n_j0 parities, diagrams/S*_diagrams.py), and whose FP64 epilogue adds u100 and
+   H1 x 1 + 1 x H1 and scatters from charge-blocked to product-state order.
+
+The monomer two-electron energy (v0000, SV_1mer_0.py:24) never materialises the N^4
+ccaa density: a sigma-vector kernel plus one GEMM compute sum V rho^ccaa directly.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr, stream_ptr
+from .densities import DensityBuilder, FragmentSpace
+from .gemm import GroupedGemm
+
+
+class DeviceIntegrals:
+    """Fragment-blocked spin-orbital integrals on the device.
+
+    source: any object with block accessors T[m,n], U[k,m,n], V[m,n,o,p] returning arrays
+    (the interface of the reference's integral structs, hermitian-XRCC/get_ints.py), or
+    the supersystem arrays h (with U folded in) and V plus the spin orbitals per fragment."""
+
+    def __init__(self, h=None, V=None, Ns=None, U=None, source=None, device="cuda"):
+        self.device = torch.device(device)
+        self._cache = {}
+        if source is not None:
+            self._src = source
+            return
+        self.Ns = list(Ns)
+        off = np.concatenate([[0], np.cumsum(self.Ns)]).astype(int)
+        self.off = off
+        n_f = len(self.Ns)
+        tot = off[-1]
+        U = np.zeros((n_f, tot, tot)) if U is None else np.asarray(U, dtype=np.float64)
+        self._h = torch.as_tensor(np.asarray(h, dtype=np.float64), device=self.device)
+        self._U = torch.as_tensor(U, device=self.device)
+        self._Tfull = self._h - self._U.sum(0)
+        self._V = torch.as_tensor(np.asarray(V, dtype=np.float64), device=self.device)
+        self._src = None
+
+    def _sl(self, m):
+        return slice(int(self.off[m]), int(self.off[m + 1]))
+
+    def T(self, m, n):
+        if self._src is not None:
+            return self._get(("T", m, n), lambda: self._src.T[m, n])
+        return self._Tfull[self._sl(m), self._sl(n)]
+
+    def U(self, k, m, n):
+        if self._src is not None:
+            return self._get(("U", k, m, n), lambda: self._src.U[k, m, n])
+        return self._U[k][self._sl(m), self._sl(n)]
+
+    def V(self, m, n, o, p):
+        if self._src is not None:
+            return self._get(("V", m, n, o, p), lambda: self._src.V[m, n, o, p])
+        return self._V[self._sl(m), self._sl(n), self._sl(o), self._sl(p)]
+
+    def _get(self, key, fn):
+        if key not in self._cache:
+            self._cache[key] = torch.as_tensor(np.asarray(fn(), dtype=np.float64), device=self.device)
+        return self._cache[key]
+
+
+class SigmaTwoElectron:
+    """E2[I,J] = sum_PQ zb[I,P] <P|V|Q> zk[J,Q] for one fragment and charge (v0000)."""
+
+    def __init__(self, space, charge, n_states, V_block, precision=_lib.FP64):
+        self.space, self.c, self.n = space, charge, n_states
+        self.V = V_block.contiguous()
+        self.precision = precision if precision in (_lib.FP64, _lib.FP32) else _lib.FP32
+        nconf = space.n_conf[charge]
+        self.sigmaT = torch.empty((n_states, nconf), dtype=torch.float64, device=space.device)
+
+    def run_sigma(self, zT):
+        sp = self.space
+        c = self.c
+        call("xrh_sigma2e", self.precision, sp.n_orbs, ptr(self.V), ptr(sp.masks[c]), sp.n_conf[c],
+             ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(zT), self.n, ptr(self.sigmaT),
+             stream_ptr())
+
+
+def monomer_two_electron(space, coeffs, V_block, c):
+    """sum_pqrs V_pqrs rho^ccaa_IJ[p,q,s,r] for all state pairs of charge c (FP64)."""
+    z = coeffs[c].contiguous()
+    n = z.shape[0]
+    zT = z.t().contiguous()
+    s2 = SigmaTwoElectron(space, c, n, V_block)
+    s2.run_sigma(zT)
+    out = torch.zeros((n, n), dtype=torch.float64, device=space.device)
+    g = GroupedGemm(space.device)
+    nconf = space.n_conf[c]
+    splitk = max(1, min(64, nconf // 512))
+    g.add(n, n, [(z, nconf, s2.sigmaT, nconf, nconf, 1.0)], out, n, mode=1, splitk=splitk)
+    g.finalize().run()
+    return out
+
+
+def _product_offsets(n_states, charges):
+    off, acc = {}, 0
+    for c in charges:
+        off[c] = acc
+        acc += n_states[c]
+    return off, acc
+
+
+class XRDimerPlan:
+    """Planned order-0 XR-H build of a dimer (fragments 0 and 1, S = 1 integrals).
+
+    spaces:   two FragmentSpace objects (resident coupling lists)
+    n_states: two {charge: number of states}
+    charges:  two charge lists (also the state order of each fragment's H1 and of the
+              product basis, as monomer_charges in get_xr_result.py:76-79)
+    ints:     DeviceIntegrals
+    output:   'split' -> (H1 list, H2) as get_xr_H returns them;
+              'full'  -> H = H2 + H1 x 1 + 1 x H1 (mains/workflow.py:216-230)
+    convention: 'hermitian' (diagram phases of hermitian-XRCC) or 'general' (the sign
+              convention of general-XRCC/build_H.py:68, charge-transfer blocks differ by
+              the gauge (-1)^(n_i1 + n_j0)).
+    """
+
+    def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
+                 convention="hermitian", nuc=0.0):
+        self.spaces, self.charges = spaces, [list(c) for c in charges]
+        self.n_states = [dict(n) for n in n_states]
+        self.ints = ints
+        self.output, self.convention = output, convention
+        self.precision = _lib.PRECISIONS[precision]
+        self.device = spaces[0].device
+        dev = self.device
+        self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=precision) for m in (0, 1)]
+        N = [spaces[0].N, spaces[1].N]
+        self.N = N
+        rho = [b.rho for b in self.builders]
+        f64 = dict(dtype=torch.float64, device=dev)
+
+        # ---- integral matrices in B-role layout [x, y] (y contracted, contiguous) ----
+        W = {}
+        W["v0101"] = (4.0 * ints.V(0, 1, 0, 1).permute(1, 3, 0, 2).reshape(N[1] ** 2, N[0] ** 2)).contiguous()
+        for m, o in ((0, 1), (1, 0)):
+            h_mo = ints.T(m, o) + ints.U(m, m, o) + ints.U(o, m, o)
+            W[("h1", m)] = h_mo.t().contiguous()                                                   # [q, p]
+            W[("cca", m)] = (-2.0 * ints.V(m, m, m, o).permute(3, 0, 1, 2).reshape(N[o], N[m] ** 3)).contiguous()
+            W[("caa", m)] = (2.0 * ints.V(m, o, m, m).permute(1, 0, 3, 2).reshape(N[o], N[m] ** 3)).contiguous()
+            W[("cc", m)] = ints.V(m, m, o, o).permute(3, 2, 0, 1).reshape(N[o] ** 2, N[m] ** 2).contiguous()
+            W[("hmm", m)] = (ints.T(m, m) + ints.U(m, m, m)).reshape(1, N[m] ** 2).contiguous()
+            W[("u100", m)] = ints.U(o, m, m).reshape(1, N[m] ** 2).contiguous()
+        self.W = W
+
+        # ---- precontraction buffers and tasks ----
+        pre = GroupedGemm(dev)
+        self.P = {}
+        chg = self.charges
+        ns = self.n_states
+        for c in chg[0]:
+            if ("ca", c, c) in spaces[0].couplings:
+                n2 = ns[0][c] ** 2
+                buf = torch.empty((n2, N[1] ** 2), **f64)
+                pre.add(n2, N[1] ** 2, [(rho[0]["ca"][(c, c)], N[0] ** 2, W["v0101"], N[0] ** 2, N[0] ** 2, 1.0)],
+                        buf, N[1] ** 2)
+                self.P[("v0101", c)] = buf
+        for m, o in ((0, 1), (1, 0)):
+            for (op, bc, kc) in spaces[m].couplings:
+                nbk = ns[m][bc] * ns[m][kc]
+                if op == "c":        # bra - ket = -1: P1 = rho^c h + rho^cca (-2V)
+                    buf = torch.empty((nbk, N[o]), **f64)
+                    segs = [(rho[m]["c"][(bc, kc)], N[m], W[("h1", m)], N[m], N[m], 1.0)]
+                    if ("cca", bc, kc) in spaces[m].couplings:
+                        segs.append((rho[m]["cca"][(bc, kc)], N[m] ** 3, W[("cca", m)], N[m] ** 3, N[m] ** 3, 1.0))
+                    pre.add(nbk, N[o], segs, buf, N[o])
+                    self.P[("p1", m, bc, kc)] = buf
+                elif op == "caa":
+                    buf = torch.empty((nbk, N[o]), **f64)
+                    pre.add(nbk, N[o], [(rho[m]["caa"][(bc, kc)], N[m] ** 3, W[("caa", m)], N[m] ** 3, N[m] ** 3, 1.0)],
+                            buf, N[o])
+                    self.P[("pcaa", m, bc, kc)] = buf
+                elif op == "cc":
+                    buf = torch.empty((nbk, N[o] ** 2), **f64)
+                    pre.add(nbk, N[o] ** 2, [(rho[m]["cc"][(bc, kc)], N[m] ** 2, W[("cc", m)], N[m] ** 2, N[m] ** 2, 1.0)],
+                            buf, N[o] ** 2)
+                    self.P[("pcc", m, bc, kc)] = buf
+        # monomer pieces: H1 (e1 + e2) and u100 (du); atomically accumulated (mode 1)
+        self.H1blk = [{}, {}]
+        self.DU = [{}, {}]
+        self.FULLD = [{}, {}]
+        self.sigma = [{}, {}]
+        for m, o in ((0, 1), (1, 0)):
+            for c in chg[m]:
+                if ("ca", c, c) not in spaces[m].couplings:
+                    continue
+                n = ns[m][c]
+                ca = rho[m]["ca"][(c, c)]
+                h1 = torch.zeros((n * n, 1), **f64)
+                du = torch.zeros((n * n, 1), **f64)
+                fd = torch.zeros((n * n, 1), **f64)
+                self.H1blk[m][c], self.DU[m][c], self.FULLD[m][c] = h1, du, fd
+                sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m), precision=self.precision)
+                self.sigma[m][c] = sg
+                nconf = spaces[m].n_conf[c]
+                splitk = max(1, min(64, nconf // 512))
+                z = self.builders[m].zT[c]     # (nconf, n): need Z rows (n, nconf) -> separate buffer
+                zrow = torch.empty((n, nconf), **f64)
+                sg.zrow = zrow
+                targets = [h1, fd] if output == "full" else [h1]
+                for tgt in targets:
+                    pre.add(n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1, mode=1)
+                    pre.add(n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n, mode=1, splitk=splitk)
+                for tgt in ([du, fd] if output == "full" else [du]):
+                    pre.add(n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1, mode=1)
+                del z
+        self.pre = pre.finalize()
+
+        # ---- final tasks: one per output charge block ----
+        nb = [ns[m] for m in (0, 1)]
+        off0, tot0 = _product_offsets(nb[0], chg[0])
+        off1, tot1 = _product_offsets(nb[1], chg[1])
+        self.dim = (tot0 * tot1, tot0 * tot1)
+        self.tot = (tot0, tot1)
+        self.H = torch.zeros(self.dim, **f64)
+        fin = GroupedGemm(dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        n_ref0 = spaces[0].n_elec_ref
+        n_ref1 = spaces[1].n_elec_ref
+        self.block_keys = []
+        for ci0 in chg[0]:
+            for ci1 in chg[1]:
+                for cj0 in chg[0]:
+                    for cj1 in chg[1]:
+                        if ci0 + ci1 != cj0 + cj1:
+                            continue
+                        d0 = ci0 - cj0
+                        if abs(d0) > 2:
+                            continue
+                        sgn = -1.0 if ((n_ref0 - cj0) % 2) else 1.0
+                        if convention == "general" and abs(d0) == 1:
+                            sign2 = -1.0 if ((n_ref1 - ci1) % 2) else 1.0
+                            gauge = sign2 * sgn
+                        else:
+                            gauge = 1.0
+                        k0, k1 = (ci0, cj0), (ci1, cj1)
+                        segs = []
+                        try:
+                            if d0 == 0:
+                                segs.append((self.P[("v0101", ci0)], N[1] ** 2, rho[1]["ca"][k1], N[1] ** 2, N[1] ** 2, 1.0))
+                            elif d0 == -1:
+                                segs.append((self.P[("p1", 0, ci0, cj0)], N[1], rho[1]["a"][k1], N[1], N[1], sgn))
+                                segs.append((rho[0]["c"][k0], N[0], self.P[("pcaa", 1, ci1, cj1)], N[0], N[0], -sgn))
+                            elif d0 == 1:
+                                segs.append((rho[0]["a"][k0], N[0], self.P[("p1", 1, ci1, cj1)], N[0], N[0], -sgn))
+                                segs.append((self.P[("pcaa", 0, ci0, cj0)], N[1], rho[1]["c"][k1], N[1], N[1], sgn))
+                            elif d0 == -2:
+                                segs.append((self.P[("pcc", 0, ci0, cj0)], N[1] ** 2, rho[1]["aa"][k1], N[1] ** 2, N[1] ** 2, 1.0))
+                            elif d0 == 2:
+                                segs.append((rho[0]["aa"][k0], N[0] ** 2, self.P[("pcc", 1, ci1, cj1)], N[0] ** 2, N[0] ** 2, 1.0))
+                        except KeyError:
+                            continue     # a density is absent (charge not present): block is zero
+                        segs = [(A, lda, B, ldb, K, a * gauge) for (A, lda, B, ldb, K, a) in segs]
+                        ni0, nj0, ni1, nj1 = nb[0][ci0], nb[0][cj0], nb[1][ci1], nb[1][cj1]
+                        M, Nn = ni0 * nj0, ni1 * nj1
+                        i0 = np.repeat(np.arange(ni0), nj0)
+                        j0 = np.tile(np.arange(nj0), ni0)
+                        i1 = np.repeat(np.arange(ni1), nj1)
+                        j1 = np.tile(np.arange(nj1), ni1)
+                        rowA = torch.as_tensor((off0[ci0] + i0) * tot1, **i32)
+                        colA = torch.as_tensor((off0[cj0] + j0) * tot1, **i32)
+                        rowB = torch.as_tensor(off1[ci1] + i1, **i32)
+                        colB = torch.as_tensor(off1[cj1] + j1, **i32)
+                        diagA = torch.as_tensor(((ci0 == cj0) & (i0 == j0)).astype(np.uint8), device=dev)
+                        diagB = torch.as_tensor(((ci1 == cj1) & (i1 == j1)).astype(np.uint8), device=dev)
+                        DA = DB = None
+                        if d0 == 0:
+                            src = self.FULLD if output == "full" else self.DU
+                            DA = src[0].get(ci0)
+                            DB = src[1].get(ci1)
+                        fin.add(M, Nn, segs, self.H, self.dim[1], mode=2,
+                                maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB)
+                        self.block_keys.append((ci0, ci1, cj0, cj1))
+        self.fin = fin.finalize()
+        if nuc:
+            raise NotImplementedError("nuclear repulsion constants are added by the caller")
+
+    # ------------------------------------------------------------------------------------
+    def build(self, coeffs):
+        """coeffs: two {charge: CUDA float64 (n_states, n_conf)} dicts -> fills self.H (and H1)."""
+        for m in (0, 1):
+            self.builders[m].build(coeffs[m])
+            for c, sg in self.sigma[m].items():
+                sg.zrow.copy_(coeffs[m][c])
+                sg.run_sigma(self.builders[m].zT[c])
+                self.H1blk[m][c].zero_()
+                self.DU[m][c].zero_()
+                self.FULLD[m][c].zero_()
+        self.pre.run()
+        self.fin.run()
+        return self.H
+
+    def H1(self):
+        out = []
+        for m in (0, 1):
+            tot = self.tot[m]
+            h = torch.zeros((tot, tot), dtype=torch.float64, device=self.device)
+            acc = 0
+            for c in self.charges[m]:
+                n = self.n_states[m][c]
+                if c in self.H1blk[m]:
+                    h[acc:acc + n, acc:acc + n] = self.H1blk[m][c].view(n, n)
+                acc += n
+            out.append(h)
+        return out
+
+    @property
+    def flops(self):
+        return self.pre.flops + self.fin.flops
+
+
+def lowest_eigenpairs(H, k=5):
+    """Lowest k eigenvalues/vectors of the symmetric excitonic H in FP64 on the GPU."""
+    w, v = torch.linalg.eigh(0.5 * (H + H.t()))
+    return w[:k], v[:, :k]
