@@ -100,17 +100,19 @@ int xrh_sigma2e(int precision, int n_orbs, const double* V_dev,
  *              acc + (diagB[n] ? DA[m] : 0) + (diagA[m] ? DB[n] : 0)
  *           (charge-block to product-state scatter with the delta-function terms,
  *            hermitian-XRCC/XR_term.py:36-94, get_xr_result.py:300-353)
+ * Operand storage per segment (flags): bit 0 clear: A[m,k] = A[m*lda + k]; set: A[k*lda + m].
+ * bit 1 clear: B[n,k] = B[n*ldb + k]; set: B[k*ldb + n].  A task covers `batch`
+ * independent problems: problem b uses A + b*sA, B + b*sB (per segment) and C + b*sC.
  * tasks_dev / segs_dev are device arrays of the structs below; tile_begin of every task
- * and total_tiles come from the host (tiles are 64x64 for XRH_FP64, 128x128 for the
- * tensor-core precisions, times splitk).  For XRH_BF16X3 / XRH_TF32X3 the segment
- * operands must first be split with xrh_split_operand and described by tensor maps; see
- * xrh_gemm_tc_grouped. */
+ * and total_tiles come from the host (64x64 tiles for XRH_FP64, times splitk, times batch). */
 typedef struct {
     const double* A;
     const double* B;
     int64_t lda, ldb;
     int64_t K;
     double alpha;
+    int64_t flags;
+    int64_t sA, sB;
 } xrh_gemm_segment;
 
 typedef struct {
@@ -129,10 +131,45 @@ typedef struct {
     const double* DB;
     const uint8_t* diagA;
     const uint8_t* diagB;
+    int64_t batch;
+    int64_t sC;
 } xrh_gemm_task;
 
 int xrh_gemm_fp64_grouped(const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
                           const xrh_gemm_segment* segs_dev, void* stream);
+
+/* FP64 Lanczos building blocks for the lowest eigenpairs of H (replaces the dense
+ * scipy.linalg.eig of hermitian-XRCC/mains/workflow.py:229 and
+ * StateSpaceOptimizer/state_gradients.py:107 for the eigenpairs the optimizer uses):
+ *   xrh_gemv_rows: y[i] = alpha * sum_j A[i*lda+j] x[j] + beta * y[i],  i < rows
+ *   xrh_gemv_cols: y[j] += scale * sum_i c[i] A[i*lda+j],                j < cols
+ *   xrh_lanczos_normalize: *beta = ||w||_2, v = w / *beta (v = 0 when w = 0). */
+int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* x_dev,
+                  double alpha, double beta, double* y_dev, void* stream);
+int xrh_gemv_cols(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* c_dev,
+                  double scale, double* y_dev, void* stream);
+int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double* beta_dev, void* stream);
+
+/* Adjoint of the density build (dE/dz from dE/drho), the reverse of xrh_density_accumulate
+ * over the same coupling lists; replaces the determinant-bra density rebuild plus second H
+ * build of StateSpaceOptimizer/state_gradients.py:164-185.  gT_dev is dE/drho in
+ * [K, n_b, n_k] layout; results are ADDED (atomically) to gzbT_dev [n_bra_conf, n_b] and
+ * gzkT_dev [n_ket_conf, n_k], which may be the same buffer.  precision XRH_FP64 or XRH_FP32. */
+int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev,
+                        const int32_t* P_dev, const int32_t* Q_dev, const int8_t* sign_dev,
+                        const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
+                        const double* gT_dev, double* gzbT_dev, double* gzkT_dev, void* stream);
+
+/* Two-particle density of a weighted ensemble for the monomer two-electron term:
+ *   Gamma[p,q,r,s] += sum_{P,Q} W[P,Q] <P| c+_p c+_q a_s a_r |Q>,  p<q and r<s only,
+ *   W[P,Q] = sum_I zbT[P, I] YT[Q, I]   (Y = G . z for weights G over state pairs)
+ * i.e. dE/dV for E = sum_IJ G_IJ sum_pqrs V_pqrs rho^ccaa_IJ[p,q,s,r] (orb_grads.py:921
+ * two_p_dens for the intra-fragment term) without the N^4 density.  Gamma_dev is N^4
+ * (N = 2 n_orbs), accumulated atomically; the caller fills the other index orders by
+ * antisymmetry.  n <= 256 states. */
+int xrh_ccaa_weighted(int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
+                      const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev, int n_ket_conf,
+                      const double* zbT_dev, const double* YT_dev, int n, double* Gamma_dev, void* stream);
 
 #ifdef __cplusplus
 }

@@ -604,3 +604,65 @@ def h_element(name, *args):
         n1, n2, n3, Rca1, Rc2, Ra3, V = args
         return float(4 * np.einsum("prqs,pq,r,s->", V.reshape(n1, n2, n1, n3), Rca1.reshape(n1, n1), Rc2, Ra3))
     raise NotImplementedError(name)
+
+
+# ----------------------------------------------------------------------------------------
+# energies and the reference's state-gradient formula (checkers for the adjoint)
+# ----------------------------------------------------------------------------------------
+
+def xr_energy(h, V, Ns, n_orb, n_core, n_elec_ref, states, charges):
+    """Lowest eigenvalue and eigenvector of the full order-0 XR H for fragment states
+    states[m][chg] = (coeffs, masks) (coefficients need not be orthonormal)."""
+    ints = FragInts(h, V, Ns)
+    dens = [build_densities({c: Sector(*states[m][c]) for c in charges}, n_orb, n_core, n_elec_ref)
+            for m in range(2)]
+    H1, H2 = get_xr_H0(ints, dens, [list(charges), list(charges)])
+    H = full_H(H1, H2)
+    w, v = np.linalg.eigh(0.5 * (H + H.T))
+    return w[0], v[:, 0], H1, H2
+
+
+def reference_state_gradient_herm(h, V, Ns, n_orb, n_core, n_elec_ref, states, charges, frag=0):
+    """The 'herm' state gradient of StateSpaceOptimizer/state_gradients.py:121-244 restated
+    by brute force: for fragment A = frag, G[k, P] = sum_l d[k,l] <P (x) l| H - E |Psi>,
+    where P runs over A's determinants and l over the other fragment's states
+    (state_gradients.py:205-216: monomer H term with determinant bras, E term with the
+    adapted overlaps, dimer term with bra_det densities, other fragment's H1 term).
+    The bra-determinant Hamiltonian is built with complete determinant bases on A (the
+    'bra_det' densities of Be-states/densities.py:107-113) and contracted with the states
+    on the ket side.  Returns {chg: (n_states, n_conf)}."""
+    E, d, _, _ = xr_energy(h, V, Ns, n_orb, n_core, n_elec_ref, states, charges)
+    A, B = frag, 1 - frag
+    det_states = [dict(s) for s in states]
+    det_states[A] = {c: (np.eye(len(states[A][c][1])), states[A][c][1]) for c in charges}
+    ints = FragInts(h, V, Ns)
+    dens = [build_densities({c: Sector(*det_states[m][c]) for c in charges}, n_orb, n_core, n_elec_ref)
+            for m in range(2)]
+    H1, H2 = get_xr_H0(ints, dens, [list(charges), list(charges)])
+    Hdet = full_H(H1, H2)
+    nA_det = [len(states[A][c][1]) for c in charges]
+    nA = [states[A][c][0].shape[0] for c in charges]
+    nB = sum(states[B][c][0].shape[0] for c in charges)
+    Zt = np.zeros((sum(nA_det), sum(nA)))      # det x state, block diagonal by charge
+    r0 = c0 = 0
+    for c, nd, ns_ in zip(charges, nA_det, nA):
+        Zt[r0:r0 + nd, c0:c0 + ns_] = states[A][c][0].T
+        r0 += nd
+        c0 += ns_
+    if A == 0:
+        Smix = np.kron(Zt, np.eye(nB))
+        Dm = d.reshape(sum(nA), nB)
+    else:
+        Smix = np.kron(np.eye(nB), Zt)
+        Dm = d.reshape(nB, sum(nA)).T
+    Hmix = Hdet @ Smix
+    r = (Hmix - E * Smix) @ d
+    R = r.reshape(sum(nA_det), nB) if A == 0 else r.reshape(nB, sum(nA_det)).T   # [P, l]
+    Gfull = Dm @ R.T                                                                # [k, P]
+    out = {}
+    r0 = c0 = 0
+    for c, nd, ns_ in zip(charges, nA_det, nA):
+        out[c] = Gfull[c0:c0 + ns_, r0:r0 + nd]
+        r0 += nd
+        c0 += ns_
+    return out, E

@@ -32,6 +32,11 @@ _SIGS = {
     "xrh_transpose": (_i32, [_vp, _i64, _i64, _vp, _vp]),
     "xrh_sigma2e": (_i32, [_i32, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_gemm_fp64_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
+    "xrh_gemv_rows": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _dbl, _vp, _vp]),
+    "xrh_gemv_cols": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _vp, _vp]),
+    "xrh_lanczos_normalize": (_i32, [_i64, _vp, _vp, _vp, _vp]),
+    "xrh_density_adjoint": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
+    "xrh_ccaa_weighted": (_i32, [_i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
 }
 _OPTIONAL = {}
 
@@ -66,7 +71,18 @@ def register(name, restype, argtypes):
         f.argtypes = argtypes
 
 
+class LaunchCounter:
+    """Counts library calls that launch one kernel each (the gpu_launches figure)."""
+    launching = {"xrh_density_accumulate", "xrh_transpose", "xrh_sigma2e", "xrh_gemm_fp64_grouped",
+                 "xrh_couplings_count", "xrh_couplings_fill", "xrh_gemv_rows", "xrh_gemv_cols",
+                 "xrh_lanczos_normalize", "xrh_density_adjoint", "xrh_ccaa_weighted"}
+    count = 0
+
+
 def call(name, *args):
+    """Call one ABI function; raise XRHError on a non-zero status."""
+    if name in LaunchCounter.launching:
+        LaunchCounter.count += 1
     st = getattr(lib(), name)(*args)
     if st != XRH_OK:
         msg = lib().xrh_status_string(st).decode()
@@ -94,10 +110,12 @@ def op_code(op):
 
 # numpy mirrors of the ABI structs (field order and sizes match include/xrh.h)
 SEGMENT_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("lda", np.int64), ("ldb", np.int64),
-                          ("K", np.int64), ("alpha", np.float64)])
+                          ("K", np.int64), ("alpha", np.float64), ("flags", np.int64), ("sA", np.int64),
+                          ("sB", np.int64)])
 TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
                        ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("C", np.uint64),
                        ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64), ("rowB", np.uint64),
                        ("colB", np.uint64), ("DA", np.uint64), ("DB", np.uint64), ("diagA", np.uint64),
-                       ("diagB", np.uint64)])
-assert SEGMENT_DTYPE.itemsize == 48 and TASK_DTYPE.itemsize == 136
+                       ("diagB", np.uint64), ("batch", np.int64), ("sC", np.int64)])
+assert SEGMENT_DTYPE.itemsize == 72 and TASK_DTYPE.itemsize == 152
+

@@ -25,5 +25,5 @@ extern "C" int xrh_last_cuda_error(void) {
     return g_last_cuda_error;
 }
 
-static_assert(sizeof(xrh_gemm_segment) == 48, "xrh_gemm_segment layout is part of the ABI");
-static_assert(sizeof(xrh_gemm_task) == 136, "xrh_gemm_task layout is part of the ABI");
+static_assert(sizeof(xrh_gemm_segment) == 72, "xrh_gemm_segment layout is part of the ABI");
+static_assert(sizeof(xrh_gemm_task) == 152, "xrh_gemm_task layout is part of the ABI");

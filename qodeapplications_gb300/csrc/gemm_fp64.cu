@@ -34,6 +34,9 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
     const xrh_gemm_task& T = tasks[t_id];
     const int64_t tiles_m = (T.M + BM - 1) / BM, tiles_n = (T.N + BN - 1) / BN;
     int64_t local = tile - T.tile_begin;
+    const int64_t per_batch = tiles_m * tiles_n * T.splitk;
+    const int64_t bidx = local / per_batch;
+    local -= bidx * per_batch;
     const int64_t split = local / (tiles_m * tiles_n);
     local -= split * tiles_m * tiles_n;
     const int64_t m0 = (local / tiles_n) * BM, n0 = (local % tiles_n) * BN;
@@ -46,6 +49,9 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 
     for (int64_t s = T.seg_begin; s < T.seg_begin + T.seg_count; ++s) {
         const xrh_gemm_segment S = segs[s];
+        const double* __restrict__ Ap = S.A + bidx * S.sA;
+        const double* __restrict__ Bp = S.B + bidx * S.sB;
+        const bool at = (S.flags & 1) != 0, bt = (S.flags & 2) != 0;
         int64_t kb = 0, ke = S.K;
         if (T.splitk > 1) {
             const int64_t per = (S.K + T.splitk - 1) / T.splitk;
@@ -62,11 +68,19 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 #pragma unroll
             for (int e = 0; e < (BM * BK) / NT; ++e) {
                 const int l = threadIdx.x + e * NT;
+                // K-contiguous operands: consecutive threads walk k; otherwise they walk m / n
                 const int r = l / BK, c = l % BK;
-                const int64_t gm = m0 + r, gk = k0 + c;
-                As[c][r] = (gm < T.M && gk < ke) ? S.A[gm * S.lda + gk] : 0.0;
-                const int64_t gn = n0 + r;
-                Bs[c][r] = (gn < T.N && gk < ke) ? S.B[gn * S.ldb + gk] : 0.0;
+                const int r2 = l % BM, c2 = l / BM;
+                {
+                    const int rr = at ? r2 : r, cc = at ? c2 : c;
+                    const int64_t gm = m0 + rr, gk = k0 + cc;
+                    As[cc][rr] = (gm < T.M && gk < ke) ? (at ? Ap[gk * S.lda + gm] : Ap[gm * S.lda + gk]) : 0.0;
+                }
+                {
+                    const int rr = bt ? r2 : r, cc = bt ? c2 : c;
+                    const int64_t gn = n0 + rr, gk = k0 + cc;
+                    Bs[cc][rr] = (gn < T.N && gk < ke) ? (bt ? Bp[gk * S.ldb + gn] : Bp[gn * S.ldb + gk]) : 0.0;
+                }
             }
             __syncthreads();
 #pragma unroll
@@ -97,14 +111,15 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
             const int64_t n = n0 + tx + 16 * j;
             if (n >= T.N) continue;
             double v = acc[i][j];
+            double* Cb = T.C + bidx * T.sC;
             if (T.mode == 0) {
-                T.C[m * T.ldc + n] = v;
+                Cb[m * T.ldc + n] = v;
             } else if (T.mode == 1) {
-                atomicAdd(T.C + m * T.ldc + n, v);
+                atomicAdd(Cb + m * T.ldc + n, v);
             } else {
                 if (T.DA && T.diagB[n]) v += T.DA[m];
                 if (T.DB && T.diagA[m]) v += T.DB[n];
-                T.C[((int64_t)T.rowA[m] + T.rowB[n]) * T.ldc + T.colA[m] + T.colB[n]] = v;
+                Cb[((int64_t)T.rowA[m] + T.rowB[n]) * T.ldc + T.colA[m] + T.colB[n]] = v;
             }
         }
     }

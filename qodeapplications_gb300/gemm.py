@@ -24,21 +24,29 @@ class GroupedGemm:
         self.total_tiles = 0
         self.flops = 0.0         # algorithmic FLOPs of one launch (2*M*N*K per segment)
 
-    def add(self, M, N, segments, C, ldc, mode=0, splitk=1, maps=None, DA=None, DB=None):
-        """segments: list of (A, lda, B, ldb, K, alpha) with A, B torch CUDA float64 tensors
-        (row-major, K contiguous).  maps: (rowA, colA, rowB, colB, diagA, diagB) for mode 2."""
-        if M <= 0 or N <= 0:
+    def add(self, M, N, segments, C, ldc, mode=0, splitk=1, maps=None, DA=None, DB=None, batch=1, sC=0):
+        """segments: list of (A, lda, B, ldb, K, alpha[, flags, sA, sB]) with A, B torch CUDA
+        float64 tensors.  flags bit 0: A stored [k][m] (else [m][k]); bit 1: B stored [k][n]
+        (else [n][k]).  batch > 1 repeats the problem with pointer strides sA, sB, sC.
+        maps: (rowA, colA, rowB, colB, diagA, diagB) for mode 2."""
+        if M <= 0 or N <= 0 or batch <= 0:
             return
         seg_begin = len(self._segs)
-        for A, lda, B, ldb, K, alpha in segments:
+        for seg in segments:
+            A, lda, B, ldb, K, alpha = seg[:6]
+            flags, sA, sB = (seg[6], seg[7], seg[8]) if len(seg) > 6 else (0, 0, 0)
             assert A.dtype == torch.float64 and B.dtype == torch.float64 and A.is_cuda and B.is_cuda
             assert A.is_contiguous() and B.is_contiguous()
-            assert A.numel() >= (M - 1) * lda + K and B.numel() >= (N - 1) * ldb + K, "operand too small"
-            self._segs.append((A.data_ptr(), B.data_ptr(), lda, ldb, K, float(alpha)))
+            a_need = (batch - 1) * sA + ((K - 1) * lda + M if flags & 1 else (M - 1) * lda + K)
+            b_need = (batch - 1) * sB + ((K - 1) * ldb + N if flags & 2 else (N - 1) * ldb + K)
+            assert A.numel() >= a_need and B.numel() >= b_need, "operand too small"
+            self._segs.append((A.data_ptr(), B.data_ptr(), lda, ldb, K, float(alpha), flags, sA, sB))
             self._keep += [A, B]
-            self.flops += 2.0 * M * N * K
+            self.flops += 2.0 * M * N * K * batch
+        if mode != 2:
+            assert C.numel() >= (batch - 1) * sC + (M - 1) * ldc + N, "output too small"
         t = dict(M=M, N=N, seg_begin=seg_begin, seg_count=len(segments), mode=mode, splitk=splitk,
-                 C=C.data_ptr(), ldc=ldc)
+                 C=C.data_ptr(), ldc=ldc, batch=batch, sC=sC)
         self._keep.append(C)
         if mode == 2:
             rowA, colA, rowB, colB, diagA, diagB = maps
@@ -57,7 +65,7 @@ class GroupedGemm:
             for k, v in t.items():
                 tasks[i][k] = v
             tasks[i]["tile_begin"] = begin
-            begin += ((t["M"] + tile - 1) // tile) * ((t["N"] + tile - 1) // tile) * t["splitk"]
+            begin += ((t["M"] + tile - 1) // tile) * ((t["N"] + tile - 1) // tile) * t["splitk"] * t["batch"]
         self.total_tiles = begin
         segs = np.zeros(len(self._segs), dtype=SEGMENT_DTYPE)
         for i, s in enumerate(self._segs):

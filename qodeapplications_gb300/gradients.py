@@ -1,0 +1,265 @@
+"""Adjoint of the XR-H build: energy gradients w.r.t. fragment-state coefficients and
+orbital rotations, on the GPU.
+
+What the reference computes (StateSpaceOptimizer/state_gradients.py:121-244 for the states,
+orb_grads.py:976-1000 for the orbitals) is re-derived as one reverse pass of the planned
+build.  With d the normalised ground-state eigenvector of the symmetric excitonic H and
+E = d^T H d (Hellmann-Feynman), every planned contraction is differentiated in reverse:
+
+  final blocks    C = sum_s alpha_s A_s B_s^T scattered to H  ->  dE/dA_s, dE/dB_s
+                  (two small GEMMs each with the ground-state coefficient matrix D)
+  delta terms     u100, H1 x 1, 1 x H1                        ->  G_m = D D^T / D^T D blocks
+  precontractions P = rho W^T                                 ->  dE/drho, dE/dW
+  densities       rho = zb O zk^T (coupling lists)            ->  dE/dz (xrh_density_adjoint)
+  monomer 2e      zb M2 zk^T (sigma vectors)                  ->  dE/dz, dE/dV_mmmm (xrh_ccaa_weighted)
+
+dE/dW, dE/dT, dE/dU, dE/dV then give the orbital-rotation gradient by the chain rule of
+X' = R^T X R (R = exp(kappa), at kappa = 0 on the current orbitals).  All FP64.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr, stream_ptr
+from .gemm import GroupedGemm
+from .hamiltonian import _Arena, _splitk
+
+
+class XRDimerAdjoint:
+    def __init__(self, plan):
+        assert plan.output == "full", "the adjoint differentiates the full H (H2 + H1 x 1 + 1 x H1)"
+        self.plan = plan
+        dev = plan.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        tot0, tot1 = plan.tot
+        self.d = torch.zeros(tot0 * tot1, **f64)
+        Dflat = self.d
+        off0, off1 = plan.offsets
+        ns, chg, N = plan.n_states, plan.charges, plan.N
+
+        arena = _Arena(dev)
+        req = {}
+
+        def want(key, shape):
+            if key not in req:
+                req[key] = arena.request(shape)
+
+        # gradients of every operand that appears in the plan
+        operands = {}
+        for t in plan.final_tasks:
+            for (A, lda, B, ldb, K, a) in t["segs"]:
+                operands[A.data_ptr()] = A
+                operands[B.data_ptr()] = B
+        for out, segs in plan.pre_specs:
+            operands[out.data_ptr()] = out
+            for rho_t, _wk in segs:
+                operands[rho_t.data_ptr()] = rho_t
+        for m in (0, 1):
+            for c in plan.H1blk[m]:
+                operands[plan.builders[m].rho["ca"][(c, c)].data_ptr()] = plan.builders[m].rho["ca"][(c, c)]
+        for p_, t_ in operands.items():
+            want(("g", p_), tuple(t_.shape))
+        for wk, Wt in plan.W.items():
+            want(("gW", wk), tuple(Wt.shape))
+        for m in (0, 1):
+            want(("gmono1", m), (1, N[m] ** 2))
+            want(("Gamma", m), (N[m] ** 4,))
+            for c in plan.charges[m]:
+                want(("gzT", m, c), (plan.spaces[m].n_conf[c], ns[m][c]))
+                if c in plan.H1blk[m]:
+                    want(("gblk", m, c), (ns[m][c], ns[m][c]))
+                    want(("YT", m, c), (plan.spaces[m].n_conf[c], ns[m][c]))
+        for i, t in enumerate(plan.final_tasks):
+            ni0, nj0, ni1, nj1 = t["dims"]
+            for s, (A, lda, B, ldb, K, a) in enumerate(t["segs"]):
+                want(("Y", i, s), (ni0, nj1 * K))
+                want(("Z", i, s), (ni1, nj0 * K))
+        views = arena.allocate()
+        self.arena = arena
+        G = {k: views[v] for k, v in req.items()}
+        self.G = G
+        grad_of = {p_: G[("g", p_)] for p_ in operands}
+        self.grad_of = grad_of
+
+        # ---- launch 1: G blocks, Y and Z per final segment ----
+        L1 = GroupedGemm(dev)
+        for m in (0, 1):
+            for c in plan.H1blk[m]:
+                n = ns[m][c]
+                gb = G[("gblk", m, c)]
+                if m == 0:      # G0[i,j] = sum_b D[off+i, b] D[off+j, b]
+                    Dsub = Dflat[off0[c] * tot1:]
+                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot1, 1.0)], gb, n)
+                else:           # G1[i,j] = sum_a D[a, off+i] D[a, off+j]
+                    Dsub = Dflat[off1[c]:]
+                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot0, 1.0, 3, 0, 0)], gb, n)
+        self.final_adj = []
+        for i, t in enumerate(plan.final_tasks):
+            ci0, ci1, cj0, cj1 = t["key"]
+            ni0, nj0, ni1, nj1 = t["dims"]
+            Di = Dflat[off0[ci0] * tot1 + off1[ci1]:]     # rows i0, cols i1
+            Dj = Dflat[off0[cj0] * tot1 + off1[cj1]:]     # rows j0, cols j1
+            for s, (A, lda, B, ldb, K, a) in enumerate(t["segs"]):
+                Y, Z = G[("Y", i, s)], G[("Z", i, s)]
+                # Y[i0, (j1,x)] = a sum_i1 D[i0,i1] B[(i1,j1),x]
+                L1.add(ni0, nj1 * K, [(Di, tot1, B, nj1 * K, ni1, a, 2, 0, 0)], Y, nj1 * K)
+                # Z[i1, (j0,x)] = a sum_i0 D[i0,i1] A[(i0,j0),x]
+                L1.add(ni1, nj0 * K, [(Di, tot1, A, nj0 * K, ni0, a, 3, 0, 0)], Z, nj0 * K)
+                self.final_adj.append((A, B, K, Y, Z, Dj, (ni0, nj0, ni1, nj1)))
+        self.L1 = L1.finalize()
+
+        # ---- launch 2: dA, dB (batched), monomer pieces ----
+        L2 = GroupedGemm(dev)
+        for (A, B, K, Y, Z, Dj, (ni0, nj0, ni1, nj1)) in self.final_adj:
+            gA, gB = grad_of[A.data_ptr()], grad_of[B.data_ptr()]
+            # dA[(i0,j0),x] += sum_j1 D[j0,j1] Y[i0,(j1,x)]          (batch over i0)
+            L2.add(nj0, K, [(Dj, tot1, Y, K, nj1, 1.0, 2, 0, nj1 * K)], gA, K, mode=1, batch=ni0, sC=nj0 * K)
+            # dB[(i1,j1),x] += sum_j0 D[j0,j1] Z[i1,(j0,x)]          (batch over i1)
+            L2.add(nj1, K, [(Dj, tot1, Z, K, nj0, 1.0, 3, 0, nj0 * K)], gB, K, mode=1, batch=ni1, sC=nj1 * K)
+        for m in (0, 1):
+            for c in plan.H1blk[m]:
+                n = ns[m][c]
+                gb = G[("gblk", m, c)]
+                ca = plan.builders[m].rho["ca"][(c, c)]
+                gca = grad_of[ca.data_ptr()]
+                N2 = N[m] ** 2
+                # d rho^ca += g (x) (h_mm + U_omm)  (rank one, K = 1)
+                L2.add(n * n, N2, [(gb, 1, plan.W[("hmm", m)], N2, 1, 1.0, 2, 0, 0),
+                                   (gb, 1, plan.W[("u100", m)], N2, 1, 1.0, 2, 0, 0)], gca, N2, mode=1)
+                # d(h_mm) = d(U_omm) += sum_ij g[i,j] rho^ca[i,j,:]
+                L2.add(1, N2, [(gb, n * n, ca, N2, n * n, 1.0, 2, 0, 0)], G[("gmono1", m)], N2, mode=1,
+                       splitk=_splitk(n * n, 256, 16))
+                # e2 = z M2 z^T: dz^T[P, I] += 2 sum_J sigma^T[J, P] g[I, J]
+                sg = plan.sigma[m][c]
+                nconf = plan.spaces[m].n_conf[c]
+                L2.add(nconf, n, [(sg.sigmaT, nconf, gb, n, n, 2.0, 1, 0, 0)], G[("gzT", m, c)], n, mode=1)
+                # Y^T = z^T g^T for the two-particle density of the weighted ensemble
+                L2.add(nconf, n, [(plan.builders[m].zT[c], n, gb, n, n, 1.0)], G[("YT", m, c)], n)
+        self.L2 = L2.finalize()
+
+        # ---- launch 3: precontraction adjoint ----
+        L3 = GroupedGemm(dev)
+        for out, segs in plan.pre_specs:
+            gP = grad_of[out.data_ptr()]
+            M, X = out.shape
+            for rho_t, wk in segs:
+                Wt = plan.W[wk]
+                Yk = Wt.shape[1]
+                grho = grad_of[rho_t.data_ptr()]
+                # d rho[m, y] += sum_x dP[m, x] W[x, y]
+                L3.add(M, Yk, [(gP, X, Wt, Yk, X, 1.0, 2, 0, 0)], grho, Yk, mode=1)
+                # dW[x, y] += sum_m dP[m, x] rho[m, y]
+                L3.add(X, Yk, [(gP, X, rho_t, Yk, M, 1.0, 3, 0, 0)], G[("gW", wk)], Yk, mode=1,
+                       splitk=_splitk(M, 256, 32))
+        self.L3 = L3.finalize()
+
+        # ---- launch 4 inputs: transposed density gradients for the coupling-list adjoint ----
+        self.dens_adj = []
+        for m in (0, 1):
+            b = plan.builders[m]
+            for (op, bc, kc), cp in plan.spaces[m].couplings.items():
+                rt = b.rho[op][(bc, kc)]
+                if rt.data_ptr() not in grad_of:
+                    continue
+                gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
+                self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
+
+    # ------------------------------------------------------------------------------------
+    def launch(self, d):
+        """Enqueue the reverse pass for ground-state vector d (device, product order)."""
+        plan = self.plan
+        s = stream_ptr()
+        if d is not None:
+            self.d.copy_(d)
+        self.arena.buf.zero_()
+        self.L1.run()
+        self.L2.run()
+        self.L3.run()
+        for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
+            nb, nk = rt.shape[0], rt.shape[1]
+            call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
+            call("xrh_density_adjoint", _lib.FP64, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
+                 ptr(plan.builders[m].zbT[bc]), nb, ptr(plan.builders[m].zT[kc]), nk, ptr(gT),
+                 ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
+        for m in (0, 1):
+            sp = plan.spaces[m]
+            for c in plan.H1blk[m]:
+                call("xrh_ccaa_weighted", sp.n_orbs, ptr(sp.masks[c]), sp.n_conf[c], ptr(sp.sorted_masks[c]),
+                     ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]),
+                     plan.n_states[m][c], ptr(self.G[("Gamma", m)]), s)
+
+    # ---------------------------------------------------------------------- results ---
+    def state_gradient(self):
+        """dE/dz[m][charge] (n_states x n_conf), the unconstrained derivative of the lowest
+        eigenvalue w.r.t. the CI coefficients (bra and ket occurrences)."""
+        return [{c: self.G[("gzT", m, c)].t() for c in self.plan.charges[m]} for m in (0, 1)]
+
+    def integral_gradients(self):
+        """dE/dT, dE/dU, dE/dV as supersystem spin-orbital tensors (device)."""
+        plan = self.plan
+        Ns = plan.N
+        off = [0, Ns[0], Ns[0] + Ns[1]]
+        tot = off[-1]
+        dev = plan.device
+        dT = torch.zeros((tot, tot), dtype=torch.float64, device=dev)
+        dU = torch.zeros((2, tot, tot), dtype=torch.float64, device=dev)
+        dV = torch.zeros((tot,) * 4, dtype=torch.float64, device=dev)
+        sl = [slice(off[m], off[m + 1]) for m in (0, 1)]
+        G = self.G
+        gw = G[("gW", "v0101")].view(Ns[1], Ns[1], Ns[0], Ns[0])
+        dV[sl[0], sl[1], sl[0], sl[1]] += 4.0 * gw.permute(2, 0, 3, 1)
+        for m, o in ((0, 1), (1, 0)):
+            dh = G[("gW", ("h1", m))].t()
+            dT[sl[m], sl[o]] += dh
+            dU[m][sl[m], sl[o]] += dh
+            dU[o][sl[m], sl[o]] += dh
+            dV[sl[m], sl[m], sl[m], sl[o]] += -2.0 * G[("gW", ("cca", m))].view(Ns[o], Ns[m], Ns[m], Ns[m]).permute(1, 2, 3, 0)
+            dV[sl[m], sl[o], sl[m], sl[m]] += 2.0 * G[("gW", ("caa", m))].view(Ns[o], Ns[m], Ns[m], Ns[m]).permute(1, 0, 3, 2)
+            dV[sl[m], sl[m], sl[o], sl[o]] += G[("gW", ("cc", m))].view(Ns[o], Ns[o], Ns[m], Ns[m]).permute(2, 3, 1, 0)
+            g1 = G[("gmono1", m)].view(Ns[m], Ns[m])
+            dT[sl[m], sl[m]] += g1
+            dU[m][sl[m], sl[m]] += g1
+            dU[o][sl[m], sl[m]] += g1
+            Gm = G[("Gamma", m)].view(Ns[m], Ns[m], Ns[m], Ns[m])
+            Gf = Gm - Gm.permute(1, 0, 2, 3) - Gm.permute(0, 1, 3, 2) + Gm.permute(1, 0, 3, 2)
+            dV[sl[m], sl[m], sl[m], sl[m]] += Gf
+        return dT, dU, dV
+
+    def orbital_gradient(self, T, U, V, spatial_index):
+        """dE/dkappa (antisymmetric, spatial orbitals) for X' = R^T X R with R = exp(kappa)
+        applied to every integral at kappa = 0.  T (tot x tot), U (n_frag x tot x tot),
+        V (tot^4) are the current spin-orbital integrals on the device; spatial_index[i]
+        is the spatial orbital of spin orbital i."""
+        dT, dU, dV = self.integral_gradients()
+        Gso = T @ dT.t() + T.t() @ dT
+        for k in range(U.shape[0]):
+            Gso += U[k] @ dU[k].t() + U[k].t() @ dU[k]
+        t = V.shape[0]
+        Vm = V.reshape(t, -1)
+        Gso += Vm @ dV.reshape(t, -1).t()                                             # index 1
+        Gso += V.permute(1, 0, 2, 3).reshape(t, -1) @ dV.permute(1, 0, 2, 3).reshape(t, -1).t()
+        Gso += V.permute(2, 0, 1, 3).reshape(t, -1) @ dV.permute(2, 0, 1, 3).reshape(t, -1).t()
+        Gso += V.permute(3, 0, 1, 2).reshape(t, -1) @ dV.permute(3, 0, 1, 2).reshape(t, -1).t()
+        idx = torch.as_tensor(np.asarray(spatial_index), device=T.device)
+        n_sp = int(idx.max().item()) + 1
+        Gsp = torch.zeros((n_sp, n_sp), dtype=torch.float64, device=T.device)
+        # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs
+        Gsp.index_put_((idx[:, None].expand(t, t), idx[None, :].expand(t, t)),
+                       Gso * _same_spin(t, spatial_index, T.device), accumulate=True)
+        return Gsp - Gsp.t()
+
+
+def _same_spin(t, spatial_index, device):
+    """Mask of spin-orbital pairs with the same spin (alpha block then beta block per fragment)."""
+    spins = np.zeros(t, dtype=np.int64)
+    seen = {}
+    for i, sp in enumerate(spatial_index):
+        spins[i] = seen.get(sp, 0)
+        seen[sp] = seen.get(sp, 0) + 1
+    s = torch.as_tensor(spins, device=device)
+    return (s[:, None] == s[None, :]).to(torch.float64)
+
+
+def tangent_project(g, z):
+    """Project dE/dz onto the tangent space of row-orthonormal z (Stiefel manifold)."""
+    return g - 0.5 * (g @ z.t() + z @ g.t()) @ z

@@ -118,6 +118,32 @@ def _product_offsets(n_states, charges):
     return off, acc
 
 
+class _Arena:
+    """One device buffer carved into the accumulation targets of a build, so that a single
+    memset clears every split-K / atomic output before the launches."""
+
+    def __init__(self, device):
+        self.device, self.sizes, self.views, self.buf = device, [], [], None
+
+    def request(self, shape):
+        n = int(np.prod(shape))
+        self.sizes.append((n, tuple(shape)))
+        return len(self.sizes) - 1
+
+    def allocate(self):
+        total = sum(n for n, _ in self.sizes)
+        self.buf = torch.zeros(max(total, 1), dtype=torch.float64, device=self.device)
+        off = 0
+        for n, shape in self.sizes:
+            self.views.append(self.buf[off:off + n].view(shape))
+            off += n
+        return self.views
+
+
+def _splitk(K_total, target=384, cap=32):
+    return int(max(1, min(cap, K_total // target)))
+
+
 class XRDimerPlan:
     """Planned order-0 XR-H build of a dimer (fragments 0 and 1, S = 1 integrals).
 
@@ -131,10 +157,14 @@ class XRDimerPlan:
     convention: 'hermitian' (diagram phases of hermitian-XRCC) or 'general' (the sign
               convention of general-XRCC/build_H.py:68, charge-transfer blocks differ by
               the gauge (-1)^(n_i1 + n_j0)).
+
+    The inputs are the persistent coefficient buffers self.coeffs[m][charge]
+    (n_states x n_conf); launch() enqueues the whole build on the current stream without
+    host synchronisation or allocation, so it can be captured in a CUDA graph.
     """
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
-                 convention="hermitian", nuc=0.0):
+                 convention="hermitian"):
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
         self.ints = ints
@@ -142,11 +172,14 @@ class XRDimerPlan:
         self.precision = _lib.PRECISIONS[precision]
         self.device = spaces[0].device
         dev = self.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.coeffs = [{c: torch.zeros((self.n_states[m][c], spaces[m].n_conf[c]), **f64) for c in self.charges[m]}
+                       for m in (0, 1)]
         self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=precision) for m in (0, 1)]
         N = [spaces[0].N, spaces[1].N]
         self.N = N
         rho = [b.rho for b in self.builders]
-        f64 = dict(dtype=torch.float64, device=dev)
+        chg, ns = self.charges, self.n_states
 
         # ---- integral matrices in B-role layout [x, y] (y contracted, contiguous) ----
         W = {}
@@ -161,73 +194,90 @@ class XRDimerPlan:
             W[("u100", m)] = ints.U(o, m, m).reshape(1, N[m] ** 2).contiguous()
         self.W = W
 
-        # ---- precontraction buffers and tasks ----
-        pre = GroupedGemm(dev)
-        self.P = {}
-        chg = self.charges
-        ns = self.n_states
+        # ---- accumulation targets (one arena, cleared by one memset per build) ----
+        arena = _Arena(dev)
+        req = {}
         for c in chg[0]:
             if ("ca", c, c) in spaces[0].couplings:
+                req[("v0101", c)] = arena.request((ns[0][c] ** 2, N[1] ** 2))
+        for m, o in ((0, 1), (1, 0)):
+            for (op, bc, kc) in spaces[m].couplings:
+                nbk = ns[m][bc] * ns[m][kc]
+                if op == "c":
+                    req[("p1", m, bc, kc)] = arena.request((nbk, N[o]))
+                elif op == "caa":
+                    req[("pcaa", m, bc, kc)] = arena.request((nbk, N[o]))
+                elif op == "cc":
+                    req[("pcc", m, bc, kc)] = arena.request((nbk, N[o] ** 2))
+            for c in chg[m]:
+                if ("ca", c, c) in spaces[m].couplings:
+                    n = ns[m][c]
+                    for kind in ("h1", "du", "fd"):
+                        req[(kind, m, c)] = arena.request((n * n, 1))
+        views = arena.allocate()
+        self.arena = arena
+        self.P = {k: views[i] for k, i in req.items() if k[0] in ("v0101", "p1", "pcaa", "pcc")}
+        self.H1blk = [{c: views[req[("h1", m, c)]] for c in chg[m] if ("h1", m, c) in req} for m in (0, 1)]
+        self.DU = [{c: views[req[("du", m, c)]] for c in chg[m] if ("du", m, c) in req} for m in (0, 1)]
+        self.FULLD = [{c: views[req[("fd", m, c)]] for c in chg[m] if ("fd", m, c) in req} for m in (0, 1)]
+
+        # ---- precontraction tasks (split-K, atomic accumulation into the arena) ----
+        pre = GroupedGemm(dev)
+        self.pre_specs = []       # (output P, [(rho, integral-matrix key)]) for the adjoint
+
+        def add_pre(M, Ncols, segs, out, ldc, wkeys=None):
+            pre.add(M, Ncols, segs, out, ldc, mode=1, splitk=_splitk(sum(sg[4] for sg in segs)))
+            if wkeys is not None:
+                self.pre_specs.append((out, [(sg[0], wk) for sg, wk in zip(segs, wkeys)]))
+
+        for c in chg[0]:
+            if ("v0101", c) in self.P:
                 n2 = ns[0][c] ** 2
-                buf = torch.empty((n2, N[1] ** 2), **f64)
-                pre.add(n2, N[1] ** 2, [(rho[0]["ca"][(c, c)], N[0] ** 2, W["v0101"], N[0] ** 2, N[0] ** 2, 1.0)],
-                        buf, N[1] ** 2)
-                self.P[("v0101", c)] = buf
+                add_pre(n2, N[1] ** 2, [(rho[0]["ca"][(c, c)], N[0] ** 2, W["v0101"], N[0] ** 2, N[0] ** 2, 1.0)],
+                        self.P[("v0101", c)], N[1] ** 2, wkeys=["v0101"])
         for m, o in ((0, 1), (1, 0)):
             for (op, bc, kc) in spaces[m].couplings:
                 nbk = ns[m][bc] * ns[m][kc]
                 if op == "c":        # bra - ket = -1: P1 = rho^c h + rho^cca (-2V)
-                    buf = torch.empty((nbk, N[o]), **f64)
                     segs = [(rho[m]["c"][(bc, kc)], N[m], W[("h1", m)], N[m], N[m], 1.0)]
+                    wk = [("h1", m)]
                     if ("cca", bc, kc) in spaces[m].couplings:
                         segs.append((rho[m]["cca"][(bc, kc)], N[m] ** 3, W[("cca", m)], N[m] ** 3, N[m] ** 3, 1.0))
-                    pre.add(nbk, N[o], segs, buf, N[o])
-                    self.P[("p1", m, bc, kc)] = buf
+                        wk.append(("cca", m))
+                    add_pre(nbk, N[o], segs, self.P[("p1", m, bc, kc)], N[o], wkeys=wk)
                 elif op == "caa":
-                    buf = torch.empty((nbk, N[o]), **f64)
-                    pre.add(nbk, N[o], [(rho[m]["caa"][(bc, kc)], N[m] ** 3, W[("caa", m)], N[m] ** 3, N[m] ** 3, 1.0)],
-                            buf, N[o])
-                    self.P[("pcaa", m, bc, kc)] = buf
+                    add_pre(nbk, N[o], [(rho[m]["caa"][(bc, kc)], N[m] ** 3, W[("caa", m)], N[m] ** 3, N[m] ** 3, 1.0)],
+                            self.P[("pcaa", m, bc, kc)], N[o], wkeys=[("caa", m)])
                 elif op == "cc":
-                    buf = torch.empty((nbk, N[o] ** 2), **f64)
-                    pre.add(nbk, N[o] ** 2, [(rho[m]["cc"][(bc, kc)], N[m] ** 2, W[("cc", m)], N[m] ** 2, N[m] ** 2, 1.0)],
-                            buf, N[o] ** 2)
-                    self.P[("pcc", m, bc, kc)] = buf
-        # monomer pieces: H1 (e1 + e2) and u100 (du); atomically accumulated (mode 1)
-        self.H1blk = [{}, {}]
-        self.DU = [{}, {}]
-        self.FULLD = [{}, {}]
+                    add_pre(nbk, N[o] ** 2, [(rho[m]["cc"][(bc, kc)], N[m] ** 2, W[("cc", m)], N[m] ** 2, N[m] ** 2, 1.0)],
+                            self.P[("pcc", m, bc, kc)], N[o] ** 2, wkeys=[("cc", m)])
+        # monomer pieces: H1 (e1 + e2), u100 (du), and their sum (fd) for the full H
         self.sigma = [{}, {}]
         for m, o in ((0, 1), (1, 0)):
             for c in chg[m]:
-                if ("ca", c, c) not in spaces[m].couplings:
+                if c not in self.H1blk[m]:
                     continue
                 n = ns[m][c]
                 ca = rho[m]["ca"][(c, c)]
-                h1 = torch.zeros((n * n, 1), **f64)
-                du = torch.zeros((n * n, 1), **f64)
-                fd = torch.zeros((n * n, 1), **f64)
-                self.H1blk[m][c], self.DU[m][c], self.FULLD[m][c] = h1, du, fd
                 sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m), precision=self.precision)
                 self.sigma[m][c] = sg
                 nconf = spaces[m].n_conf[c]
-                splitk = max(1, min(64, nconf // 512))
-                z = self.builders[m].zT[c]     # (nconf, n): need Z rows (n, nconf) -> separate buffer
-                zrow = torch.empty((n, nconf), **f64)
-                sg.zrow = zrow
-                targets = [h1, fd] if output == "full" else [h1]
-                for tgt in targets:
-                    pre.add(n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1, mode=1)
-                    pre.add(n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n, mode=1, splitk=splitk)
-                for tgt in ([du, fd] if output == "full" else [du]):
-                    pre.add(n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1, mode=1)
-                del z
+                zrow = self.coeffs[m][c]
+                targets_h1 = [self.H1blk[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
+                targets_du = [self.DU[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
+                for tgt in targets_h1:
+                    add_pre(n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1)
+                    pre.add(n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n, mode=1,
+                            splitk=_splitk(nconf, target=256, cap=64))
+                for tgt in targets_du:
+                    add_pre(n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1)
         self.pre = pre.finalize()
 
         # ---- final tasks: one per output charge block ----
         nb = [ns[m] for m in (0, 1)]
         off0, tot0 = _product_offsets(nb[0], chg[0])
         off1, tot1 = _product_offsets(nb[1], chg[1])
+        self.offsets = (off0, off1)
         self.dim = (tot0 * tot1, tot0 * tot1)
         self.tot = (tot0, tot1)
         self.H = torch.zeros(self.dim, **f64)
@@ -236,6 +286,7 @@ class XRDimerPlan:
         n_ref0 = spaces[0].n_elec_ref
         n_ref1 = spaces[1].n_elec_ref
         self.block_keys = []
+        self.final_tasks = []
         for ci0 in chg[0]:
             for ci1 in chg[1]:
                 for cj0 in chg[0]:
@@ -289,23 +340,33 @@ class XRDimerPlan:
                         fin.add(M, Nn, segs, self.H, self.dim[1], mode=2,
                                 maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB)
                         self.block_keys.append((ci0, ci1, cj0, cj1))
+                        self.final_tasks.append(dict(key=(ci0, ci1, cj0, cj1), segs=segs, M=M, N=Nn,
+                                                     dims=(ni0, nj0, ni1, nj1),
+                                                     maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB))
         self.fin = fin.finalize()
-        if nuc:
-            raise NotImplementedError("nuclear repulsion constants are added by the caller")
 
     # ------------------------------------------------------------------------------------
-    def build(self, coeffs):
-        """coeffs: two {charge: CUDA float64 (n_states, n_conf)} dicts -> fills self.H (and H1)."""
+    def set_coeffs(self, coeffs):
+        """Copy new state coefficients {charge: (n_states, n_conf)} per fragment into the plan."""
         for m in (0, 1):
-            self.builders[m].build(coeffs[m])
+            for c in self.charges[m]:
+                self.coeffs[m][c].copy_(coeffs[m][c], non_blocking=True)
+
+    def launch(self):
+        """Enqueue the whole build (densities, sigma, precontractions, final blocks)."""
+        for m in (0, 1):
+            self.builders[m].build(self.coeffs[m])
             for c, sg in self.sigma[m].items():
-                sg.zrow.copy_(coeffs[m][c])
                 sg.run_sigma(self.builders[m].zT[c])
-                self.H1blk[m][c].zero_()
-                self.DU[m][c].zero_()
-                self.FULLD[m][c].zero_()
+        self.arena.buf.zero_()
         self.pre.run()
         self.fin.run()
+
+    def build(self, coeffs=None):
+        """coeffs: two {charge: CUDA float64 (n_states, n_conf)} dicts -> fills self.H."""
+        if coeffs is not None:
+            self.set_coeffs(coeffs)
+        self.launch()
         return self.H
 
     def H1(self):

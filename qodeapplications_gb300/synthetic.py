@@ -120,3 +120,33 @@ def make_system(n_frag=2, n_orb=9, n_states=10, charges=(+1, 0, -1), n_elec_ref=
         states.append(st)
     return dict(n_frag=n_frag, n_orb=n_orb, n_core=n_core, n_elec_ref=n_elec_ref,
                 charges=tuple(charges), Ns=[2 * n_orb] * n_frag, h=h, V=V, states=states)
+
+
+def spin_orbital_spatial_index(frag_sizes):
+    """Spatial orbital of every spin orbital (alpha block then beta block per fragment)."""
+    out, off = [], 0
+    for nf in frag_sizes:
+        out += [off + i for i in range(nf)] * 2
+        off += nf
+    return out
+
+
+def rotate_integrals(h, V, kappa_sp, frag_sizes):
+    """Integrals in the orbitals rotated by R = expm(kappa) (kappa antisymmetric over the
+    supersystem's spatial orbitals, the same rotation for both spins):
+    h' = R^T h R, V'_pqrs = sum R_ap R_bq R_cr R_ds V_abcd."""
+    from scipy.linalg import expm
+    R_sp = expm(np.asarray(kappa_sp, dtype=np.float64))
+    sidx = spin_orbital_spatial_index(frag_sizes)
+    n = len(sidx)
+    spins = []
+    seen = {}
+    for sp in sidx:
+        spins.append(seen.get(sp, 0))
+        seen[sp] = seen.get(sp, 0) + 1
+    spins = np.array(spins)
+    R = R_sp[np.ix_(sidx, sidx)] * (spins[:, None] == spins[None, :])
+    h2 = R.T @ h @ R
+    V2 = np.einsum("ap,bq,cr,ds,abcd->pqrs", R, R, R, R, V, optimize=True)
+    assert h2.shape == (n, n)
+    return h2, V2
