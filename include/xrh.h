@@ -171,6 +171,54 @@ int xrh_ccaa_weighted(int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
                       const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev, int n_ket_conf,
                       const double* zbT_dev, const double* YT_dev, int n, double* Gamma_dev, void* stream);
 
+/* ---- split-precision tensor-core path (tcgen05, sm_103a) -------------------------------
+ * Same task model as xrh_gemm_fp64_grouped for the forward build.  Every FP64 operand is
+ * first split by xrh_split_operand into hi = round(x), lo = round(x - hi) in BF16
+ * (XRH_BF16X3) or TF32 stored as 32-bit words (XRH_TF32X3), row-major [rows, Kp] with
+ * Kp a multiple of xrh_tc_chunk_elems(precision) (64 or 32; the padding is zero).
+ * xrh_tc_encode_map writes (on the host) the 128-byte TMA descriptor of one such array with
+ * a box of xrh_tc_chunk_elems x box_rows and 128-byte swizzle; an operand is described by
+ * two consecutive maps (hi, lo) in a device array of maps (64-byte aligned).
+ * A segment contributes A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with FP32 accumulation
+ * (negate != 0 flips its sign; other scale factors must be folded into the operands).
+ * Tiles are 128 x bn (bn = 32, 64 or 128, the box rows of the B maps), times splitk.
+ * Modes and the epilogue are those of xrh_gemm_fp64_grouped (FP64 output).  A bounded
+ * wait that expires sets *status_dev = XRH_ERR_TIMEOUT (status_dev must start at 0). */
+typedef struct {
+    int64_t tmA;       /* index of A's hi map (lo map at tmA + 1) */
+    int64_t tmB;       /* index of B's hi map (lo map at tmB + 1) */
+    int64_t kchunks;   /* K chunks of this segment (Kp / xrh_tc_chunk_elems) */
+    int64_t negate;
+} xrh_tc_segment;
+
+typedef struct {
+    int64_t M, N;
+    int64_t seg_begin, seg_count;
+    int64_t mode;
+    int64_t splitk;
+    int64_t tile_begin;
+    int64_t bn;
+    double* C;
+    int64_t ldc;
+    const int32_t* rowA;
+    const int32_t* colA;
+    const int32_t* rowB;
+    const int32_t* colB;
+    const double* DA;
+    const double* DB;
+    const uint8_t* diagA;
+    const uint8_t* diagB;
+} xrh_tc_task;
+
+int xrh_tc_chunk_elems(int precision);
+int xrh_split_operand(int precision, const double* src_dev, int64_t rows, int64_t K, int64_t ld,
+                      int64_t Kp, void* hi_dev, void* lo_dev, void* stream);
+int xrh_tc_encode_map(int precision, const void* base_dev, int64_t rows, int64_t Kp, int box_rows,
+                      void* map_out_host);
+int xrh_gemm_tc_grouped(int precision, const xrh_tc_task* tasks_dev, int n_tasks, int64_t total_tiles,
+                        const xrh_tc_segment* segs_dev, const void* maps_dev, int32_t* status_dev,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

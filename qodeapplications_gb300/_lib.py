@@ -37,6 +37,10 @@ _SIGS = {
     "xrh_lanczos_normalize": (_i32, [_i64, _vp, _vp, _vp, _vp]),
     "xrh_density_adjoint": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
     "xrh_ccaa_weighted": (_i32, [_i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
+    "xrh_tc_chunk_elems": (_i32, [_i32]),
+    "xrh_split_operand": (_i32, [_i32, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),
+    "xrh_tc_encode_map": (_i32, [_i32, _vp, _i64, _i64, _i32, _vp]),
+    "xrh_gemm_tc_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp, _vp, _vp, _vp]),
 }
 _OPTIONAL = {}
 
@@ -75,7 +79,8 @@ class LaunchCounter:
     """Counts library calls that launch one kernel each (the gpu_launches figure)."""
     launching = {"xrh_density_accumulate", "xrh_transpose", "xrh_sigma2e", "xrh_gemm_fp64_grouped",
                  "xrh_couplings_count", "xrh_couplings_fill", "xrh_gemv_rows", "xrh_gemv_cols",
-                 "xrh_lanczos_normalize", "xrh_density_adjoint", "xrh_ccaa_weighted"}
+                 "xrh_lanczos_normalize", "xrh_density_adjoint", "xrh_ccaa_weighted", "xrh_split_operand",
+                 "xrh_gemm_tc_grouped"}
     count = 0
 
 

@@ -4,11 +4,13 @@ A task is one output block; its segments are the contractions summed into it (K
 concatenation).  Tables are built once per plan with the device addresses of persistent
 buffers and uploaded once, so every later launch is a single call (CUDA-graph safe).
 """
+import ctypes
+
 import numpy as np
 import torch
 
 from . import _lib
-from ._lib import SEGMENT_DTYPE, TASK_DTYPE, call, stream_ptr
+from ._lib import SEGMENT_DTYPE, TASK_DTYPE, call, ptr, stream_ptr
 
 FP64_TILE = 64
 
@@ -81,3 +83,137 @@ class GroupedGemm:
             return
         call("xrh_gemm_fp64_grouped", _lib.ptr(self.tasks_dev), self.n_tasks, self.total_tiles,
              _lib.ptr(self.segs_dev), stream_ptr(stream))
+
+
+TC_TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
+                          ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("bn", np.int64),
+                          ("C", np.uint64), ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64),
+                          ("rowB", np.uint64), ("colB", np.uint64), ("DA", np.uint64), ("DB", np.uint64),
+                          ("diagA", np.uint64), ("diagB", np.uint64)])
+TC_SEG_DTYPE = np.dtype([("tmA", np.int64), ("tmB", np.int64), ("kchunks", np.int64), ("negate", np.int64)])
+assert TC_TASK_DTYPE.itemsize == 144 and TC_SEG_DTYPE.itemsize == 32
+TC_BM = 128
+
+
+class SplitRegistry:
+    """hi/lo split copies of FP64 operands for the tensor-core path, and their TMA maps.
+
+    Every operand tensor is split once per build (split(group)); its two 128-byte TMA
+    descriptors per box height are encoded once on the host and uploaded with upload()."""
+
+    def __init__(self, precision, device="cuda"):
+        self.prec = _lib.PRECISIONS[precision]
+        assert self.prec in (_lib.BF16X3, _lib.TF32X3)
+        self.kch = 64 if self.prec == _lib.BF16X3 else 32
+        self.dtype = torch.bfloat16 if self.prec == _lib.BF16X3 else torch.int32
+        self.device = torch.device(device)
+        self.ops = {}        # data_ptr -> dict
+        self.maps = []       # host byte strings, 128 B each
+        self.map_index = {}
+        self.maps_dev = None
+
+    def operand(self, t, rows, K, ld, group="in"):
+        key = t.data_ptr()
+        if key not in self.ops:
+            Kp = ((K + self.kch - 1) // self.kch) * self.kch
+            hi = torch.zeros((rows, Kp), dtype=self.dtype, device=self.device)
+            lo = torch.zeros((rows, Kp), dtype=self.dtype, device=self.device)
+            self.ops[key] = dict(src=t, rows=rows, K=K, ld=ld, Kp=Kp, hi=hi, lo=lo, group=group)
+        op = self.ops[key]
+        assert op["rows"] == rows and op["K"] == K and op["ld"] == ld, "operand registered with another shape"
+        return op
+
+    def map_for(self, t, box_rows):
+        key = (t.data_ptr(), box_rows)
+        if key not in self.map_index:
+            op = self.ops[t.data_ptr()]
+            idx = len(self.maps)
+            for part in ("hi", "lo"):
+                buf = ctypes.create_string_buffer(128)
+                call("xrh_tc_encode_map", self.prec, ptr(op[part]), op["rows"], op["Kp"], box_rows, buf)
+                self.maps.append(buf.raw)
+            self.map_index[key] = idx
+        return self.map_index[key]
+
+    def upload(self):
+        raw = b"".join(self.maps) if self.maps else bytes(128)
+        self.maps_dev = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(self.device)
+        assert self.maps_dev.data_ptr() % 64 == 0
+
+    def split(self, group, stream=None):
+        s = stream_ptr(stream)
+        for op in self.ops.values():
+            if op["group"] == group:
+                call("xrh_split_operand", self.prec, ptr(op["src"]), op["rows"], op["K"], op["ld"], op["Kp"],
+                     ptr(op["hi"]), ptr(op["lo"]), s)
+
+
+class TCGroupedGemm:
+    """Task tables for xrh_gemm_tc_grouped (split precision on tcgen05)."""
+
+    def __init__(self, registry):
+        self.reg = registry
+        self.device = registry.device
+        self._tasks, self._segs, self._keep = [], [], []
+        self.flops = 0.0
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+    def add(self, M, N, segments, C, ldc, mode=0, splitk=None, maps=None, DA=None, DB=None, groups=None):
+        if M <= 0 or N <= 0:
+            return
+        bn = 32 if N <= 32 else (64 if N <= 64 else 128)
+        seg_begin = len(self._segs)
+        kc_total = 0
+        for i, (A, lda, B, ldb, K, alpha) in enumerate(segments):
+            assert abs(abs(alpha) - 1.0) < 1e-15, "tensor-core segments take alpha = +-1 (fold scales into operands)"
+            ga, gb = (groups[i] if groups else ("in", "in"))
+            opA = self.reg.operand(A, M, K, lda, ga)
+            opB = self.reg.operand(B, N, K, ldb, gb)
+            tmA = self.reg.map_for(A, 128)
+            tmB = self.reg.map_for(B, bn)
+            kch = opA["Kp"] // self.reg.kch
+            self._segs.append((tmA, tmB, kch, 1 if alpha < 0 else 0))
+            kc_total += kch
+            self.flops += 2.0 * M * N * K
+            self._keep += [A, B]
+        if splitk is None:
+            splitk = int(max(1, min(32, kc_total // 16))) if mode == 1 else 1
+        t = dict(M=M, N=N, seg_begin=seg_begin, seg_count=len(segments), mode=mode, splitk=splitk, bn=bn,
+                 C=C.data_ptr(), ldc=ldc)
+        self._keep.append(C)
+        if mode == 2:
+            for nm, tt in zip(("rowA", "colA", "rowB", "colB", "diagA", "diagB"), maps):
+                t[nm] = tt.data_ptr()
+                self._keep.append(tt)
+            t["DA"] = DA.data_ptr() if DA is not None else 0
+            t["DB"] = DB.data_ptr() if DB is not None else 0
+            self._keep += [x for x in (DA, DB) if x is not None]
+        self._tasks.append(t)
+
+    def finalize(self):
+        tasks = np.zeros(len(self._tasks), dtype=TC_TASK_DTYPE)
+        begin = 0
+        for i, t in enumerate(self._tasks):
+            for k, v in t.items():
+                tasks[i][k] = v
+            tasks[i]["tile_begin"] = begin
+            begin += ((t["M"] + TC_BM - 1) // TC_BM) * ((t["N"] + t["bn"] - 1) // t["bn"]) * t["splitk"]
+        self.total_tiles = begin
+        segs = np.zeros(max(len(self._segs), 1), dtype=TC_SEG_DTYPE)
+        for i, s in enumerate(self._segs):
+            segs[i] = s
+        self.tasks_dev = torch.from_numpy(tasks.view(np.uint8).copy()).to(self.device)
+        self.segs_dev = torch.from_numpy(segs.view(np.uint8).copy()).to(self.device)
+        self.n_tasks = len(self._tasks)
+        return self
+
+    def run(self, stream=None):
+        if self.n_tasks == 0:
+            return
+        call("xrh_gemm_tc_grouped", self.reg.prec, ptr(self.tasks_dev), self.n_tasks, self.total_tiles,
+             ptr(self.segs_dev), ptr(self.reg.maps_dev), ptr(self.status), stream_ptr(stream))
+
+    def check(self):
+        st = int(self.status.item())
+        if st != 0:
+            raise _lib.XRHError(f"tensor-core GEMM reported status {st} ({_lib.lib().xrh_status_string(st).decode()})")

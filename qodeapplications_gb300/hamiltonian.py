@@ -24,7 +24,7 @@ import torch
 from . import _lib
 from ._lib import call, ptr, stream_ptr
 from .densities import DensityBuilder, FragmentSpace
-from .gemm import GroupedGemm
+from .gemm import GroupedGemm, SplitRegistry, TCGroupedGemm
 
 
 class DeviceIntegrals:
@@ -253,6 +253,7 @@ class XRDimerPlan:
                             self.P[("pcc", m, bc, kc)], N[o] ** 2, wkeys=[("cc", m)])
         # monomer pieces: H1 (e1 + e2), u100 (du), and their sum (fd) for the full H
         self.sigma = [{}, {}]
+        mono = []
         for m, o in ((0, 1), (1, 0)):
             for c in chg[m]:
                 if c not in self.H1blk[m]:
@@ -266,11 +267,15 @@ class XRDimerPlan:
                 targets_h1 = [self.H1blk[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
                 targets_du = [self.DU[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
                 for tgt in targets_h1:
-                    add_pre(n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1)
-                    pre.add(n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n, mode=1,
-                            splitk=_splitk(nconf, target=256, cap=64))
+                    mono.append((n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
+                                 _splitk(N[m] ** 2)))
+                    mono.append((n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n,
+                                 _splitk(nconf, target=256, cap=64)))
                 for tgt in targets_du:
-                    add_pre(n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1)
+                    mono.append((n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
+                                 _splitk(N[m] ** 2)))
+        for (M_, N_, segs_, out_, ldc_, sk_) in mono:
+            pre.add(M_, N_, segs_, out_, ldc_, mode=1, splitk=sk_)
         self.pre = pre.finalize()
 
         # ---- final tasks: one per output charge block ----
@@ -345,6 +350,33 @@ class XRDimerPlan:
                                                      maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB))
         self.fin = fin.finalize()
 
+        # ---- split-precision tensor-core variant of both launches ----
+        self.tc = self.precision in (_lib.BF16X3, _lib.TF32X3)
+        if self.tc:
+            reg = SplitRegistry(precision, dev)
+            p_ptrs = {t.data_ptr() for t in self.P.values()}
+            w_ptrs = {t.data_ptr() for t in W.values()}
+
+            def grp(t):
+                return "P" if t.data_ptr() in p_ptrs else ("W" if t.data_ptr() in w_ptrs else "in")
+
+            pre_tc = TCGroupedGemm(reg)
+            for out, segs_ in self.pre_specs:
+                M_, X_ = out.shape
+                tsegs = [(r_, r_.numel() // M_, W[wk], W[wk].shape[1], W[wk].shape[1], 1.0) for r_, wk in segs_]
+                pre_tc.add(M_, X_, tsegs, out, X_, mode=1,
+                           groups=[(grp(a[0]), grp(a[2])) for a in tsegs])
+            pre64 = GroupedGemm(dev)
+            for (M_, N_, segs_, out_, ldc_, sk_) in mono:
+                pre64.add(M_, N_, segs_, out_, ldc_, mode=1, splitk=sk_)
+            fin_tc = TCGroupedGemm(reg)
+            for t in self.final_tasks:
+                fin_tc.add(t["M"], t["N"], t["segs"], self.H, self.dim[1], mode=2, maps=t["maps"], DA=t["DA"],
+                           DB=t["DB"], groups=[(grp(a[0]), grp(a[2])) for a in t["segs"]])
+            reg.upload()
+            reg.split("W")
+            self.reg, self.pre_tc, self.pre64, self.fin_tc = reg, pre_tc.finalize(), pre64.finalize(), fin_tc.finalize()
+
     # ------------------------------------------------------------------------------------
     def set_coeffs(self, coeffs):
         """Copy new state coefficients {charge: (n_states, n_conf)} per fragment into the plan."""
@@ -359,8 +391,15 @@ class XRDimerPlan:
             for c, sg in self.sigma[m].items():
                 sg.run_sigma(self.builders[m].zT[c])
         self.arena.buf.zero_()
-        self.pre.run()
-        self.fin.run()
+        if self.tc:
+            self.reg.split("in")
+            self.pre_tc.run()
+            self.pre64.run()
+            self.reg.split("P")
+            self.fin_tc.run()
+        else:
+            self.pre.run()
+            self.fin.run()
 
     def build(self, coeffs=None):
         """coeffs: two {charge: CUDA float64 (n_states, n_conf)} dicts -> fills self.H."""
@@ -386,6 +425,12 @@ class XRDimerPlan:
     @property
     def flops(self):
         return self.pre.flops + self.fin.flops
+
+    def check_status(self):
+        """Raise if a bounded device wait of the tensor-core kernels timed out (syncs)."""
+        if self.tc:
+            self.pre_tc.check()
+            self.fin_tc.check()
 
 
 def lowest_eigenpairs(H, k=5):

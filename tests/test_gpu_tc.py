@@ -1,0 +1,71 @@
+"""Split-precision tensor-core path (tcgen05): GEMM unit checks and the XR-H build.
+
+Tolerances are those of the arithmetic: 3xBF16 keeps about 16 significant bits per operand
+(relative error of a product term ~1e-5), 3xTF32 about 21 bits (~5e-7), both accumulated
+in FP32; they are stated per test against an FP64 result."""
+import numpy as np
+import pytest
+
+import xr_oracle as O
+from qodeapplications_gb300 import synthetic as S
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = {"bf16x3": 3e-5, "tf32x3": 2e-6}
+
+
+def _rel(a, b):
+    return float((a - b).abs().max() / b.abs().max())
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_tc_gemm_store_and_splitk(prec):
+    from qodeapplications_gb300.gemm import SplitRegistry, TCGroupedGemm
+    g = torch.Generator().manual_seed(3)
+    A = torch.randn(300, 200, generator=g, dtype=torch.float64).cuda()
+    B = torch.randn(150, 200, generator=g, dtype=torch.float64).cuda()
+    A2 = torch.randn(300, 70, generator=g, dtype=torch.float64).cuda()
+    B2 = torch.randn(150, 70, generator=g, dtype=torch.float64).cuda()
+    reg = SplitRegistry(prec)
+    C0 = torch.zeros(300, 150, dtype=torch.float64, device="cuda")
+    C1 = torch.zeros(300, 150, dtype=torch.float64, device="cuda")
+    tc = TCGroupedGemm(reg)
+    tc.add(300, 150, [(A, 200, B, 200, 200, 1.0)], C0, 150, mode=0)
+    tc.add(300, 150, [(A, 200, B, 200, 200, 1.0), (A2, 70, B2, 70, 70, -1.0)], C1, 150, mode=1, splitk=3)
+    reg.upload()
+    tc.finalize()
+    reg.split("in")
+    tc.run()
+    torch.cuda.synchronize()
+    tc.check()
+    ref0 = A @ B.t()
+    ref1 = ref0 - A2 @ B2.t()
+    assert _rel(C0, ref0) < TOL[prec], _rel(C0, ref0)
+    assert _rel(C1, ref1) < TOL[prec], _rel(C1, ref1)
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_tc_dimer_H_close_to_oracle(prec):
+    from qodeapplications_gb300.densities import FragmentSpace
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+    chg = (+1, 0, -1)
+    sysd = S.make_system(n_frag=2, n_orb=5, n_states=4, charges=chg, seed=21)
+    spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in chg}, 5, 0, 4) for m in range(2)]
+    ns = [{c: 4 for c in chg}] * 2
+    plan = XRDimerPlan(spaces, ns, [list(chg)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
+                       precision=prec)
+    coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in chg} for m in range(2)]
+    H = plan.build(coeffs)
+    torch.cuda.synchronize()
+    plan.check_status()
+    ints = O.FragInts(sysd["h"], sysd["V"], sysd["Ns"])
+    dens = [O.build_densities({c: O.Sector(*sysd["states"][m][c]) for c in chg}, 5, 0, 4) for m in range(2)]
+    H1, H2 = O.get_xr_H0(ints, dens, [list(chg)] * 2)
+    Href = O.full_H(H1, H2)
+    err = np.abs(H.cpu().numpy() - Href).max()
+    e_gpu = np.linalg.eigvalsh(H.cpu().numpy())[0]
+    e_ref = np.linalg.eigvalsh(Href)[0]
+    print(f"{prec}: max|dH| = {err:.3e}, |dE0| = {abs(e_gpu - e_ref):.3e}")
+    assert err < {"bf16x3": 1e-3, "tf32x3": 2e-5}[prec]
+    assert abs(e_gpu - e_ref) < 1e-6 if prec == "tf32x3" else abs(e_gpu - e_ref) < 1e-4
