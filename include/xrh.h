@@ -77,6 +77,23 @@ int xrh_density_accumulate(int precision, int64_t K, const int64_t* idx_ptr_dev,
                            const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
                            double* rhoT_dev, void* stream);
 
+/* Allocation-free transition densities (this entry point has no counterpart in the
+ * reference).  For callers that cannot allocate device memory -- for example code running
+ * inside another application's CUDA context whose allocator owns all device memory, or a
+ * host program without a device allocator of its own -- this variant needs no scratch from
+ * the caller: it uses a fixed 8 MiB array in the library's own device memory
+ * (K * n_b * n_k <= 1048576 doubles, else XRH_ERR_CAPACITY) and writes rho_dev directly in
+ * the (n_b, n_k, K) layout.  Arguments are those of xrh_density_accumulate.  It calls no
+ * cudaMalloc/cudaFree.  The first call on a device looks up that device's address of the
+ * array (cudaGetSymbolAddress) and must therefore happen before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller.  Every GPU that loads the library keeps the
+ * 8 MiB until the process exits. */
+int xrh_density_build_noalloc(int precision, int64_t K, const int64_t* idx_ptr_dev,
+                              const int32_t* P_dev, const int32_t* Q_dev, const int8_t* sign_dev,
+                              const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
+                              double* rho_dev, void* stream);
+
 /* out[c, r] = in[r, c] for a row-major [rows, cols] FP64 matrix. */
 int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_dev, void* stream);
 

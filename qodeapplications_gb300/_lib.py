@@ -30,6 +30,7 @@ _SIGS = {
     "xrh_couplings_fill": (_i32, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "xrh_density_accumulate": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_transpose": (_i32, [_vp, _i64, _i64, _vp, _vp]),
+    "xrh_density_build_noalloc": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_sigma2e": (_i32, [_i32, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_gemm_fp64_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_gemv_rows": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _dbl, _vp, _vp]),

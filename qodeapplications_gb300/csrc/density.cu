@@ -229,3 +229,44 @@ extern "C" int xrh_sigma2e(int precision, int n_orbs, const double* V_dev, const
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }
+
+// ---- allocation-free density build ------------------------------------------------------
+// For callers that cannot allocate device memory: the scratch that xrh_density_accumulate's
+// callers provide (the [K, n_b, n_k] buffer before the transpose) is a fixed-size array in
+// the module's own global memory.  Every GPU that loads libxrh.so holds it until exit.
+namespace {
+constexpr int64_t kNoAllocScratchDoubles = 1LL << 20;          // 8 MiB of FP64
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+double* g_noalloc_scratch_addr[256] = {};                      // device address per device ordinal
+}  // namespace
+
+extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t* idx_ptr_dev, const int32_t* P_dev,
+                                         const int32_t* Q_dev, const int8_t* sign_dev, const double* zbT_dev, int n_b,
+                                         const double* zkT_dev, int n_k, double* rho_dev, void* stream) {
+    if (K <= 0 || n_b <= 0 || n_k <= 0 || !idx_ptr_dev || !zbT_dev || !zkT_dev || !rho_dev) return XRH_ERR_ARG;
+    if (precision != XRH_FP64 && precision != XRH_FP32) return XRH_ERR_UNSUPPORTED;
+    if (K * (int64_t)n_b * (int64_t)n_k > kNoAllocScratchDoubles) return XRH_ERR_CAPACITY;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        xrh_set_last_cuda_error((int)e);
+        return XRH_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= 256) return XRH_ERR_CAPACITY;
+    double* scratch = g_noalloc_scratch_addr[dev];
+    if (!scratch) {
+        // once per device, with that device current: the host-side name of the array is not a
+        // device address, so ask the runtime for this device's address of it
+        e = cudaGetSymbolAddress(reinterpret_cast<void**>(&scratch), g_noalloc_scratch);
+        if (e != cudaSuccess || !scratch) {
+            xrh_set_last_cuda_error((int)e);
+            return XRH_ERR_CUDA;
+        }
+        g_noalloc_scratch_addr[dev] = scratch;
+    }
+    // the accumulate kernel overwrites every scratch element it uses: nothing to clear
+    int st = xrh_density_accumulate(precision, K, idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k,
+                                    scratch, stream);
+    if (st != XRH_OK) return st;
+    return xrh_transpose(scratch, K, (int64_t)n_b * n_k, rho_dev, stream);
+}
