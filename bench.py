@@ -42,8 +42,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
-    p.add_argument("--precision", default="fp64")
+    p.add_argument("--precision", default="bf16x3")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-variants", action="store_true")
     return p.parse_args()
 
 
@@ -126,60 +127,88 @@ class ClockSampler:
 
 
 class GPUIteration:
-    """Device-resident optimizer iteration: densities -> H -> lowest eigenpair."""
+    """Device-resident optimizer iteration (qodeapplications_gb300.iteration.XRStateOptimizer):
+    densities -> H -> lowest eigenpair (FP64 Lanczos) -> state and orbital gradients -> state step."""
 
     def __init__(self, sysd, precision):
         import torch
-        from qodeapplications_gb300.densities import FragmentSpace
-        from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+        from qodeapplications_gb300.iteration import XRStateOptimizer
         self.torch = torch
-        charges = list(sysd["charges"])
-        self.charges = charges
-        spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in charges}, sysd["n_orb"], sysd["n_core"],
-                                sysd["n_elec_ref"]) for m in range(2)]
-        ns = [{c: sysd["states"][m][c][0].shape[0] for c in charges} for m in range(2)]
-        self.plan = XRDimerPlan(spaces, ns, [charges, charges], DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
-                                output="full", precision=precision)
-        self.coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda").contiguous() for c in charges}
-                       for m in range(2)]
-        self.host = [{c: torch.as_tensor(sysd["states"][m][c][0]).pin_memory() for c in charges} for m in range(2)]
+        self.opt = XRStateOptimizer(sysd, precision=precision)
+        self.charges = list(sysd["charges"])
+        self.host = [{c: torch.as_tensor(sysd["states"][m][c][0]).pin_memory() for c in self.charges}
+                     for m in range(2)]
         self.h2d_bytes = sum(t.numel() * 8 for d in self.host for t in d.values())
         self.E_host = torch.empty(1, dtype=torch.float64).pin_memory()
-        self.phase_events = []
+        n_g = sum(t.numel() for d in self.host for t in d.values())
+        self.g_host = torch.empty(n_g, dtype=torch.float64).pin_memory()
+        self.d2h_bytes = 8 + n_g * 8
 
-    def step(self, events=None):
-        torch = self.torch
-        if events is not None:
-            events[0].record()
-        for m in (0, 1):
-            self.plan.builders[m].build(self.coeffs[m])
-        for m in (0, 1):
-            for c, sg in self.plan.sigma[m].items():
-                sg.zrow.copy_(self.coeffs[m][c])
-                sg.run_sigma(self.plan.builders[m].zT[c])
-                self.plan.H1blk[m][c].zero_()
-                self.plan.DU[m][c].zero_()
-                self.plan.FULLD[m][c].zero_()
-        if events is not None:
-            events[1].record()
-        self.plan.pre.run()
-        if events is not None:
-            events[2].record()
-        self.plan.fin.run()
-        if events is not None:
-            events[3].record()
-        w, v = torch.linalg.eigh(self.plan.H)
-        if events is not None:
-            events[4].record()
-        return w[:1]
+    def step(self):
+        return self.opt.iterate()
 
     def step_e2e(self):
+        """Through host buffers: states from pinned host memory in, energy and the updated
+        states (the optimizer's output) back to pinned host memory."""
+        torch = self.torch
         for m in (0, 1):
             for c in self.charges:
-                self.coeffs[m][c].copy_(self.host[m][c], non_blocking=True)
-        e = self.step()
-        self.E_host.copy_(e, non_blocking=True)
-        return self.E_host
+                self.opt.plan.coeffs[m][c].copy_(self.host[m][c], non_blocking=True)
+        e = self.opt.iterate()
+        off = 0
+        for m in (0, 1):
+            for c in self.charges:
+                z = self.opt.plan.coeffs[m][c].reshape(-1)
+                self.g_host[off:off + z.numel()].copy_(z, non_blocking=True)
+                off += z.numel()
+        torch.cuda.current_stream().synchronize()
+        return e
+
+
+def graph_launches(it):
+    """Kernels of this library launched per replayed iteration (counted while capturing)."""
+    return getattr(it.opt, "graph_kernels", None)
+
+
+def time_variant(sysd, precision, steps, warmup, l2_flush):
+    """Device-resident seconds per iteration of one precision variant; returns (s/iter, E list, it)."""
+    import torch
+    it = GPUIteration(sysd, precision)
+    for _ in range(max(warmup, 3)):
+        it.step()
+    torch.cuda.synchronize()
+    ms, Es = [], []
+    for _ in range(steps):
+        l2_flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        Es.append(it.step())
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return sum(ms) / 1e3 / steps, Es, it
+
+
+def dominant_kernel_roofline(it, reps=20):
+    """Live CUDA-event timing of the final grouped-GEMM launch (the dominant tensor-contraction
+    kernel), on the launching stream, buffers as left by the last iteration."""
+    import torch
+    plan = it.opt.plan
+    if plan.tc:
+        g, flops, name = plan.fin_tc, plan.fin_tc.flops, f"gemm_tc_kernel<{'bf16' if plan.precision == 2 else 'tf32'}> (final blocks)"
+    else:
+        g, flops, name = plan.fin, plan.fin.flops, "gemm_fp64_kernel (final blocks)"
+    for _ in range(3):
+        g.run()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        g.run()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / reps
+    return name, flops, ms
 
 
 def run_ours(args):
@@ -193,95 +222,134 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     sysd = make_system(args.config)
-    it = GPUIteration(sysd, args.precision)
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    for _ in range(max(args.warmup, 3)):
-        it.step()
-    torch.cuda.synchronize()
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    clock_path = os.path.join(tempfile.gettempdir(), f"xrh_clocks_{os.getpid()}.csv")
-    n_ph = 5
-    step_ms, phase_ms = [], [0.0] * (n_ph - 1)
+    it = GPUIteration(sysd, args.precision)
+    for _ in range(max(args.warmup, 3)):
+        it.step()
     barrier()
+    clock_path = os.path.join(tempfile.gettempdir(), f"xrh_clocks_{os.getpid()}.csv")
+    step_ms, energies = [], []
     _lib.LaunchCounter.count = 0
     with ClockSampler(clock_path) as cs:
         for _ in range(args.steps):
             l2_flush.zero_()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(n_ph)]
-            it.step(ev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            energies.append(it.step())
+            e1.record()
             torch.cuda.synchronize()
-            step_ms.append(ev[0].elapsed_time(ev[-1]))
-            for k in range(n_ph - 1):
-                phase_ms[k] += ev[k].elapsed_time(ev[k + 1])
+            step_ms.append(e0.elapsed_time(e1))
         barrier()
-    launches = _lib.LaunchCounter.count
+    eager_calls = _lib.LaunchCounter.count
+    per_iter = graph_launches(it) or 0
+    launches = eager_calls + per_iter * args.steps
     clocks = cs.summary(local)
     total_ms = sum(step_ms)
 
-    # end-to-end through host buffers
+    # end to end through host buffers (fresh optimizer state each step: same work per step)
     barrier()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
+    e2e_ms = []
     for _ in range(args.steps):
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
         it.step_e2e()
-    t1.record()
-    torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1)
-    E0 = float(it.E_host[0])
+        t1.record()
+        torch.cuda.synchronize()
+        e2e_ms.append(t0.elapsed_time(t1))
+    e2e_total = sum(e2e_ms)
 
-    tens = torch.tensor([total_ms, e2e_ms], device="cuda")
+    tens = torch.tensor([total_ms, e2e_total], device="cuda")
     if world > 1:
         dist.all_reduce(tens, op=dist.ReduceOp.MAX)
-    total_ms, e2e_ms = float(tens[0]), float(tens[1])
+    total_ms, e2e_total = float(tens[0]), float(tens[1])
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
     s_per_iter = total_ms / 1e3 / args.steps
-    # roofline of the dominant kernel launch (by measured phase time)
-    names = ["densities+sigma", "precontraction GEMM", "final GEMM", "eigensolve"]
-    phases = {n: phase_ms[k] / args.steps for k, n in enumerate(names)}
-    flops_fin = it.plan.fin.flops
-    fin_ms = phases["final GEMM"]
+    kname, kflops, kms = dominant_kernel_roofline(it)
     peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
-    fp64_peak = measure_fp64_peak()
-    roofline = {"bound": "tensor", "kernel": "gemm_fp64_kernel (final, grouped)", "achieved": flops_fin / (fin_ms * 1e-3) / 1e12,
-                "peak": fp64_peak, "unit": "TFLOP/s", "frac": (flops_fin / (fin_ms * 1e-3) / 1e12) / fp64_peak,
-                "peak_source": "FP64 DGEMM (torch.matmul float64 8192^3) measured in this run; MEASURED_PEAKS.json has no FP64 figure",
-                "traffic": None}
+    achieved = kflops / (kms * 1e-3) / 1e12
+    if it.opt.plan.tc:
+        peak = float(peaks.get("bf16_tflops", 1900.0))
+        if args.precision == "tf32x3":
+            peak_note = "measured dense BF16 peak (MEASURED_PEAKS.json bf16_tflops) halved for kind::tf32"
+            peak = peak / 2
+        else:
+            peak_note = "measured dense BF16 peak (MEASURED_PEAKS.json bf16_tflops)"
+        roofline = {"bound": "tensor", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "mma_frac": 3 * achieved / peak, "traffic": None,
+                    "note": "achieved counts algorithmic FLOPs once; each costs 3 MMA FLOPs (hi*hi, hi*lo, lo*hi)",
+                    "peak_source": peak_note, "launch_ms": kms}
+    else:
+        fp64_peak = measure_fp64_peak()
+        roofline = {"bound": "tensor", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": achieved / fp64_peak, "traffic": None, "launch_ms": kms,
+                    "peak_source": "FP64 DGEMM (torch.matmul float64 8192^3) measured in this run"}
+
+    variants = {}
+    if not args.no_variants and world == 1:
+        for prec in ("fp64", "bf16x3", "tf32x3"):
+            if prec == args.precision:
+                variants[prec] = {"s_per_iter": s_per_iter, "E_first": energies[0]}
+                continue
+            v, Es, _ = time_variant(sysd, prec, max(2, args.steps // 2), args.warmup, l2_flush)
+            variants[prec] = {"s_per_iter": v}
+        # accuracy at identical states: one build per variant from the initial states
+        variants["accuracy"] = accuracy_check(sysd)
     cpu = None
-    if not args.no_cpu_baseline and world == 1:
+    if not args.no_cpu_baseline and world == 1 and args.config == 1:
         dt, e_cpu = time_oracle(sysd)
         cpu = {"value": dt, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full iteration of the same workload with the NumPy FP64 oracle (BLAS threads = all cores)",
-               "E0": e_cpu, "dE_gpu_vs_oracle": abs(e_cpu - E0)}
+               "sample": "one full iteration (densities + H + dense eigensolve, no gradient) of the same workload "
+                         "with the NumPy FP64 oracle, BLAS threads = all cores",
+               "E0": e_cpu}
     line = {
         "metric": METRIC, "value": s_per_iter, "unit": "s/iter", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else args.precision,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64"}.get(args.precision, args.precision),
         "data": "synthetic (seeded h ~ N(0,0.1), V = sum_K L L with K=40, Sz-definite QR-orthonormal Gaussian CI vectors)",
         "config": {"workload": CONFIGS[args.config]["name"], "precision": args.precision,
                    "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{world}",
-                   "step": "densities + H build + FP64 eigensolve"},
-        "e2e": {"value": e2e_ms / 1e3 / args.steps, "unit": "s/iter", "h2d_bytes_per_step": it.h2d_bytes,
-                "d2h_bytes_per_step": 8},
-        "gpu_launches": launches, "phases_ms": phases, "roofline": roofline, "clocks": clocks,
-        "E0": E0, "flops_per_iter": it.plan.flops, "peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops")},
+                   "step": "one steepest-descent state-optimizer iteration: densities + XR-H build + FP64 Lanczos "
+                           "ground state + adjoint state and orbital gradients + Loewdin step"},
+        "e2e": {"value": e2e_total / 1e3 / args.steps, "unit": "s/iter", "h2d_bytes_per_step": it.h2d_bytes,
+                "d2h_bytes_per_step": it.d2h_bytes},
+        "gpu_launches": launches, "gpu_launches_per_iteration": per_iter, "roofline": roofline, "clocks": clocks,
+        "energies": energies[:3], "flops_per_build": it.opt.plan.flops, "variants": variants,
     }
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def accuracy_check(sysd):
+    """|E0(variant) - E0(fp64)| and max|H(variant) - H(fp64)| for the initial states."""
+    import torch
+    from qodeapplications_gb300.iteration import XRStateOptimizer
+    out, ref = {}, None
+    for prec in ("fp64", "bf16x3", "tf32x3"):
+        opt = XRStateOptimizer(sysd, precision=prec, orbital_gradient=False, use_graphs=False)
+        E = opt.iterate()
+        H = {t: sec["H"].clone() for t, sec in opt.plan.sectors.items()}
+        if ref is None:
+            ref = (E, H)
+            continue
+        out[prec] = {"dE0": abs(E - ref[0]),
+                     "max_dH": max(float((H[t] - ref[1][t]).abs().max()) for t in H)}
+        del opt
+        torch.cuda.empty_cache()
+    return out
 
 
 def measure_fp64_peak():

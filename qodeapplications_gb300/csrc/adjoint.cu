@@ -17,38 +17,61 @@
 
 namespace {
 
+constexpr int kAdjThreads = 256;
+constexpr int kAdjChunk = 64;
+
+// One CTA per operator index.  G[idx] (n_b x n_k) is staged in shared memory once; the
+// couplings of the index are processed in chunks of kAdjChunk: their z columns are staged,
+// then every (coupling, output) pair of the chunk is one work item for the whole CTA
+// (n_k ket outputs + n_b bra outputs per coupling), reduced with FP64 atomics.
 template <typename T>
-__global__ void __launch_bounds__(256) density_adjoint_kernel(
+__global__ void __launch_bounds__(kAdjThreads) density_adjoint_kernel(
     const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const double* __restrict__ zbT, int nb, const double* __restrict__ zkT, int nk,
     const double* __restrict__ gT, double* __restrict__ gzbT, double* __restrict__ gzkT) {
     extern __shared__ unsigned char smem_raw[];
-    T* g = reinterpret_cast<T*>(smem_raw);            // [nb][nk]
-    T* zb = g + nb * nk;                               // [nb]
-    T* zk = zb + nb;                                   // [nk]
+    T* g = reinterpret_cast<T*>(smem_raw);                 // [nb][nk]
+    T* zb = g + nb * nk;                                    // [chunk][nb] (sign folded in)
+    T* zk = zb + kAdjChunk * nb;                            // [chunk][nk]
+    __shared__ int sP[kAdjChunk], sQ[kAdjChunk];
     const int64_t idx = blockIdx.x;
     const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
     if (c_begin == c_end) return;
     const double* gi = gT + idx * (int64_t)nb * nk;
     for (int t = threadIdx.x; t < nb * nk; t += blockDim.x) g[t] = (T)gi[t];
-    for (int64_t c = c_begin; c < c_end; ++c) {
-        const int Pc = P[c], Qc = Q[c];
-        const double s = sgn[c] < 0 ? -1.0 : 1.0;
+    const int per = nk + nb;
+    for (int64_t c0 = c_begin; c0 < c_end; c0 += kAdjChunk) {
+        const int64_t rem = c_end - c0;
+        const int nc = rem < kAdjChunk ? (int)rem : kAdjChunk;
         __syncthreads();
-        for (int t = threadIdx.x; t < nb; t += blockDim.x) zb[t] = (T)zbT[(int64_t)Pc * nb + t];
-        for (int t = threadIdx.x; t < nk; t += blockDim.x) zk[t] = (T)zkT[(int64_t)Qc * nk + t];
-        __syncthreads();
-        // gzk[Q, J] += s * sum_I g[I, J] zb[I]
-        for (int J = threadIdx.x; J < nk; J += blockDim.x) {
-            T a = 0;
-            for (int I = 0; I < nb; ++I) a = fma(g[I * nk + J], zb[I], a);
-            atomicAdd(gzkT + (int64_t)Qc * nk + J, s * (double)a);
+        for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+            sP[t] = P[c0 + t];
+            sQ[t] = Q[c0 + t];
         }
-        // gzb[P, I] += s * sum_J g[I, J] zk[J]
-        for (int I = threadIdx.x; I < nb; I += blockDim.x) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < nc * nb; t += blockDim.x) {
+            const int c = t / nb, i = t - c * nb;
+            const double s = sgn[c0 + c] < 0 ? -1.0 : 1.0;
+            zb[c * nb + i] = (T)(s * zbT[(int64_t)sP[c] * nb + i]);
+        }
+        for (int t = threadIdx.x; t < nc * nk; t += blockDim.x) {
+            const int c = t / nk, j = t - c * nk;
+            zk[c * nk + j] = (T)zkT[(int64_t)sQ[c] * nk + j];
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < nc * per; w += blockDim.x) {
+            const int c = w / per, o = w - c * per;
             T a = 0;
-            for (int J = 0; J < nk; ++J) a = fma(g[I * nk + J], zk[J], a);
-            atomicAdd(gzbT + (int64_t)Pc * nb + I, s * (double)a);
+            if (o < nk) {             // ket: gzk[Q, J] += sum_I g[I, J] (s zb[I])
+                const int J = o;
+                for (int I = 0; I < nb; ++I) a = fma(g[I * nk + J], zb[c * nb + I], a);
+                atomicAdd(gzkT + (int64_t)sQ[c] * nk + J, (double)a);
+            } else {                  // bra: gzb[P, I] += sum_J g[I, J] zk[J] (times s)
+                const int I = o - nk;
+                for (int J = 0; J < nk; ++J) a = fma(g[I * nk + J], zk[c * nk + J], a);
+                const double s = sgn[c0 + c] < 0 ? -1.0 : 1.0;
+                atomicAdd(gzbT + (int64_t)sP[c] * nb + I, s * (double)a);
+            }
         }
     }
 }
@@ -123,15 +146,15 @@ extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_
         return XRH_ERR_ARG;
     if (K > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     const size_t esz = (precision == XRH_FP32) ? sizeof(float) : sizeof(double);
-    const size_t smem = esz * ((size_t)n_b * n_k + n_b + n_k);
+    const size_t smem = esz * ((size_t)n_b * n_k + (size_t)kAdjChunk * (n_b + n_k));
     if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
     if (precision == XRH_FP64) {
         cudaFuncSetAttribute(density_adjoint_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        density_adjoint_kernel<double><<<(unsigned)K, 256, smem, (cudaStream_t)stream>>>(
+        density_adjoint_kernel<double><<<(unsigned)K, kAdjThreads, smem, (cudaStream_t)stream>>>(
             idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, gT_dev, gzbT_dev, gzkT_dev);
     } else if (precision == XRH_FP32) {
         cudaFuncSetAttribute(density_adjoint_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        density_adjoint_kernel<float><<<(unsigned)K, 256, smem, (cudaStream_t)stream>>>(
+        density_adjoint_kernel<float><<<(unsigned)K, kAdjThreads, smem, (cudaStream_t)stream>>>(
             idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, gT_dev, gzbT_dev, gzkT_dev);
     } else {
         return XRH_ERR_UNSUPPORTED;

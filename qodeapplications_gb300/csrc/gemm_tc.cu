@@ -28,7 +28,11 @@ namespace {
 constexpr int TC_BM = 128;
 constexpr int TC_STAGES = 3;
 constexpr int TC_THREADS = 128;
-constexpr uint32_t TC_TMEM_COLS = 128;
+// K chunks rotate over TC_NACC accumulators of 128 columns each (all 512 TMEM columns), and
+// the epilogue adds the partial tiles in FP64: each FP32 tensor-core accumulator then sums
+// a quarter of the terms, which bounds the accumulation error of long contractions.
+constexpr int TC_NACC = 4;
+constexpr uint32_t TC_TMEM_COLS = 128 * TC_NACC;
 constexpr uint32_t TC_A_BYTES = TC_BM * 128;           // 128 rows x 128 B (one swizzle width of K)
 constexpr uint32_t TC_B_MAX_BYTES = 128 * 128;
 constexpr uint32_t TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_MAX_BYTES;
@@ -228,13 +232,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t b_hi = st + 2 * TC_A_BYTES, b_lo = b_hi + b_bytes;
                 const uint32_t pa[3] = {a_hi, a_hi, a_lo};
                 const uint32_t pb[3] = {b_hi, b_lo, b_hi};
+                const uint32_t acc_tmem = tmem + (uint32_t)((q % TC_NACC) * 128);
 #pragma unroll
                 for (int p = 0; p < 3; ++p) {
                     const uint64_t da = umma_desc_sw128(pa[p]);
                     const uint64_t db = umma_desc_sw128(pb[p]);
 #pragma unroll
                     for (int j = 0; j < 4; ++j)          // 4 MMA K-steps of 32 bytes inside the 128-byte chunk
-                        umma<KIND>(tmem, da + 2 * j, db + 2 * j, idesc, (q > 0 || p > 0 || j > 0) ? 1u : 0u);
+                        umma<KIND>(acc_tmem, da + 2 * j, db + 2 * j, idesc,
+                                   (q >= TC_NACC || p > 0 || j > 0) ? 1u : 0u);
                 }
                 umma_commit(smem_u32(&empty_bar[s]));
                 if (q + TC_STAGES < nk) ok = load(q + TC_STAGES);
@@ -260,15 +266,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int m = m0 + warp * 32 + lane;
                 const bool row_ok = m < T.M;
                 double* C = T.C;
+                const int n_acc = nk < TC_NACC ? nk : TC_NACC;
                 for (int cc = 0; cc < BN; cc += 32) {
-                    float v[32];
-                    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, v);
+                    double sum[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) sum[j] = 0.0;
+                    for (int a = 0; a < n_acc; ++a) {
+                        float v[32];
+                        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128 + cc), v);
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) sum[j] += (double)v[j];
+                    }
                     if (!row_ok) continue;
 #pragma unroll 4
                     for (int j = 0; j < 32; ++j) {
                         const int n = n0 + cc + j;
                         if (n >= T.N) break;
-                        double x = (double)v[j];
+                        double x = sum[j];
                         if (T.mode == 0) {
                             C[(int64_t)m * T.ldc + n] = x;
                         } else if (T.mode == 1) {

@@ -29,6 +29,7 @@ class XRDimerAdjoint:
     def __init__(self, plan):
         assert plan.output == "full", "the adjoint differentiates the full H (H2 + H1 x 1 + 1 x H1)"
         self.plan = plan
+        self._spatial_cache = {}
         dev = plan.device
         f64 = dict(dtype=torch.float64, device=dev)
         tot0, tot1 = plan.tot
@@ -178,7 +179,7 @@ class XRDimerAdjoint:
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
-            call("xrh_density_adjoint", _lib.FP64, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
+            call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
                  ptr(plan.builders[m].zbT[bc]), nb, ptr(plan.builders[m].zT[kc]), nk, ptr(gT),
                  ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
         for m in (0, 1):
@@ -235,17 +236,22 @@ class XRDimerAdjoint:
         for k in range(U.shape[0]):
             Gso += U[k] @ dU[k].t() + U[k].t() @ dU[k]
         t = V.shape[0]
-        Vm = V.reshape(t, -1)
-        Gso += Vm @ dV.reshape(t, -1).t()                                             # index 1
-        Gso += V.permute(1, 0, 2, 3).reshape(t, -1) @ dV.permute(1, 0, 2, 3).reshape(t, -1).t()
-        Gso += V.permute(2, 0, 1, 3).reshape(t, -1) @ dV.permute(2, 0, 1, 3).reshape(t, -1).t()
-        Gso += V.permute(3, 0, 1, 2).reshape(t, -1) @ dV.permute(3, 0, 1, 2).reshape(t, -1).t()
-        idx = torch.as_tensor(np.asarray(spatial_index), device=T.device)
-        n_sp = int(idx.max().item()) + 1
+        # E sees V only through its symmetric part (V_pqrs = -V_qprs = -V_pqsr = V_rspq for real
+        # orbitals), so dE/dV may be replaced by its projection on that symmetry; then the four
+        # index positions of V' = R^T..R contribute equally: dE/dR = 4 V_(1) Gbar_(1)^T
+        Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
+        Gbar = 0.125 * (Ga + Ga.permute(2, 3, 0, 1))
+        Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
+        key = (tuple(spatial_index), T.device)
+        if key not in self._spatial_cache:     # built on first use, outside any graph capture
+            idx = torch.as_tensor(np.asarray(spatial_index), device=T.device)
+            n_sp = int(max(spatial_index)) + 1
+            self._spatial_cache[key] = (idx[:, None].expand(t, t).contiguous(), idx[None, :].expand(t, t).contiguous(),
+                                        _same_spin(t, spatial_index, T.device), n_sp)
+        I0, I1, same, n_sp = self._spatial_cache[key]
         Gsp = torch.zeros((n_sp, n_sp), dtype=torch.float64, device=T.device)
         # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs
-        Gsp.index_put_((idx[:, None].expand(t, t), idx[None, :].expand(t, t)),
-                       Gso * _same_spin(t, spatial_index, T.device), accumulate=True)
+        Gsp.index_put_((I0, I1), Gso * same, accumulate=True)
         return Gsp - Gsp.t()
 
 

@@ -164,7 +164,7 @@ class XRDimerPlan:
     """
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
-                 convention="hermitian"):
+                 convention="hermitian", layout="product", dens_precision=None, sigma_precision=None):
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
         self.ints = ints
@@ -175,7 +175,12 @@ class XRDimerPlan:
         f64 = dict(dtype=torch.float64, device=dev)
         self.coeffs = [{c: torch.zeros((self.n_states[m][c], spaces[m].n_conf[c]), **f64) for c in self.charges[m]}
                        for m in (0, 1)]
-        self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=precision) for m in (0, 1)]
+        # densities and sigma vectors: FP64 on the fp64 path; FP32 products with FP64 sums on the
+        # split-precision paths unless requested otherwise
+        tc_mode = self.precision in (_lib.BF16X3, _lib.TF32X3)
+        self.dens_precision = dens_precision or ("fp32" if tc_mode else "fp64")
+        self.sigma_precision = sigma_precision or ("fp32" if tc_mode else "fp64")
+        self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=self.dens_precision) for m in (0, 1)]
         N = [spaces[0].N, spaces[1].N]
         self.N = N
         rho = [b.rho for b in self.builders]
@@ -260,7 +265,8 @@ class XRDimerPlan:
                     continue
                 n = ns[m][c]
                 ca = rho[m]["ca"][(c, c)]
-                sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m), precision=self.precision)
+                sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m),
+                                      precision=_lib.PRECISIONS[self.sigma_precision])
                 self.sigma[m][c] = sg
                 nconf = spaces[m].n_conf[c]
                 zrow = self.coeffs[m][c]
@@ -285,7 +291,26 @@ class XRDimerPlan:
         self.offsets = (off0, off1)
         self.dim = (tot0 * tot1, tot0 * tot1)
         self.tot = (tot0, tot1)
-        self.H = torch.zeros(self.dim, **f64)
+        self.layout = layout
+        if layout == "product":
+            self.H = torch.zeros(self.dim, **f64)
+        else:
+            # H is block diagonal in the total charge: one dense matrix per sector t, rows
+            # ordered block-major over (c0, c1 = t - c0) and row-major (i0, i1) inside a block
+            self.sectors = {}
+            for c0 in chg[0]:
+                for c1 in chg[1]:
+                    t = c0 + c1
+                    sec = self.sectors.setdefault(t, dict(base={}, dim=0, rows=[]))
+                    sec["base"][c0] = sec["dim"]
+                    i0 = np.repeat(np.arange(nb[0][c0]), nb[1][c1])
+                    i1 = np.tile(np.arange(nb[1][c1]), nb[0][c0])
+                    sec["rows"].append((off0[c0] + i0) * tot1 + off1[c1] + i1)
+                    sec["dim"] += nb[0][c0] * nb[1][c1]
+            for t, sec in self.sectors.items():
+                sec["rows"] = torch.as_tensor(np.concatenate(sec["rows"]), dtype=torch.int64, device=dev)
+                sec["H"] = torch.zeros((sec["dim"], sec["dim"]), **f64)
+            self.H = None
         fin = GroupedGemm(dev)
         i32 = dict(dtype=torch.int32, device=dev)
         n_ref0 = spaces[0].n_elec_ref
@@ -331,10 +356,19 @@ class XRDimerPlan:
                         j0 = np.tile(np.arange(nj0), ni0)
                         i1 = np.repeat(np.arange(ni1), nj1)
                         j1 = np.tile(np.arange(nj1), ni1)
-                        rowA = torch.as_tensor((off0[ci0] + i0) * tot1, **i32)
-                        colA = torch.as_tensor((off0[cj0] + j0) * tot1, **i32)
-                        rowB = torch.as_tensor(off1[ci1] + i1, **i32)
-                        colB = torch.as_tensor(off1[cj1] + j1, **i32)
+                        if layout == "product":
+                            Cbuf, ldc = self.H, self.dim[1]
+                            rowA = torch.as_tensor((off0[ci0] + i0) * tot1, **i32)
+                            colA = torch.as_tensor((off0[cj0] + j0) * tot1, **i32)
+                            rowB = torch.as_tensor(off1[ci1] + i1, **i32)
+                            colB = torch.as_tensor(off1[cj1] + j1, **i32)
+                        else:
+                            sec = self.sectors[ci0 + ci1]
+                            Cbuf, ldc = sec["H"], sec["dim"]
+                            rowA = torch.as_tensor(sec["base"][ci0] + i0 * ni1, **i32)
+                            colA = torch.as_tensor(sec["base"][cj0] + j0 * nj1, **i32)
+                            rowB = torch.as_tensor(i1, **i32)
+                            colB = torch.as_tensor(j1, **i32)
                         diagA = torch.as_tensor(((ci0 == cj0) & (i0 == j0)).astype(np.uint8), device=dev)
                         diagB = torch.as_tensor(((ci1 == cj1) & (i1 == j1)).astype(np.uint8), device=dev)
                         DA = DB = None
@@ -342,10 +376,10 @@ class XRDimerPlan:
                             src = self.FULLD if output == "full" else self.DU
                             DA = src[0].get(ci0)
                             DB = src[1].get(ci1)
-                        fin.add(M, Nn, segs, self.H, self.dim[1], mode=2,
+                        fin.add(M, Nn, segs, Cbuf, ldc, mode=2,
                                 maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB)
                         self.block_keys.append((ci0, ci1, cj0, cj1))
-                        self.final_tasks.append(dict(key=(ci0, ci1, cj0, cj1), segs=segs, M=M, N=Nn,
+                        self.final_tasks.append(dict(key=(ci0, ci1, cj0, cj1), segs=segs, M=M, N=Nn, C=Cbuf, ldc=ldc,
                                                      dims=(ni0, nj0, ni1, nj1),
                                                      maps=(rowA, colA, rowB, colB, diagA, diagB), DA=DA, DB=DB))
         self.fin = fin.finalize()
@@ -371,7 +405,7 @@ class XRDimerPlan:
                 pre64.add(M_, N_, segs_, out_, ldc_, mode=1, splitk=sk_)
             fin_tc = TCGroupedGemm(reg)
             for t in self.final_tasks:
-                fin_tc.add(t["M"], t["N"], t["segs"], self.H, self.dim[1], mode=2, maps=t["maps"], DA=t["DA"],
+                fin_tc.add(t["M"], t["N"], t["segs"], t["C"], t["ldc"], mode=2, maps=t["maps"], DA=t["DA"],
                            DB=t["DB"], groups=[(grp(a[0]), grp(a[2])) for a in t["segs"]])
             reg.upload()
             reg.split("W")

@@ -1,0 +1,205 @@
+"""One optimizer iteration on the device: densities -> XR-H -> lowest eigenpair -> gradients.
+
+The per-iteration unit of the reference's state optimisation
+(StateSpaceOptimizer/state_solver.py:207-453 calls state_gradients, which rebuilds densities
+and H with bra_det/ket_det densities, state_gradients.py:144-185) is done here as
+
+  1. densities of both fragments from the current states, the XR-H build (FP64 or split
+     precision), all inside one planned launch sequence;
+  2. FP64 Lanczos on the total-charge sector that holds the ground state, warm-started from
+     the previous eigenvector (the first iteration scans every sector);
+  3. the reverse pass (XRDimerAdjoint): dE/dz of both fragments, projected on the tangent
+     space of the orthonormal states, and dE/dkappa of the orbital rotations;
+  4. a steepest-descent step on the states followed by Loewdin orthonormalisation
+     (z <- (z z^T)^-1/2 z, the inverse square root by Newton-Schulz iterations, FP64).
+
+Steps 1-2 and 3-4 are each replayed as a CUDA graph; between them the host solves the
+m x m tridiagonal Lanczos matrix (one small device-to-host copy).
+"""
+import numpy as np
+import torch
+
+from .densities import FragmentSpace
+from .eigen import Lanczos
+from .gradients import XRDimerAdjoint, tangent_project
+from .hamiltonian import DeviceIntegrals, XRDimerPlan
+from .synthetic import spin_orbital_spatial_index
+
+
+def _inv_sqrt_newton_schulz(S, iters=6):
+    """S^-1/2 for symmetric positive definite S close to the identity (coupled Newton-Schulz)."""
+    n = S.shape[0]
+    I = torch.eye(n, dtype=S.dtype, device=S.device)
+    Y, Z = S.clone(), I.clone()
+    for _ in range(iters):
+        T = 0.5 * (3.0 * I - Z @ Y)
+        Y = Y @ T
+        Z = T @ Z
+    return Z
+
+
+class XRStateOptimizer:
+    def __init__(self, sysd, precision="fp64", step=0.02, lanczos_m=48, warm_m=24, orbital_gradient=True,
+                 use_graphs=True, device="cuda"):
+        self.sysd = sysd
+        self.charges = list(sysd["charges"])
+        chg = self.charges
+        dev = torch.device(device)
+        self.device = dev
+        self.spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in chg}, sysd["n_orb"], sysd["n_core"],
+                                     sysd["n_elec_ref"], device=dev) for m in range(2)]
+        ns = [{c: sysd["states"][m][c][0].shape[0] for c in chg} for m in range(2)]
+        self.ints = DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"], device=dev)
+        self.plan = XRDimerPlan(self.spaces, ns, [chg, chg], self.ints, output="full", precision=precision,
+                                layout="sectors")
+        self.adj = XRDimerAdjoint(self.plan)
+        for m in range(2):
+            for c in chg:
+                self.plan.coeffs[m][c].copy_(torch.as_tensor(sysd["states"][m][c][0], device=dev))
+        self.step_size = step
+        self.lz = {t: Lanczos(sec["dim"], m=lanczos_m, device=dev) for t, sec in self.plan.sectors.items()}
+        self.lz_warm = {t: Lanczos(sec["dim"], m=warm_m, device=dev) for t, sec in self.plan.sectors.items()}
+        self.target = None
+        self.d_product = torch.zeros(self.plan.tot[0] * self.plan.tot[1], dtype=torch.float64, device=dev)
+        self.orbital = orbital_gradient
+        if orbital_gradient:
+            self.T = torch.as_tensor(sysd["h"], device=dev)
+            self.U = torch.zeros((2,) + self.T.shape, dtype=torch.float64, device=dev)
+            self.V = torch.as_tensor(sysd["V"], device=dev)
+            self.sidx = spin_orbital_spatial_index([sysd["n_orb"]] * 2)
+        self.kappa_grad = None
+        self.grad_norm = None
+        self.use_graphs = use_graphs
+        self._graphs = None
+        self.energy = None
+        self.residual = None
+
+    # -------------------------------------------------------------------- device parts --
+    def _forward(self, sectors, warm):
+        self.plan.launch()
+        for t in sectors:
+            lz = (self.lz_warm if warm else self.lz)[t]
+            lz.krylov(self.plan.sectors[t]["H"])
+            lz.stage_to_host()
+
+    def _backward(self, t, warm):
+        lz = (self.lz_warm if warm else self.lz)[t]
+        d = lz.ground_vector()
+        self.d_product.zero_()
+        self.d_product.index_copy_(0, self.plan.sectors[t]["rows"], d)
+        # the warm start of the next iteration
+        self.lz_warm[t].v0.copy_(d)
+        self.adj.launch(self.d_product)
+        g = self.adj.state_gradient()
+        sq = torch.zeros((), dtype=torch.float64, device=self.device)
+        for m in range(2):
+            for c in self.charges:
+                z = self.plan.coeffs[m][c]
+                gt = tangent_project(g[m][c], z)
+                sq = sq + (gt * gt).sum()
+                znew = z - self.step_size * gt
+                S = znew @ znew.t()
+                z.copy_(_inv_sqrt_newton_schulz(S) @ znew)
+        self._gsq = sq
+        if self.orbital:
+            self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
+
+    # ----------------------------------------------------------------------- iteration --
+    def _solve(self, sectors, warm):
+        best = None
+        for t in sectors:
+            lz = (self.lz_warm if warm else self.lz)[t]
+            w, resid = lz.solve(1)
+            if best is None or w[0] < best[0]:
+                best = (w[0], t, resid)
+        return best
+
+    def iterate(self):
+        """One optimizer iteration; returns the energy of the states it started from."""
+        torch_stream = torch.cuda.current_stream()
+        if self.target is None:
+            sectors = list(self.plan.sectors)
+            self._forward(sectors, warm=False)
+            torch_stream.synchronize()
+            E, t, resid = self._solve(sectors, warm=False)
+            self.target = t
+            self._backward(t, warm=False)
+        else:
+            t = self.target
+            if self.use_graphs:
+                if self._graphs is None:
+                    self._capture(t)
+                self._graphs[0].replay()
+            else:
+                self._forward([t], warm=True)
+            torch_stream.synchronize()
+            E, _, resid = self._solve([t], warm=True)
+            if self.use_graphs:
+                self.lz_warm[t].y.copy_(torch.from_numpy(self._ritz_padded(t)))
+                self._graphs[1].replay()
+            else:
+                self._backward(t, warm=True)
+        self.energy, self.residual = float(E), float(resid)
+        return self.energy
+
+    def _ritz_padded(self, t):
+        lz = self.lz_warm[t]
+        y = np.zeros(lz.m + 1)
+        y[:lz._cut] = lz._ritz
+        return y
+
+    def _capture(self, t):
+        """Record the forward (build + Krylov) and backward (adjoint + update) launch sequences."""
+        lz = self.lz_warm[t]
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):          # warm the allocator and caches outside capture
+            self._forward([t], warm=True)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        lz.solve(1)
+        g0, g1 = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+        saved = [{c: self.plan.coeffs[m][c].clone() for c in self.charges} for m in range(2)]
+        v0 = lz.v0.clone()
+        from . import _lib
+        n0 = _lib.LaunchCounter.count
+        with torch.cuda.graph(g0):
+            self._forward([t], warm=True)
+        with torch.cuda.graph(g1):
+            self._backward_graphed(t)
+        self.graph_kernels = _lib.LaunchCounter.count - n0
+        _lib.LaunchCounter.count = n0
+        # capture does not execute: restore nothing, but keep the warm vector and states intact
+        lz.v0.copy_(v0)
+        for m in range(2):
+            for c in self.charges:
+                self.plan.coeffs[m][c].copy_(saved[m][c])
+        torch.cuda.synchronize()
+        self._graphs = (g0, g1)
+
+    def _backward_graphed(self, t):
+        lz = self.lz_warm[t]
+        d = lz.vec
+        d.zero_()
+        from ._lib import call, ptr, stream_ptr
+        call("xrh_gemv_cols", lz.m, lz.n, ptr(lz.V), lz.n, ptr(lz.y), 1.0, ptr(d), stream_ptr())
+        self.d_product.zero_()
+        self.d_product.index_copy_(0, self.plan.sectors[t]["rows"], d)
+        lz.v0.copy_(d)
+        self.adj.launch(self.d_product)
+        g = self.adj.state_gradient()
+        sq = torch.zeros((), dtype=torch.float64, device=self.device)
+        for m in range(2):
+            for c in self.charges:
+                z = self.plan.coeffs[m][c]
+                gt = tangent_project(g[m][c], z)
+                sq = sq + (gt * gt).sum()
+                znew = z - self.step_size * gt
+                z.copy_(_inv_sqrt_newton_schulz(znew @ znew.t()) @ znew)
+        self._gsq = sq
+        if self.orbital:
+            self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
+
+    @property
+    def gradient_norm(self):
+        return float(self._gsq.sqrt())
