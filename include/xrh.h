@@ -77,6 +77,15 @@ int xrh_density_accumulate(int precision, int64_t K, const int64_t* idx_ptr_dev,
                            const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
                            double* rhoT_dev, void* stream);
 
+/* FP32 variant of xrh_density_accumulate for the split-precision paths: coefficients given
+ * pre-converted to FP32 as zb32 [n_bra_conf, round_up(n_b,4)] and zk32 [n_ket_conf,
+ * round_up(n_k,4)] (rows padded with zeros, 16-byte aligned); FP32 products and chunk sums,
+ * FP64 running sums.  splits > 1 divides the couplings of every operator index over that
+ * many CTAs and ADDS to rhoT_dev, which must then be zeroed by the caller. */
+int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* idx_ptr_dev, const int32_t* P_dev,
+                               const int32_t* Q_dev, const int8_t* sign_dev, const float* zb32_dev, int n_b,
+                               const float* zk32_dev, int n_k, double* rhoT_dev, void* stream);
+
 /* Allocation-free transition densities (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- for example code running
  * inside another application's CUDA context whose allocator owns all device memory, or a
@@ -105,7 +114,13 @@ int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_
 int xrh_sigma2e(int precision, int n_orbs, const double* V_dev,
                 const uint64_t* bra_masks_dev, int n_bra_conf,
                 const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev, int n_ket_conf,
+                const int32_t* rank_table_dev, int64_t table_size, const int64_t* binom_dev,
                 const double* zkT_dev, int n_k, double* sigmaT_dev, void* stream);
+/* Determinant lookup in xrh_sigma2e and xrh_ccaa_weighted: with rank_table_dev == NULL, a
+ * binary search of the sorted ket list; otherwise rank_table_dev[colex_rank(mask)] (size
+ * table_size = C(N, n_e), -1 for determinants not in the list) with
+ * colex_rank = sum_i C(o_i, i+1) over the occupied spin orbitals o_0 < o_1 < ..., and
+ * binom_dev[n*17 + k] = C(n, k) for n <= 64, k <= 16. */
 
 /* Grouped GEMM with K-concatenated segments and an FP64 epilogue.
  * For each task t and each (m, n) in [0,M) x [0,N):
@@ -154,6 +169,11 @@ typedef struct {
 
 int xrh_gemm_fp64_grouped(const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
                           const xrh_gemm_segment* segs_dev, void* stream);
+/* Same tasks with a choice of arithmetic on CUDA cores: XRH_FP64 (identical to
+ * xrh_gemm_fp64_grouped) or XRH_FP32 (operands rounded to FP32, products and the partial
+ * sum of each 16-wide K step in FP32, running sums and epilogue in FP64). */
+int xrh_gemm_simt_grouped(int precision, const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
+                          const xrh_gemm_segment* segs_dev, void* stream);
 
 /* FP64 Lanczos building blocks for the lowest eigenpairs of H (replaces the dense
  * scipy.linalg.eig of hermitian-XRCC/mains/workflow.py:229 and
@@ -171,22 +191,26 @@ int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double*
  * over the same coupling lists; replaces the determinant-bra density rebuild plus second H
  * build of StateSpaceOptimizer/state_gradients.py:164-185.  gT_dev is dE/drho in
  * [K, n_b, n_k] layout; results are ADDED (atomically) to gzbT_dev [n_bra_conf, n_b] and
- * gzkT_dev [n_ket_conf, n_k], which may be the same buffer.  precision XRH_FP64 or XRH_FP32. */
+ * gzkT_dev [n_ket_conf, n_k], which may be the same buffer: double arrays for XRH_FP64,
+ * float arrays for XRH_FP32 (FP32 products and sums, 16-byte vector atomics).  For XRH_FP32
+ * the coefficients zbT_dev/zkT_dev are the padded FP32 copies of xrh_density_accumulate_f32
+ * (rows of round_up(n,4) floats); for XRH_FP64 the double [n_conf, n] arrays. */
 int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev,
                         const int32_t* P_dev, const int32_t* Q_dev, const int8_t* sign_dev,
-                        const double* zbT_dev, int n_b, const double* zkT_dev, int n_k,
-                        const double* gT_dev, double* gzbT_dev, double* gzkT_dev, void* stream);
+                        const void* zbT_dev, int n_b, const void* zkT_dev, int n_k,
+                        const double* gT_dev, void* gzbT_dev, void* gzkT_dev, void* stream);
 
 /* Two-particle density of a weighted ensemble for the monomer two-electron term:
  *   Gamma[p,q,r,s] += sum_{P,Q} W[P,Q] <P| c+_p c+_q a_s a_r |Q>,  p<q and r<s only,
  *   W[P,Q] = sum_I zbT[P, I] YT[Q, I]   (Y = G . z for weights G over state pairs)
  * i.e. dE/dV for E = sum_IJ G_IJ sum_pqrs V_pqrs rho^ccaa_IJ[p,q,s,r] (orb_grads.py:921
  * two_p_dens for the intra-fragment term) without the N^4 density.  Gamma_dev is N^4
- * (N = 2 n_orbs), accumulated atomically; the caller fills the other index orders by
- * antisymmetry.  n <= 256 states. */
-int xrh_ccaa_weighted(int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
+ * (N = 2 n_orbs) doubles (XRH_FP64) or floats (XRH_FP32), accumulated atomically; the
+ * caller fills the other index orders by antisymmetry.  n <= 256 states. */
+int xrh_ccaa_weighted(int precision, int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
                       const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev, int n_ket_conf,
-                      const double* zbT_dev, const double* YT_dev, int n, double* Gamma_dev, void* stream);
+                      const int32_t* rank_table_dev, int64_t table_size, const int64_t* binom_dev,
+                      const double* zbT_dev, const double* YT_dev, int n, void* Gamma_dev, void* stream);
 
 /* ---- split-precision tensor-core path (tcgen05, sm_103a) -------------------------------
  * Same task model as xrh_gemm_fp64_grouped for the forward build.  Every FP64 operand is

@@ -30,14 +30,16 @@ _SIGS = {
     "xrh_couplings_fill": (_i32, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "xrh_density_accumulate": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_transpose": (_i32, [_vp, _i64, _i64, _vp, _vp]),
+    "xrh_density_accumulate_f32": (_i32, [_i64, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
     "xrh_density_build_noalloc": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
-    "xrh_sigma2e": (_i32, [_i32, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _i32, _vp, _vp]),
+    "xrh_sigma2e": (_i32, [_i32, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _i64, _vp, _vp, _i32, _vp, _vp]),
     "xrh_gemm_fp64_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
+    "xrh_gemm_simt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp, _vp]),
     "xrh_gemv_rows": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _dbl, _vp, _vp]),
     "xrh_gemv_cols": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _vp, _vp]),
     "xrh_lanczos_normalize": (_i32, [_i64, _vp, _vp, _vp, _vp]),
     "xrh_density_adjoint": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
-    "xrh_ccaa_weighted": (_i32, [_i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),
+    "xrh_ccaa_weighted": (_i32, [_i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _i64, _vp, _vp, _vp, _i32, _vp, _vp]),
     "xrh_tc_chunk_elems": (_i32, [_i32]),
     "xrh_split_operand": (_i32, [_i32, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),
     "xrh_tc_encode_map": (_i32, [_i32, _vp, _i64, _i64, _i32, _vp]),
@@ -78,7 +80,7 @@ def register(name, restype, argtypes):
 
 class LaunchCounter:
     """Counts library calls that launch one kernel each (the gpu_launches figure)."""
-    launching = {"xrh_density_accumulate", "xrh_transpose", "xrh_sigma2e", "xrh_gemm_fp64_grouped",
+    launching = {"xrh_density_accumulate", "xrh_density_accumulate_f32", "xrh_transpose", "xrh_sigma2e", "xrh_gemm_fp64_grouped", "xrh_gemm_simt_grouped",
                  "xrh_couplings_count", "xrh_couplings_fill", "xrh_gemv_rows", "xrh_gemv_cols",
                  "xrh_lanczos_normalize", "xrh_density_adjoint", "xrh_ccaa_weighted", "xrh_split_operand",
                  "xrh_gemm_tc_grouped"}

@@ -76,16 +76,156 @@ __global__ void __launch_bounds__(kAdjThreads) density_adjoint_kernel(
     }
 }
 
+// FP32 variant for the split-precision paths.  Per chunk of 64 couplings of one operator
+// index, the ket and bra results are two small GEMMs against G[idx]:
+//   U[c, J] = sum_I (s_c zb[I, P_c]) G[I, J],   W[c, I] = s_c sum_J G[I, J] zk[J, Q_c]
+// computed in 4 couplings x 4 outputs register tiles from shared memory laid out so that every
+// load is a 16-byte vector (G in both orientations, staged z columns transposed), and reduced
+// into FP32 gradient rows with 16-byte vector atomics.
+__device__ __forceinline__ void atomic_add4(float* dst, const float (&v)[4], int valid) {
+    if (valid == 4 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(v[0], v[1], v[2], v[3]));
+    } else {
+        for (int k = 0; k < valid; ++k) atomicAdd(dst + k, v[k]);
+    }
+}
+
+__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
+    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+    const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
+    const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT) {
+    // coefficient rows come pre-converted to FP32 and padded to nbp/nkp (16-byte rows), so the
+    // z rows of a chunk are gathered with cp.async into a double-buffered ring while the
+    // previous chunk is multiplied
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
+    float* g = reinterpret_cast<float*>(smem_raw);          // [nbp][nkp]
+    float* gt = g + nbp * nkp;                              // [nkp][nbp]
+    float* zb_s = gt + nkp * nbp;                           // [2][chunk][nbp]
+    float* zk_s = zb_s + 2 * kAdjChunk * nbp;               // [2][chunk][nkp]
+    __shared__ int sP[2][kAdjChunk], sQ[2][kAdjChunk];
+    __shared__ float sS[2][kAdjChunk];
+    const int64_t idx = blockIdx.x;
+    const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
+    if (c_begin == c_end) return;
+    const double* gi = gT + idx * (int64_t)nb * nk;
+    for (int t = threadIdx.x; t < nbp * nkp; t += blockDim.x) {
+        const int i = t / nkp, j = t - i * nkp;
+        const float v = (i < nb && j < nk) ? (float)gi[i * nk + j] : 0.f;
+        g[t] = v;
+        gt[j * nbp + i] = v;
+    }
+    const int n_chunks = (int)((c_end - c_begin + kAdjChunk - 1) / kAdjChunk);
+    const int gb = nbp / 4, gk = nkp / 4;
+    auto load_idx = [&](int k, int buf) {
+        const int64_t c0 = c_begin + (int64_t)k * kAdjChunk;
+        for (int t = threadIdx.x; t < kAdjChunk; t += blockDim.x) {
+            const int64_t c = c0 + t;
+            const bool ok = c < c_end;
+            sP[buf][t] = ok ? P[c] : -1;
+            sQ[buf][t] = ok ? Q[c] : -1;
+            sS[buf][t] = ok ? (sgn[c] < 0 ? -1.f : 1.f) : 0.f;
+        }
+    };
+    auto stage = [&](int buf) {
+        float* zbb = zb_s + buf * kAdjChunk * nbp;
+        float* zkb = zk_s + buf * kAdjChunk * nkp;
+        for (int x = threadIdx.x; x < kAdjChunk * gb; x += blockDim.x) {
+            const int c = x / gb, part = x - c * gb;
+            const int p = sP[buf][c];
+            if (p >= 0) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)p * nbp + part * 4);
+            else *reinterpret_cast<float4*>(zbb + c * nbp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        for (int x = threadIdx.x; x < kAdjChunk * gk; x += blockDim.x) {
+            const int c = x / gk, part = x - c * gk;
+            const int q = sQ[buf][c];
+            if (q >= 0) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)q * nkp + part * 4);
+            else *reinterpret_cast<float4*>(zkb + c * nkp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        cp_async_commit();
+    };
+    const int tj = nkp / 4, ti = nbp / 4;
+    const int ket_tiles = (kAdjChunk / 4) * tj, bra_tiles = (kAdjChunk / 4) * ti;
+    __syncthreads();
+    load_idx(0, 0);
+    __syncthreads();
+    stage(0);
+    for (int k = 0; k < n_chunks; ++k) {
+        const int buf = k & 1;
+        __syncthreads();                             // chunk k-1 (buffer buf ^ 1) fully consumed
+        if (k + 1 < n_chunks) load_idx(k + 1, buf ^ 1);
+        __syncthreads();                             // indices of k+1 visible
+        if (k + 1 < n_chunks) {
+            stage(buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const float* zbb = zb_s + buf * kAdjChunk * nbp;
+        const float* zkb = zk_s + buf * kAdjChunk * nkp;
+        for (int w = threadIdx.x; w < ket_tiles + bra_tiles; w += blockDim.x) {
+            float acc[4][4] = {};
+            if (w < ket_tiles) {            // U[c, J] = s_c sum_I zb[c, I] G[I, J]
+                const int c4 = (w / tj) * 4, j4 = (w % tj) * 4;
+                for (int I = 0; I < nb; ++I) {
+                    const float4 b = *reinterpret_cast<const float4*>(g + I * nkp + j4);
+                    const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) {
+                        const float a = zbb[(c4 + x) * nbp + I];
+#pragma unroll
+                        for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a, bv[y], acc[x][y]);
+                    }
+                }
+                const int valid = nk - j4 < 4 ? nk - j4 : 4;
+                for (int x = 0; x < 4; ++x) {
+                    const int q = sQ[buf][c4 + x];
+                    if (q < 0) continue;
+                    const float sc = sS[buf][c4 + x];
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
+                    atomic_add4(gzkT + (int64_t)q * nk + j4, acc[x], valid);
+                }
+            } else {                        // W[c, I] = s_c sum_J G[I, J] zk[c, J]
+                const int wb = w - ket_tiles;
+                const int c4 = (wb / ti) * 4, i4 = (wb % ti) * 4;
+                for (int J = 0; J < nk; ++J) {
+                    const float4 b = *reinterpret_cast<const float4*>(gt + J * nbp + i4);
+                    const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) {
+                        const float a = zkb[(c4 + x) * nkp + J];
+#pragma unroll
+                        for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a, bv[y], acc[x][y]);
+                    }
+                }
+                const int valid = nb - i4 < 4 ? nb - i4 : 4;
+                for (int x = 0; x < 4; ++x) {
+                    const int p = sP[buf][c4 + x];
+                    if (p < 0) continue;
+                    const float sc = sS[buf][c4 + x];
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
+                    atomic_add4(gzbT + (int64_t)p * nb + i4, acc[x], valid);
+                }
+            }
+        }
+    }
+}
+
 constexpr int kWThreads = 128;
 
+template <typename T>
 __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
     int N, const uint64_t* __restrict__ bra, int n_bra, const uint64_t* __restrict__ ket_sorted,
-    const int32_t* __restrict__ ket_pos, int n_ket, const double* __restrict__ zbT, const double* __restrict__ YT,
-    int n, double* __restrict__ Gamma) {
+    const int32_t* __restrict__ ket_pos, int n_ket, const int32_t* __restrict__ rank_table, int64_t table_size,
+    const int64_t* __restrict__ binom, const double* __restrict__ zbT, const double* __restrict__ YT,
+    int n, T* __restrict__ Gamma) {
     __shared__ int s_occ[64];
     __shared__ int s_free[64];
     __shared__ int s_ne, s_nfree;
-    __shared__ double s_zb[256];
+    __shared__ T s_zb[256];
     const int Pb = blockIdx.x;
     const uint64_t m = bra[Pb];
     if (threadIdx.x == 0) {
@@ -94,7 +234,7 @@ __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
             if ((m >> o) & 1ull) s_occ[k++] = o;
         s_ne = k;
     }
-    for (int t = threadIdx.x; t < n; t += blockDim.x) s_zb[t] = zbT[(int64_t)Pb * n + t];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s_zb[t] = (T)zbT[(int64_t)Pb * n + t];
     __syncthreads();
     const int ne = s_ne;
     for (int a = 0; a < ne; ++a) {
@@ -123,12 +263,17 @@ __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
                 int s2 = s1;
                 xrh_apply(1, s, m2, s2);
                 xrh_apply(1, r, m2, s2);
-                const int hit = xrh_lookup(ket_sorted, n_ket, m2);
-                if (hit < 0) continue;
-                const int Qp = __ldg(ket_pos + hit);
-                double w = 0.0;
-                for (int I = 0; I < n; ++I) w = fma(s_zb[I], YT[(int64_t)Qp * n + I], w);
-                if (w == 0.0) continue;
+                int Qp;
+                if (rank_table) {
+                    Qp = xrh_rank_lookup(rank_table, table_size, binom, m2);
+                } else {
+                    const int hit = xrh_lookup(ket_sorted, n_ket, m2);
+                    Qp = hit < 0 ? -1 : __ldg(ket_pos + hit);
+                }
+                if (Qp < 0) continue;
+                T w = 0;
+                for (int I = 0; I < n; ++I) w = fma(s_zb[I], (T)YT[(int64_t)Qp * n + I], w);
+                if (w == (T)0) continue;
                 // <P| c+_p c+_q a_s a_r |Q>  (p<q, r<s) = sign of <Q| c+_r c+_s a_q a_p |P>
                 atomicAdd(Gamma + (((int64_t)p * N + q) * N + r) * N + s, s2 ? -w : w);
             }
@@ -139,9 +284,9 @@ __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
 }  // namespace
 
 extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev, const int32_t* P_dev,
-                                   const int32_t* Q_dev, const int8_t* sign_dev, const double* zbT_dev, int n_b,
-                                   const double* zkT_dev, int n_k, const double* gT_dev, double* gzbT_dev,
-                                   double* gzkT_dev, void* stream) {
+                                   const int32_t* Q_dev, const int8_t* sign_dev, const void* zbT_dev, int n_b,
+                                   const void* zkT_dev, int n_k, const double* gT_dev, void* gzbT_dev,
+                                   void* gzkT_dev, void* stream) {
     if (K <= 0 || n_b <= 0 || n_k <= 0 || !idx_ptr_dev || !zbT_dev || !zkT_dev || !gT_dev || !gzbT_dev || !gzkT_dev)
         return XRH_ERR_ARG;
     if (K > 0x7fffffffLL) return XRH_ERR_CAPACITY;
@@ -151,11 +296,19 @@ extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_
     if (precision == XRH_FP64) {
         cudaFuncSetAttribute(density_adjoint_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         density_adjoint_kernel<double><<<(unsigned)K, kAdjThreads, smem, (cudaStream_t)stream>>>(
-            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, gT_dev, gzbT_dev, gzkT_dev);
+            idx_ptr_dev, P_dev, Q_dev, sign_dev, reinterpret_cast<const double*>(zbT_dev), n_b,
+            reinterpret_cast<const double*>(zkT_dev), n_k, gT_dev, reinterpret_cast<double*>(gzbT_dev),
+            reinterpret_cast<double*>(gzkT_dev));
     } else if (precision == XRH_FP32) {
-        cudaFuncSetAttribute(density_adjoint_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        density_adjoint_kernel<float><<<(unsigned)K, kAdjThreads, smem, (cudaStream_t)stream>>>(
-            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, gT_dev, gzbT_dev, gzkT_dev);
+        const int nbp = (n_b + 3) & ~3, nkp = (n_k + 3) & ~3;
+        const size_t smem32 = sizeof(float) * (2 * (size_t)nbp * nkp + 2 * (size_t)kAdjChunk * (nbp + nkp));
+        if (smem32 > 200 * 1024) return XRH_ERR_CAPACITY;
+        cudaFuncSetAttribute(density_adjoint_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+        if ((reinterpret_cast<uintptr_t>(zbT_dev) & 15) || (reinterpret_cast<uintptr_t>(zkT_dev) & 15)) return XRH_ERR_ARG;
+        density_adjoint_f32_kernel<<<(unsigned)K, kAdjThreads, smem32, (cudaStream_t)stream>>>(
+            idx_ptr_dev, P_dev, Q_dev, sign_dev, reinterpret_cast<const float*>(zbT_dev), n_b,
+            reinterpret_cast<const float*>(zkT_dev), n_k, gT_dev, reinterpret_cast<float*>(gzbT_dev),
+            reinterpret_cast<float*>(gzkT_dev));
     } else {
         return XRH_ERR_UNSUPPORTED;
     }
@@ -163,17 +316,26 @@ extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_
     return XRH_OK;
 }
 
-extern "C" int xrh_ccaa_weighted(int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
+extern "C" int xrh_ccaa_weighted(int precision, int n_orbs, const uint64_t* bra_masks_dev, int n_bra_conf,
                                  const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev,
-                                 int n_ket_conf, const double* zbT_dev, const double* YT_dev, int n,
-                                 double* Gamma_dev, void* stream) {
+                                 int n_ket_conf, const int32_t* rank_table_dev, int64_t table_size,
+                                 const int64_t* binom_dev, const double* zbT_dev, const double* YT_dev, int n,
+                                 void* Gamma_dev, void* stream) {
     const int N = 2 * n_orbs;
     if (n_orbs < 1 || N > 64 || n < 1 || n > 256 || n_bra_conf < 0 || n_ket_conf < 0) return XRH_ERR_ARG;
     if (n_bra_conf == 0) return XRH_OK;
     if (!bra_masks_dev || !zbT_dev || !YT_dev || !Gamma_dev) return XRH_ERR_ARG;
-    ccaa_weighted_kernel<<<n_bra_conf, kWThreads, 0, (cudaStream_t)stream>>>(
-        N, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, zbT_dev, YT_dev, n,
-        Gamma_dev);
+    if (rank_table_dev && !binom_dev) return XRH_ERR_ARG;
+    if (precision == XRH_FP64)
+        ccaa_weighted_kernel<double><<<n_bra_conf, kWThreads, 0, (cudaStream_t)stream>>>(
+            N, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, rank_table_dev,
+            table_size, binom_dev, zbT_dev, YT_dev, n, reinterpret_cast<double*>(Gamma_dev));
+    else if (precision == XRH_FP32)
+        ccaa_weighted_kernel<float><<<n_bra_conf, kWThreads, 0, (cudaStream_t)stream>>>(
+            N, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, rank_table_dev,
+            table_size, binom_dev, zbT_dev, YT_dev, n, reinterpret_cast<float*>(Gamma_dev));
+    else
+        return XRH_ERR_UNSUPPORTED;
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -13,54 +13,82 @@
 namespace {
 
 constexpr int kAccThreads = 256;
-constexpr int kAccPerThread = 16;                 // outputs per thread per pass
-constexpr int kAccPass = kAccThreads * kAccPerThread;
+constexpr int kAccChunk = 64;
 
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
+// One CTA per operator index.  Each thread owns a 4 x 4 block of (I, J) outputs; the
+// couplings of the index are staged 64 at a time in shared memory (bra columns with the
+// sign folded in, ket columns), rows padded to a multiple of 4 so that one coupling costs
+// two 4-wide shared loads per 16 FMAs.  Partial sums of a chunk are in T, the running sum in
+// FP64 (the FP32 variant therefore rounds only within a chunk).
 template <typename T>
 __global__ void __launch_bounds__(kAccThreads) density_acc_kernel(
     const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const double* __restrict__ zbT, int nb, const double* __restrict__ zkT,
-    int nk, double* __restrict__ rhoT, int chunk) {
-    extern __shared__ unsigned char smem_raw[];
-    T* sb = reinterpret_cast<T*>(smem_raw);           // [chunk][nb]
-    T* sk = sb + (size_t)chunk * nb;                  // [chunk][nk]
+    int nk, double* __restrict__ rhoT) {
+    using V4 = typename Vec4<T>::type;
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
+    T* sb = reinterpret_cast<T*>(smem_raw);            // [chunk][nbp]
+    T* sk = sb + (size_t)kAccChunk * nbp;              // [chunk][nkp]
     const int64_t idx = blockIdx.x;
     const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
-    const int n_out = nb * nk;
-    double* out = rhoT + idx * (int64_t)n_out;
-    for (int pass0 = 0; pass0 < n_out; pass0 += kAccPass) {
-        double acc[kAccPerThread];
+    double* out = rhoT + idx * (int64_t)nb * nk;
+    const int tiles_j = nkp / 4, n_tiles = (nbp / 4) * tiles_j;
+    for (int t0 = 0; t0 < n_tiles; t0 += kAccThreads) {
+        const int t = t0 + threadIdx.x;
+        const bool active = t < n_tiles;
+        const int i0 = active ? (t / tiles_j) * 4 : 0, j0 = active ? (t % tiles_j) * 4 : 0;
+        double acc[4][4];
 #pragma unroll
-        for (int r = 0; r < kAccPerThread; ++r) acc[r] = 0.0;
-        for (int64_t c0 = c_begin; c0 < c_end; c0 += chunk) {
-            const int64_t rem_c = c_end - c0;
-            const int nc = rem_c < chunk ? (int)rem_c : chunk;
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+        for (int64_t c0 = c_begin; c0 < c_end; c0 += kAccChunk) {
+            const int64_t rem = c_end - c0;
+            const int nc = rem < kAccChunk ? (int)rem : kAccChunk;
             __syncthreads();
-            for (int t = threadIdx.x; t < nc * nb; t += blockDim.x) {
-                const int c = t / nb, i = t - c * nb;
+            for (int x = threadIdx.x; x < nc * nbp; x += blockDim.x) {
+                const int c = x / nbp, i = x - c * nbp;
                 const double s = sgn[c0 + c] < 0 ? -1.0 : 1.0;
-                sb[c * nb + i] = (T)(s * zbT[(int64_t)P[c0 + c] * nb + i]);
+                sb[x] = i < nb ? (T)(s * zbT[(int64_t)P[c0 + c] * nb + i]) : (T)0;
             }
-            for (int t = threadIdx.x; t < nc * nk; t += blockDim.x) {
-                const int c = t / nk, j = t - c * nk;
-                sk[c * nk + j] = (T)zkT[(int64_t)Q[c0 + c] * nk + j];
+            for (int x = threadIdx.x; x < nc * nkp; x += blockDim.x) {
+                const int c = x / nkp, j = x - c * nkp;
+                sk[x] = j < nk ? (T)zkT[(int64_t)Q[c0 + c] * nk + j] : (T)0;
             }
             __syncthreads();
+            if (active) {
+                T part[4][4];
 #pragma unroll
-            for (int r = 0; r < kAccPerThread; ++r) {
-                const int o = pass0 + threadIdx.x + r * kAccThreads;
-                if (o < n_out) {
-                    const int i = o / nk, j = o - i * nk;
-                    T a = 0;
-                    for (int c = 0; c < nc; ++c) a = fma(sb[c * nb + i], sk[c * nk + j], a);
-                    acc[r] += (double)a;     // FP32 variant: FP32 partial sums per chunk, FP64 total
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) part[a][b] = 0;
+                for (int c = 0; c < nc; ++c) {
+                    const V4 va = *reinterpret_cast<const V4*>(sb + c * nbp + i0);
+                    const V4 vb = *reinterpret_cast<const V4*>(sk + c * nkp + j0);
+                    const T av[4] = {va.x, va.y, va.z, va.w};
+                    const T bv[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) part[a][b] = fma(av[a], bv[b], part[a][b]);
                 }
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
             }
         }
+        if (active) {
 #pragma unroll
-        for (int r = 0; r < kAccPerThread; ++r) {
-            const int o = pass0 + threadIdx.x + r * kAccThreads;
-            if (o < n_out) out[o] = acc[r];
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    if (i0 + a < nb && j0 + b < nk) out[(int64_t)(i0 + a) * nk + j0 + b] = acc[a][b];
         }
     }
 }
@@ -87,6 +115,7 @@ template <typename T>
 __global__ void __launch_bounds__(kSigThreads) sigma2e_kernel(
     int N, const double* __restrict__ V, const uint64_t* __restrict__ bra, int n_bra,
     const uint64_t* __restrict__ ket_sorted, const int32_t* __restrict__ ket_pos, int n_ket,
+    const int32_t* __restrict__ rank_table, int64_t table_size, const int64_t* __restrict__ binom,
     const double* __restrict__ zkT, int nk, double* __restrict__ sigmaT) {
     // smem: entry list (Q position, coefficient) for one (p,q) pair: at most C(N,2) entries
     extern __shared__ unsigned char smem_raw[];
@@ -143,10 +172,16 @@ __global__ void __launch_bounds__(kSigThreads) sigma2e_kernel(
                 int s2 = s1;
                 xrh_apply(1, s, m2, s2);
                 xrh_apply(1, r, m2, s2);
-                const int hit = xrh_lookup(ket_sorted, n_ket, m2);
-                if (hit < 0) continue;
+                int qpos;
+                if (rank_table) {
+                    qpos = xrh_rank_lookup(rank_table, table_size, binom, m2);
+                } else {
+                    const int hit = xrh_lookup(ket_sorted, n_ket, m2);
+                    qpos = hit < 0 ? -1 : __ldg(ket_pos + hit);
+                }
+                if (qpos < 0) continue;
                 const int slot = atomicAdd(&s_count, 1);
-                eq[slot] = __ldg(ket_pos + hit);
+                eq[slot] = qpos;
                 ev[slot] = (s2 ? -4.0 : 4.0) * v;
             }
             __syncthreads();
@@ -177,16 +212,18 @@ extern "C" int xrh_density_accumulate(int precision, int64_t K, const int64_t* i
     if (K <= 0 || n_b <= 0 || n_k <= 0 || !idx_ptr_dev || !rhoT_dev || !zbT_dev || !zkT_dev) return XRH_ERR_ARG;
     if (K > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     const size_t esz = (precision == XRH_FP32) ? sizeof(float) : sizeof(double);
-    int chunk = (int)((40 * 1024) / (esz * (size_t)(n_b + n_k)));
-    if (chunk < 1) return XRH_ERR_CAPACITY;
-    if (chunk > 64) chunk = 64;
-    const size_t smem = esz * (size_t)chunk * (n_b + n_k);
+    const size_t smem = esz * (size_t)kAccChunk * (size_t)(((n_b + 3) & ~3) + ((n_k + 3) & ~3));
+    if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
     if (precision == XRH_FP64) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(density_acc_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         density_acc_kernel<double><<<(unsigned)K, kAccThreads, smem, (cudaStream_t)stream>>>(
-            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, rhoT_dev, chunk);
+            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, rhoT_dev);
     } else if (precision == XRH_FP32) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(density_acc_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         density_acc_kernel<float><<<(unsigned)K, kAccThreads, smem, (cudaStream_t)stream>>>(
-            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, rhoT_dev, chunk);
+            idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k, rhoT_dev);
     } else {
         return XRH_ERR_UNSUPPORTED;
     }
@@ -206,23 +243,26 @@ extern "C" int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, d
 
 extern "C" int xrh_sigma2e(int precision, int n_orbs, const double* V_dev, const uint64_t* bra_masks_dev,
                            int n_bra_conf, const uint64_t* ket_sorted_masks_dev, const int32_t* ket_sorted_pos_dev,
-                           int n_ket_conf, const double* zkT_dev, int n_k, double* sigmaT_dev, void* stream) {
+                           int n_ket_conf, const int32_t* rank_table_dev, int64_t table_size,
+                           const int64_t* binom_dev, const double* zkT_dev, int n_k, double* sigmaT_dev,
+                           void* stream) {
     const int N = 2 * n_orbs;
     if (n_orbs < 1 || N > 64 || n_k < 1 || n_k > kSigMaxNk || n_bra_conf < 0 || n_ket_conf < 0) return XRH_ERR_ARG;
     if (n_bra_conf == 0) return XRH_OK;
     if (!V_dev || !bra_masks_dev || !zkT_dev || !sigmaT_dev) return XRH_ERR_ARG;
+    if (rank_table_dev && !binom_dev) return XRH_ERR_ARG;
     // entry list capacity: C(64,2) = 2016 <= 2048
     const size_t smem = 2048 * (sizeof(int) + sizeof(double));
     if (precision == XRH_FP64) {
         cudaFuncSetAttribute(sigma2e_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         sigma2e_kernel<double><<<n_bra_conf, kSigThreads, smem, (cudaStream_t)stream>>>(
-            N, V_dev, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, zkT_dev, n_k,
-            sigmaT_dev);
+            N, V_dev, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, rank_table_dev,
+            table_size, binom_dev, zkT_dev, n_k, sigmaT_dev);
     } else if (precision == XRH_FP32) {
         cudaFuncSetAttribute(sigma2e_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         sigma2e_kernel<float><<<n_bra_conf, kSigThreads, smem, (cudaStream_t)stream>>>(
-            N, V_dev, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, zkT_dev, n_k,
-            sigmaT_dev);
+            N, V_dev, bra_masks_dev, n_bra_conf, ket_sorted_masks_dev, ket_sorted_pos_dev, n_ket_conf, rank_table_dev,
+            table_size, binom_dev, zkT_dev, n_k, sigmaT_dev);
     } else {
         return XRH_ERR_UNSUPPORTED;
     }
@@ -269,4 +309,154 @@ extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t
                                     scratch, stream);
     if (st != XRH_OK) return st;
     return xrh_transpose(scratch, K, (int64_t)n_b * n_k, rho_dev, stream);
+}
+
+// ---- FP32 density build with asynchronous gathers ----------------------------------------
+// Same product as density_acc_kernel<float>, for the split-precision paths.  The state
+// coefficients come pre-converted to FP32 with rows padded to a multiple of 4 (16-byte
+// aligned), so the z columns of a chunk of couplings are gathered with cp.async 16-byte
+// copies into a double-buffered shared-memory ring: the gathers of chunk k+1 are in flight
+// while chunk k is multiplied.  blockIdx.y splits the couplings of one operator index over
+// several CTAs (for the operator strings with few indices, e.g. K = N); with splits > 1
+// the partial sums are added atomically to rhoT, which the caller zeroes first.
+namespace {
+
+
+constexpr int kF32Chunk = 64;
+
+__global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
+    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+    const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
+    double* __restrict__ rhoT, int splits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
+    float* zb_s = reinterpret_cast<float*>(smem_raw);               // [2][chunk][nbp]
+    float* zk_s = zb_s + 2 * kF32Chunk * nbp;                        // [2][chunk][nkp]
+    __shared__ int sP[2][kF32Chunk], sQ[2][kF32Chunk];
+    __shared__ float sS[2][kF32Chunk];
+    const int64_t idx = blockIdx.x;
+    const int64_t cb0 = idx_ptr[idx], ce0 = idx_ptr[idx + 1];
+    const int64_t len = ce0 - cb0;
+    const int64_t per = (len + splits - 1) / splits;
+    const int64_t c_begin = cb0 + blockIdx.y * per;
+    const int64_t c_end = (c_begin + per < ce0) ? c_begin + per : ce0;
+    double* out = rhoT + idx * (int64_t)nb * nk;
+    const int tiles_j = nkp / 4, n_tiles = (nbp / 4) * tiles_j;
+    if (c_begin >= c_end) {
+        if (splits == 1)
+            for (int o = threadIdx.x; o < nb * nk; o += blockDim.x) out[o] = 0.0;
+        return;
+    }
+    const int n_chunks = (int)((c_end - c_begin + kF32Chunk - 1) / kF32Chunk);
+    const int gb = nbp / 4, gk = nkp / 4;       // 16-byte granules per row
+
+    auto load_idx = [&](int k, int buf) {
+        const int64_t c0 = c_begin + (int64_t)k * kF32Chunk;
+        for (int t = threadIdx.x; t < kF32Chunk; t += blockDim.x) {
+            const int64_t c = c0 + t;
+            const bool ok = c < c_end;
+            sP[buf][t] = ok ? P[c] : -1;
+            sQ[buf][t] = ok ? Q[c] : -1;
+            sS[buf][t] = ok ? (sgn[c] < 0 ? -1.f : 1.f) : 0.f;
+        }
+    };
+    auto stage = [&](int buf) {
+        float* zbb = zb_s + buf * kF32Chunk * nbp;
+        float* zkb = zk_s + buf * kF32Chunk * nkp;
+        for (int g = threadIdx.x; g < kF32Chunk * gb; g += blockDim.x) {
+            const int c = g / gb, part = g - c * gb;
+            const int p = sP[buf][c];
+            if (p >= 0) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)p * nbp + part * 4);
+            else *reinterpret_cast<float4*>(zbb + c * nbp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        for (int g = threadIdx.x; g < kF32Chunk * gk; g += blockDim.x) {
+            const int c = g / gk, part = g - c * gk;
+            const int q = sQ[buf][c];
+            if (q >= 0) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)q * nkp + part * 4);
+            else *reinterpret_cast<float4*>(zkb + c * nkp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        cp_async_commit();
+    };
+
+    for (int t0 = 0; t0 < n_tiles; t0 += kAccThreads) {
+        const int t = t0 + threadIdx.x;
+        const bool active = t < n_tiles;
+        const int i0 = active ? (t / tiles_j) * 4 : 0, j0 = active ? (t % tiles_j) * 4 : 0;
+        double acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+        __syncthreads();
+        load_idx(0, 0);
+        __syncthreads();
+        stage(0);
+        for (int k = 0; k < n_chunks; ++k) {
+            const int buf = k & 1;
+            __syncthreads();                         // chunk k-1 (buffer buf ^ 1) fully consumed
+            if (k + 1 < n_chunks) load_idx(k + 1, buf ^ 1);
+            __syncthreads();                         // indices of k+1 visible
+            if (k + 1 < n_chunks) {
+                stage(buf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();                         // gathers of chunk k visible to every thread
+            if (active) {
+                const float* zbb = zb_s + buf * kF32Chunk * nbp;
+                const float* zkb = zk_s + buf * kF32Chunk * nkp;
+                float part[4][4] = {};
+#pragma unroll 4
+                for (int c = 0; c < kF32Chunk; ++c) {
+                    const float s = sS[buf][c];
+                    const float4 va = *reinterpret_cast<const float4*>(zbb + c * nbp + i0);
+                    const float4 vb = *reinterpret_cast<const float4*>(zkb + c * nkp + j0);
+                    const float av[4] = {s * va.x, s * va.y, s * va.z, s * va.w};
+                    const float bv[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) part[a][b] = fmaf(av[a], bv[b], part[a][b]);
+                }
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    if (i0 + a >= nb || j0 + b >= nk) continue;
+                    double* o = out + (int64_t)(i0 + a) * nk + j0 + b;
+                    if (splits == 1) *o = acc[a][b];
+                    else atomicAdd(o, acc[a][b]);
+                }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* idx_ptr_dev, const int32_t* P_dev,
+                                          const int32_t* Q_dev, const int8_t* sign_dev, const float* zb32_dev, int n_b,
+                                          const float* zk32_dev, int n_k, double* rhoT_dev, void* stream) {
+    if (K <= 0 || n_b <= 0 || n_k <= 0 || splits < 1 || splits > 65535 || !idx_ptr_dev || !zb32_dev || !zk32_dev ||
+        !rhoT_dev)
+        return XRH_ERR_ARG;
+    if (K > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    if ((reinterpret_cast<uintptr_t>(zb32_dev) & 15) || (reinterpret_cast<uintptr_t>(zk32_dev) & 15)) return XRH_ERR_ARG;
+    const size_t smem = sizeof(float) * 2 * (size_t)kF32Chunk * (size_t)(((n_b + 3) & ~3) + ((n_k + 3) & ~3));
+    if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(density_acc_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((unsigned)K, (unsigned)splits);
+    density_acc_f32_kernel<<<grid, kAccThreads, smem, (cudaStream_t)stream>>>(idx_ptr_dev, P_dev, Q_dev, sign_dev,
+                                                                             zb32_dev, n_b, zk32_dev, n_k, rhoT_dev,
+                                                                             splits);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
 }

@@ -25,16 +25,20 @@ __device__ __forceinline__ int find_task(const xrh_gemm_task* __restrict__ tasks
     return lo;
 }
 
+// T = double: the plain FP64 path.  T = float: operands rounded to FP32 in shared memory,
+// products and the partial sum of each 16-wide K step in FP32, running sums in FP64 (used
+// for the adjoint on the split-precision paths).
+template <typename T_>
 __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __restrict__ tasks, int n_tasks,
                                                       const xrh_gemm_segment* __restrict__ segs) {
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
+    __shared__ T_ As[BK][BM + 1];
+    __shared__ T_ Bs[BK][BN + 1];
     const int64_t tile = blockIdx.x;
     const int t_id = find_task(tasks, n_tasks, tile);
-    const xrh_gemm_task& T = tasks[t_id];
-    const int64_t tiles_m = (T.M + BM - 1) / BM, tiles_n = (T.N + BN - 1) / BN;
-    int64_t local = tile - T.tile_begin;
-    const int64_t per_batch = tiles_m * tiles_n * T.splitk;
+    const xrh_gemm_task& Tk = tasks[t_id];
+    const int64_t tiles_m = (Tk.M + BM - 1) / BM, tiles_n = (Tk.N + BN - 1) / BN;
+    int64_t local = tile - Tk.tile_begin;
+    const int64_t per_batch = tiles_m * tiles_n * Tk.splitk;
     const int64_t bidx = local / per_batch;
     local -= bidx * per_batch;
     const int64_t split = local / (tiles_m * tiles_n);
@@ -47,22 +51,17 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-    for (int64_t s = T.seg_begin; s < T.seg_begin + T.seg_count; ++s) {
+    for (int64_t s = Tk.seg_begin; s < Tk.seg_begin + Tk.seg_count; ++s) {
         const xrh_gemm_segment S = segs[s];
         const double* __restrict__ Ap = S.A + bidx * S.sA;
         const double* __restrict__ Bp = S.B + bidx * S.sB;
         const bool at = (S.flags & 1) != 0, bt = (S.flags & 2) != 0;
         int64_t kb = 0, ke = S.K;
-        if (T.splitk > 1) {
-            const int64_t per = (S.K + T.splitk - 1) / T.splitk;
+        if (Tk.splitk > 1) {
+            const int64_t per = (S.K + Tk.splitk - 1) / Tk.splitk;
             kb = split * per;
             ke = (kb + per < S.K) ? kb + per : S.K;
         }
-        double sacc[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) sacc[i][j] = 0.0;
         for (int64_t k0 = kb; k0 < ke; k0 += BK) {
             __syncthreads();
 #pragma unroll
@@ -74,18 +73,23 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
                 {
                     const int rr = at ? r2 : r, cc = at ? c2 : c;
                     const int64_t gm = m0 + rr, gk = k0 + cc;
-                    As[cc][rr] = (gm < T.M && gk < ke) ? (at ? Ap[gk * S.lda + gm] : Ap[gm * S.lda + gk]) : 0.0;
+                    As[cc][rr] = (T_)((gm < Tk.M && gk < ke) ? S.alpha * (at ? Ap[gk * S.lda + gm] : Ap[gm * S.lda + gk]) : 0.0);
                 }
                 {
                     const int rr = bt ? r2 : r, cc = bt ? c2 : c;
                     const int64_t gn = n0 + rr, gk = k0 + cc;
-                    Bs[cc][rr] = (gn < T.N && gk < ke) ? (bt ? Bp[gk * S.ldb + gn] : Bp[gn * S.ldb + gk]) : 0.0;
+                    Bs[cc][rr] = (T_)((gn < Tk.N && gk < ke) ? (bt ? Bp[gk * S.ldb + gn] : Bp[gn * S.ldb + gk]) : 0.0);
                 }
             }
             __syncthreads();
+            T_ part[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) part[i][j] = (T_)0;
 #pragma unroll
             for (int kk = 0; kk < BK; ++kk) {
-                double a[4], b[4];
+                T_ a[4], b[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -93,33 +97,33 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) sacc[i][j] = fma(a[i], b[j], sacc[i][j]);
+                    for (int j = 0; j < 4; ++j) part[i][j] = fma(a[i], b[j], part[i][j]);
             }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] += (double)part[i][j];
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = fma(S.alpha, sacc[i][j], acc[i][j]);
     }
 
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int64_t m = m0 + ty + 16 * i;
-        if (m >= T.M) continue;
+        if (m >= Tk.M) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int64_t n = n0 + tx + 16 * j;
-            if (n >= T.N) continue;
+            if (n >= Tk.N) continue;
             double v = acc[i][j];
-            double* Cb = T.C + bidx * T.sC;
-            if (T.mode == 0) {
-                Cb[m * T.ldc + n] = v;
-            } else if (T.mode == 1) {
-                atomicAdd(Cb + m * T.ldc + n, v);
+            double* Cb = Tk.C + bidx * Tk.sC;
+            if (Tk.mode == 0) {
+                Cb[m * Tk.ldc + n] = v;
+            } else if (Tk.mode == 1) {
+                atomicAdd(Cb + m * Tk.ldc + n, v);
             } else {
-                if (T.DA && T.diagB[n]) v += T.DA[m];
-                if (T.DB && T.diagA[m]) v += T.DB[n];
-                Cb[((int64_t)T.rowA[m] + T.rowB[n]) * T.ldc + T.colA[m] + T.colB[n]] = v;
+                if (Tk.DA && Tk.diagB[n]) v += Tk.DA[m];
+                if (Tk.DB && Tk.diagA[m]) v += Tk.DB[n];
+                Cb[((int64_t)Tk.rowA[m] + Tk.rowB[n]) * Tk.ldc + Tk.colA[m] + Tk.colB[n]] = v;
             }
         }
     }
@@ -127,13 +131,23 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 
 }  // namespace
 
-extern "C" int xrh_gemm_fp64_grouped(const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
+extern "C" int xrh_gemm_simt_grouped(int precision, const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
                                      const xrh_gemm_segment* segs_dev, void* stream) {
     if (n_tasks < 0 || total_tiles < 0) return XRH_ERR_ARG;
     if (n_tasks == 0 || total_tiles == 0) return XRH_OK;
     if (!tasks_dev || !segs_dev) return XRH_ERR_ARG;
     if (total_tiles > 0x7fffffffLL) return XRH_ERR_CAPACITY;
-    gemm_fp64_kernel<<<(unsigned)total_tiles, NT, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, segs_dev);
+    if (precision == XRH_FP64)
+        gemm_fp64_kernel<double><<<(unsigned)total_tiles, NT, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, segs_dev);
+    else if (precision == XRH_FP32)
+        gemm_fp64_kernel<float><<<(unsigned)total_tiles, NT, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, segs_dev);
+    else
+        return XRH_ERR_UNSUPPORTED;
     XRH_CHECK_LAUNCH();
     return XRH_OK;
+}
+
+extern "C" int xrh_gemm_fp64_grouped(const xrh_gemm_task* tasks_dev, int n_tasks, int64_t total_tiles,
+                                     const xrh_gemm_segment* segs_dev, void* stream) {
+    return xrh_gemm_simt_grouped(XRH_FP64, tasks_dev, n_tasks, total_tiles, segs_dev, stream);
 }

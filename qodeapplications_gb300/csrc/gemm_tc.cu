@@ -27,7 +27,7 @@ namespace {
 
 constexpr int TC_BM = 128;
 constexpr int TC_STAGES = 3;
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;   // 8 warps: two per TMEM lane quarter in the epilogue
 // K chunks rotate over TC_NACC accumulators of 128 columns each (all 512 TMEM columns), and
 // the epilogue adds the partial tiles in FP64: each FP32 tensor-core accumulator then sums
 // a quarter of the terms, which bounds the accumulation error of long contractions.
@@ -146,6 +146,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_base_sh;
     __shared__ volatile int abort_sh;
+    __shared__ int s_rowB[128], s_colB[128];
+    __shared__ double s_DB[128];
+    __shared__ unsigned char s_diagB[128];
     constexpr int KCH = (KIND == 0) ? 64 : 32;          // elements of K per 128-byte chunk
     constexpr uint32_t FMT = (KIND == 0) ? 1u : 2u;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -253,7 +256,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
         if (nk > 0) {
-            // all threads: accumulator complete -> FP64 epilogue
+            // all threads: per-column scatter metadata of this tile into shared memory
+            if (T.mode == 2) {
+                for (int j = tid; j < BN; j += TC_THREADS) {
+                    const int n = n0 + j;
+                    const bool ok = n < T.N;
+                    s_rowB[j] = ok ? T.rowB[n] : 0;
+                    s_colB[j] = ok ? T.colB[n] : 0;
+                    s_diagB[j] = ok ? T.diagB[n] : 0;
+                    s_DB[j] = (ok && T.DB) ? T.DB[n] : 0.0;
+                }
+            }
+            // accumulator complete -> FP64 epilogue
             const bool done = mbar_wait(smem_u32(&done_bar), done_iter & 1u, nullptr);
             ++done_iter;
             if (!done) {
@@ -261,37 +275,57 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 atomicExch(status, XRH_ERR_TIMEOUT);
             }
             tc_fence_after();
-            __syncwarp();
+            __syncthreads();
             if (done) {
-                const int m = m0 + warp * 32 + lane;
+                const int quarter = warp & 3, half = warp >> 2;      // TMEM lanes 32*quarter.., column half
+                const int m = m0 + quarter * 32 + lane;
                 const bool row_ok = m < T.M;
+                int64_t rbase = 0, cbase = 0;
+                bool dA = false;
+                double DAm = 0.0;
+                if (row_ok) {
+                    if (T.mode == 2) {
+                        rbase = T.rowA[m];
+                        cbase = T.colA[m];
+                        dA = T.diagA[m] != 0;
+                        DAm = T.DA ? T.DA[m] : 0.0;
+                    } else {
+                        rbase = (int64_t)m * T.ldc;
+                    }
+                }
                 double* C = T.C;
                 const int n_acc = nk < TC_NACC ? nk : TC_NACC;
-                for (int cc = 0; cc < BN; cc += 32) {
+                // 32-column chunks of the tile alternate between the two warps of a lane quarter
+                for (int cc = half * 32; cc < BN; cc += 64) {
                     double sum[32];
 #pragma unroll
                     for (int j = 0; j < 32; ++j) sum[j] = 0.0;
                     for (int a = 0; a < n_acc; ++a) {
                         float v[32];
-                        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128 + cc), v);
+                        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128 + cc), v);
 #pragma unroll
                         for (int j = 0; j < 32; ++j) sum[j] += (double)v[j];
                     }
                     if (!row_ok) continue;
-#pragma unroll 4
-                    for (int j = 0; j < 32; ++j) {
-                        const int n = n0 + cc + j;
-                        if (n >= T.N) break;
-                        double x = sum[j];
-                        if (T.mode == 0) {
-                            C[(int64_t)m * T.ldc + n] = x;
-                        } else if (T.mode == 1) {
-                            atomicAdd(C + (int64_t)m * T.ldc + n, x);
-                        } else {
-                            if (T.DA && T.diagB[n]) x += T.DA[m];
-                            if (T.DB && T.diagA[m]) x += T.DB[n];
-                            C[((int64_t)T.rowA[m] + T.rowB[n]) * T.ldc + T.colA[m] + T.colB[n]] = x;
+                    if (T.mode == 2) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int jj = cc + j;
+                            if (n0 + jj < T.N) {
+                                double x = sum[j];
+                                if (s_diagB[jj]) x += DAm;
+                                if (dA) x += s_DB[jj];
+                                C[(rbase + s_rowB[jj]) * T.ldc + cbase + s_colB[jj]] = x;
+                            }
                         }
+                    } else if (T.mode == 0) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (n0 + cc + j < T.N) C[rbase + n0 + cc + j] = sum[j];
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (n0 + cc + j < T.N) atomicAdd(C + rbase + n0 + cc + j, sum[j]);
                     }
                 }
             }

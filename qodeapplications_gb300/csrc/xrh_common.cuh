@@ -44,3 +44,31 @@ __device__ __forceinline__ int xrh_lookup(const uint64_t* __restrict__ sorted, i
     }
     return -1;
 }
+
+// Position of a determinant through its colexicographic rank: rank = sum_i C(o_i, i+1) over
+// the occupied orbitals o_0 < o_1 < ... (binom[n*17 + k] = C(n, k), n <= 64, k <= 16), then
+// pos_table[rank] (-1 where the determinant is not in the list).  n_e fast steps and one
+// table load instead of a binary search over the sorted list.
+__device__ __forceinline__ int xrh_rank_lookup(const int32_t* __restrict__ pos_table, int64_t table_size,
+                                               const int64_t* __restrict__ binom, uint64_t mask) {
+    int64_t r = 0;
+    int i = 1;
+    while (mask) {
+        const int o = __ffsll((long long)mask) - 1;
+        if (i > 16) return -1;
+        r += __ldg(binom + o * 17 + i);
+        mask &= mask - 1;
+        ++i;
+    }
+    return (r < table_size) ? __ldg(pos_table + r) : -1;
+}
+
+// 16-byte asynchronous global -> shared copies (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem_dst)),
+                 "l"(gmem_src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }

@@ -11,6 +11,8 @@ the integer coupling lists <P|op_idx|Q> = +-1 are built once on the device
 is then only the floating-point gather-accumulate rho[I,J,idx] = sum s z_I[P] z_J[Q]
 plus a transpose into the reference's (n_bra, n_ket, N, ..., N) layout.
 """
+import math
+
 import numpy as np
 import torch
 
@@ -40,6 +42,26 @@ def _sort_masks(masks_np):
     return masks_np[order], order.astype(np.int32)
 
 
+_BINOM = np.zeros((65, 17), dtype=np.int64)
+for _n in range(65):
+    for _k in range(17):
+        _BINOM[_n, _k] = math.comb(_n, _k)
+RANK_TABLE_LIMIT = 1 << 26        # positions stored (int32) per charge sector at most
+
+
+def colex_rank(masks_np, N):
+    """sum_i C(o_i, i+1) over the occupied orbitals o_0 < o_1 < ... (a bijection between the
+    n_e-electron determinants over N spin orbitals and [0, C(N, n_e)))."""
+    m = np.asarray(masks_np, dtype=np.uint64)
+    rank = np.zeros(len(m), dtype=np.int64)
+    cnt = np.zeros(len(m), dtype=np.int64)
+    for o in range(N):
+        bit = ((m >> np.uint64(o)) & np.uint64(1)).astype(np.int64)
+        rank += bit * _BINOM[o, np.minimum(cnt + 1, 16)]
+        cnt += bit
+    return rank
+
+
 class FragmentSpace:
     """Determinant lists of one fragment (per charge) and their coupling lists on the GPU.
 
@@ -57,11 +79,22 @@ class FragmentSpace:
         self.masks = {}
         self.sorted_masks = {}
         self.sorted_pos = {}
+        self.rank_table, self.table_size = {}, {}
+        self.binom = torch.from_numpy(_BINOM.reshape(-1).copy()).to(self.device)
         for c, m in self.masks_np.items():
             sm, order = _sort_masks(m)
             self.masks[c] = torch.from_numpy(m.view(np.int64).copy()).to(self.device)
             self.sorted_masks[c] = torch.from_numpy(sm.view(np.int64).copy()).to(self.device)
             self.sorted_pos[c] = torch.from_numpy(order).to(self.device)
+            ne = bin(int(m[0])).count("1") if len(m) else 0
+            size = math.comb(self.N, ne) if ne <= 16 else RANK_TABLE_LIMIT + 1
+            if len(m) and size <= RANK_TABLE_LIMIT:
+                table = np.full(size, -1, dtype=np.int32)
+                table[colex_rank(m, self.N)] = np.arange(len(m), dtype=np.int32)
+                self.rank_table[c] = torch.from_numpy(table).to(self.device)
+                self.table_size[c] = size
+            else:
+                self.rank_table[c], self.table_size[c] = None, 0
         self.couplings = {}
         for bc in self.charges:
             for kc in self.charges:
@@ -125,6 +158,22 @@ class DensityBuilder:
                    for c in space.charges}
         self.zbT = {c: torch.empty((space.n_conf[c], self.n_states_bra[c]), dtype=torch.float64, device=dev)
                     for c in space.charges}
+        # FP32 path: coefficients converted once per build, rows padded to 16 bytes
+        self.f32 = self.precision == _lib.FP32
+        if self.f32:
+            pad = lambda n: (n + 3) // 4 * 4
+            self.zT32 = {c: torch.zeros((space.n_conf[c], pad(self.n_states[c])), dtype=torch.float32, device=dev)
+                         for c in space.charges}
+            self.zbT32 = {c: torch.zeros((space.n_conf[c], pad(self.n_states_bra[c])), dtype=torch.float32, device=dev)
+                          for c in space.charges}
+            # operator strings with few indices (K < 1024, e.g. K = N for a/c) spread the couplings
+            # of every index over several CTAs, about 256 couplings each
+            self.splits = {}
+            for key, cp in space.couplings.items():
+                if cp.K >= 1024:
+                    self.splits[key] = 1
+                else:
+                    self.splits[key] = int(min(64, max(1, round(cp.count / max(cp.K, 1) / 256))))
 
     def build(self, coeffs, bra_coeffs=None):
         """coeffs: {charge: CUDA float64 tensor (n_states, n_conf)}."""
@@ -132,11 +181,22 @@ class DensityBuilder:
         for c in self.space.charges:
             self.zT[c].copy_(coeffs[c].t())
             self.zbT[c].copy_((coeffs if bra_coeffs is None else bra_coeffs)[c].t())
+        if self.f32:
+            for c in self.space.charges:
+                self.zT32[c][:, :self.n_states[c]].copy_(self.zT[c])
+                self.zbT32[c][:, :self.n_states_bra[c]].copy_(self.zbT[c])
         for (op, bc, kc), cp in self.space.couplings.items():
             nb, nk = self.n_states_bra[bc], self.n_states[kc]
             tmp = self._tmp[(op, bc, kc)]
-            call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
-                 ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
+            if self.f32:
+                sp_ = self.splits[(op, bc, kc)]
+                if sp_ > 1:
+                    tmp.zero_()
+                call("xrh_density_accumulate_f32", cp.K, sp_, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
+                     ptr(self.zbT32[bc]), nb, ptr(self.zT32[kc]), nk, ptr(tmp), s)
+            else:
+                call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
+                     ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
             call("xrh_transpose", ptr(tmp), cp.K, nb * nk, ptr(self.rho[op][(bc, kc)]), s)
         return self.rho
 

@@ -16,8 +16,9 @@ FP64_TILE = 64
 
 
 class GroupedGemm:
-    def __init__(self, device="cuda"):
+    def __init__(self, device="cuda", precision="fp64"):
         self.device = torch.device(device)
+        self.precision = _lib.PRECISIONS[precision]
         self._tasks = []
         self._segs = []
         self._keep = []          # tensors whose addresses are in the tables
@@ -81,7 +82,7 @@ class GroupedGemm:
     def run(self, stream=None):
         if self.n_tasks == 0:
             return
-        call("xrh_gemm_fp64_grouped", _lib.ptr(self.tasks_dev), self.n_tasks, self.total_tiles,
+        call("xrh_gemm_simt_grouped", self.precision, _lib.ptr(self.tasks_dev), self.n_tasks, self.total_tiles,
              _lib.ptr(self.segs_dev), stream_ptr(stream))
 
 

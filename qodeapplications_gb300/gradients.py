@@ -82,8 +82,10 @@ class XRDimerAdjoint:
         grad_of = {p_: G[("g", p_)] for p_ in operands}
         self.grad_of = grad_of
 
+        # the adjoint contractions run in FP32 (FP64 sums) on the split-precision paths
+        gprec = "fp32" if plan.dens_precision == "fp32" else "fp64"
         # ---- launch 1: G blocks, Y and Z per final segment ----
-        L1 = GroupedGemm(dev)
+        L1 = GroupedGemm(dev, gprec)
         for m in (0, 1):
             for c in plan.H1blk[m]:
                 n = ns[m][c]
@@ -110,7 +112,7 @@ class XRDimerAdjoint:
         self.L1 = L1.finalize()
 
         # ---- launch 2: dA, dB (batched), monomer pieces ----
-        L2 = GroupedGemm(dev)
+        L2 = GroupedGemm(dev, gprec)
         for (A, B, K, Y, Z, Dj, (ni0, nj0, ni1, nj1)) in self.final_adj:
             gA, gB = grad_of[A.data_ptr()], grad_of[B.data_ptr()]
             # dA[(i0,j0),x] += sum_j1 D[j0,j1] Y[i0,(j1,x)]          (batch over i0)
@@ -139,7 +141,7 @@ class XRDimerAdjoint:
         self.L2 = L2.finalize()
 
         # ---- launch 3: precontraction adjoint ----
-        L3 = GroupedGemm(dev)
+        L3 = GroupedGemm(dev, gprec)
         for out, segs in plan.pre_specs:
             gP = grad_of[out.data_ptr()]
             M, X = out.shape
@@ -155,6 +157,13 @@ class XRDimerAdjoint:
         self.L3 = L3.finalize()
 
         # ---- launch 4 inputs: transposed density gradients for the coupling-list adjoint ----
+        # (FP32 accumulation buffers on the split-precision paths)
+        self.prec32 = plan.dens_precision == "fp32"
+        self.gz32, self.Gamma32 = None, None
+        if self.prec32:
+            self.gz32 = [{c: torch.zeros((plan.spaces[m].n_conf[c], ns[m][c]), dtype=torch.float32, device=dev)
+                          for c in plan.charges[m]} for m in (0, 1)]
+            self.Gamma32 = [torch.zeros(N[m] ** 4, dtype=torch.float32, device=dev) for m in (0, 1)]
         self.dens_adj = []
         for m in (0, 1):
             b = plan.builders[m]
@@ -173,26 +182,39 @@ class XRDimerAdjoint:
         if d is not None:
             self.d.copy_(d)
         self.arena.buf.zero_()
+        if self.prec32:
+            for m in (0, 1):
+                for t in self.gz32[m].values():
+                    t.zero_()
+                self.Gamma32[m].zero_()
         self.L1.run()
         self.L2.run()
         self.L3.run()
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
-            call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
-                 ptr(plan.builders[m].zbT[bc]), nb, ptr(plan.builders[m].zT[kc]), nk, ptr(gT),
-                 ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
+            gb_, gk_ = ((self.gz32[m][bc], self.gz32[m][kc]) if self.prec32 else
+                        (self.G[("gzT", m, bc)], self.G[("gzT", m, kc)]))
+            bld = plan.builders[m]
+            zb_, zk_ = ((bld.zbT32[bc], bld.zT32[kc]) if self.prec32 else (bld.zbT[bc], bld.zT[kc]))
+            call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
+                 ptr(cp.Q), ptr(cp.sign), ptr(zb_), nb, ptr(zk_), nk, ptr(gT), ptr(gb_), ptr(gk_), s)
         for m in (0, 1):
             sp = plan.spaces[m]
             for c in plan.H1blk[m]:
-                call("xrh_ccaa_weighted", sp.n_orbs, ptr(sp.masks[c]), sp.n_conf[c], ptr(sp.sorted_masks[c]),
-                     ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]),
-                     plan.n_states[m][c], ptr(self.G[("Gamma", m)]), s)
+                call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
+                     sp.n_conf[c], ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c],
+                     ptr(sp.rank_table[c]), sp.table_size[c], ptr(sp.binom),
+                     ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]), plan.n_states[m][c],
+                     ptr(self.Gamma32[m] if self.prec32 else self.G[("Gamma", m)]), s)
 
     # ---------------------------------------------------------------------- results ---
     def state_gradient(self):
         """dE/dz[m][charge] (n_states x n_conf), the unconstrained derivative of the lowest
         eigenvalue w.r.t. the CI coefficients (bra and ket occurrences)."""
+        if self.prec32:
+            return [{c: self.G[("gzT", m, c)].t() + self.gz32[m][c].t().to(torch.float64)
+                     for c in self.plan.charges[m]} for m in (0, 1)]
         return [{c: self.G[("gzT", m, c)].t() for c in self.plan.charges[m]} for m in (0, 1)]
 
     def integral_gradients(self):
@@ -221,7 +243,7 @@ class XRDimerAdjoint:
             dT[sl[m], sl[m]] += g1
             dU[m][sl[m], sl[m]] += g1
             dU[o][sl[m], sl[m]] += g1
-            Gm = G[("Gamma", m)].view(Ns[m], Ns[m], Ns[m], Ns[m])
+            Gm = (self.Gamma32[m].to(torch.float64) if self.prec32 else G[("Gamma", m)]).view(Ns[m], Ns[m], Ns[m], Ns[m])
             Gf = Gm - Gm.permute(1, 0, 2, 3) - Gm.permute(0, 1, 3, 2) + Gm.permute(1, 0, 3, 2)
             dV[sl[m], sl[m], sl[m], sl[m]] += Gf
         return dT, dU, dV

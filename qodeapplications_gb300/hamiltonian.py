@@ -90,8 +90,8 @@ class SigmaTwoElectron:
         sp = self.space
         c = self.c
         call("xrh_sigma2e", self.precision, sp.n_orbs, ptr(self.V), ptr(sp.masks[c]), sp.n_conf[c],
-             ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(zT), self.n, ptr(self.sigmaT),
-             stream_ptr())
+             ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(sp.rank_table[c]),
+             sp.table_size[c], ptr(sp.binom), ptr(zT), self.n, ptr(self.sigmaT), stream_ptr())
 
 
 def monomer_two_electron(space, coeffs, V_block, c):
@@ -276,7 +276,7 @@ class XRDimerPlan:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))
                     mono.append((n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n,
-                                 _splitk(nconf, target=256, cap=64)))
+                                 _splitk(nconf, target=128, cap=512)))
                 for tgt in targets_du:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))

@@ -110,3 +110,30 @@ def test_orbital_gradient_matches_finite_differences():
             vals.append(O.xr_energy(h2, V2, sysd["Ns"], 4, 0, 4, sysd["states"], CHG)[0])
         fd = (vals[0] - vals[1]) / (2 * eps)
         assert abs(fd - pred) <= 1e-6 * max(1.0, abs(fd)), (trial, fd, pred)
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_split_precision_gradients_close_to_fp64(prec):
+    """The split-precision adjoint (FP32 density adjoint, tensor-core build) against the FP64
+    adjoint: relative error of the tangent state gradient and of dE/dkappa below 1e-5."""
+    from qodeapplications_gb300.densities import FragmentSpace
+    from qodeapplications_gb300.gradients import XRDimerAdjoint, tangent_project
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+    sysd = S.make_system(n_frag=2, n_orb=4, n_states=3, charges=CHG, seed=31)
+    spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in CHG}, 4, 0, 4) for m in range(2)]
+    ns = [{c: 3 for c in CHG}] * 2
+    coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in CHG} for m in range(2)]
+    out = {}
+    for p in ("fp64", prec):
+        plan = XRDimerPlan(spaces, ns, [list(CHG)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
+                           precision=p)
+        adj = XRDimerAdjoint(plan)
+        E, d, _ = _gpu_energy_and_grad(plan, adj, coeffs)
+        g = adj.state_gradient()
+        gt = torch.cat([tangent_project(g[m][c], coeffs[m][c]).reshape(-1) for m in range(2) for c in CHG])
+        T = torch.as_tensor(sysd["h"], device="cuda")
+        kg = adj.orbital_gradient(T, torch.zeros((2,) + T.shape, dtype=torch.float64, device="cuda"),
+                                  torch.as_tensor(sysd["V"], device="cuda"), S.spin_orbital_spatial_index([4, 4]))
+        out[p] = (gt, kg)
+    for a, b in zip(out[prec], out["fp64"]):
+        assert float((a - b).norm() / b.norm()) < 1e-5
