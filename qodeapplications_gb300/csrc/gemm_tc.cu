@@ -4,19 +4,30 @@
 // one task whose K-concatenated segments are the density x integral contractions that land
 // in it.  Each FP64 operand X is split once per build into hi = round(X) and
 // lo = round(X - hi) in BF16 (XRH_BF16X3) or TF32 (XRH_TF32X3); a segment contributes
-//     A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T
-// accumulated in FP32 in tensor memory (TMEM).  The epilogue converts to FP64, applies the
-// segment-independent delta terms and scatters to H exactly like the FP64 path.
+//     A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T.
 //
-// Per CTA (persistent over 128 x BN output tiles, one CTA per SM):
-//   * one elected thread issues TMA loads (cp.async.bulk.tensor, 128B swizzle) of the four
-//     operand tiles of a K chunk into a 3-stage shared-memory ring, and the tcgen05.mma
-//     instructions that consume them (12 MMAs per chunk: 3 products x 4 K-steps);
-//     tcgen05.commit releases a stage when its MMAs are done;
-//   * the 4 warps read the 128 x BN FP32 accumulator with tcgen05.ld (warp w owns TMEM lanes
-//     32w..32w+31 = rows of the tile) and write FP64 results.
-// Every mbarrier wait is bounded; on timeout the kernel records XRH_ERR_TIMEOUT in
-// *status, drains what it issued (again bounded), frees its TMEM and returns.
+// Accuracy: the tensor core's FP32 accumulation is not round-to-nearest, and its error grows
+// with the number of MMA steps summed into one accumulator.  So no accumulator outlives a K
+// chunk (128 bytes of K: 64 BF16 / 32 TF32 elements): every chunk writes a fresh main slot
+// (hi*hi, 4 MMA steps) and a fresh correction slot (hi*lo + lo*hi, 8 steps, 2^-8 smaller),
+// and the epilogue warps drain both into FP32 registers with ordinary round-to-nearest adds
+// while the tensor core works on the next chunk.  The tile is converted to FP64 once, where
+// the segment-independent delta terms are added and the result is scattered like the FP64
+// path.
+//
+// Per CTA (persistent over 128 x BN output tiles, one CTA per SM), 9 warps:
+//   * warp 8, one thread: TMA loads (cp.async.bulk.tensor, 128B swizzle) of the four operand
+//     tiles of a chunk into a 3-stage shared-memory ring, prefetched across tile boundaries,
+//     and the 12 tcgen05.mma of each chunk into one of two TMEM chunk buffers (main +
+//     correction slot, 128 columns each: 512 columns); tcgen05.commit releases the ring stage
+//     (empty) and hands the buffer to the epilogue (ready);
+//   * warps 0-7: per chunk, tcgen05.ld of both slots (warp w reads TMEM lanes 32(w%4).. =
+//     rows, 32-column groups alternate between w<4 and w>=4), add into registers, release the
+//     buffer (drained); at the end of the tile, the FP64 epilogue.
+// Every mbarrier wait is bounded; on timeout the kernel records XRH_ERR_TIMEOUT in *status,
+// every warp leaves its loop (the epilogue warps decide together through bar.red.or), the
+// producer waits (bounded) for its copies and MMAs in flight, TMEM is freed and the kernel
+// returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -27,13 +38,11 @@ namespace {
 
 constexpr int TC_BM = 128;
 constexpr int TC_STAGES = 3;
-constexpr int TC_THREADS = 256;   // 8 warps: two per TMEM lane quarter in the epilogue
-// K chunks rotate over TC_NACC accumulators of 128 columns each (all 512 TMEM columns), and
-// the epilogue adds the partial tiles in FP64: each FP32 tensor-core accumulator then sums
-// a quarter of the terms, which bounds the accumulation error of long contractions.
-constexpr int TC_NACC = 4;
-constexpr uint32_t TC_TMEM_COLS = 128 * TC_NACC;
-constexpr uint32_t TC_A_BYTES = TC_BM * 128;           // 128 rows x 128 B (one swizzle width of K)
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_EPI_THREADS = TC_EPI_WARPS * 32;
+constexpr int TC_THREADS = TC_EPI_THREADS + 32;    // + the producer / MMA warp
+constexpr uint32_t TC_TMEM_COLS = 512;             // 2 chunk buffers x (main, correction) x 128
+constexpr uint32_t TC_A_BYTES = TC_BM * 128;       // 128 rows x 128 B (one swizzle width of K)
 constexpr uint32_t TC_B_MAX_BYTES = 128 * 128;
 constexpr uint32_t TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_MAX_BYTES;
 constexpr long long TC_WAIT_LIMIT = 1LL << 22;
@@ -45,6 +54,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ uint32_t mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
@@ -65,6 +77,18 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
     }
     return false;
 }
+// Named barrier 1 over the epilogue warps, returning the OR of a predicate over them.
+__device__ __forceinline__ int epi_bar_or(int pred) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.b32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\tselp.b32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"(pred), "n"(TC_EPI_THREADS)
+        : "memory");
+    return r;
+}
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(TC_EPI_THREADS) : "memory"); }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1) {
     asm volatile(
@@ -110,20 +134,33 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// Two 32-column loads (32 lanes x 32 b each) and the wait in one statement, so that no use
+// of the registers can be scheduled before the data has arrived.
+__device__ __forceinline__ void tmem_ld_pair(uint32_t ta, uint32_t tb, float (&a)[32], float (&b)[32]) {
+    uint32_t r[64];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, "
+        "%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%65];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(ta), "r"(tb)
+        : "memory");
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 32; ++i) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[32 + i]);
+    }
 }
 
 __device__ __forceinline__ int find_task(const xrh_tc_task* __restrict__ tasks, int n_tasks, int64_t tile) {
@@ -135,6 +172,33 @@ __device__ __forceinline__ int find_task(const xrh_tc_task* __restrict__ tasks, 
     return lo;
 }
 
+// Where a persistent CTA's tile lies: its task, output corner, N tile and K-chunk range.
+struct TileInfo {
+    int task, m0, n0, BN, nk;
+    int64_t cb;
+};
+
+__device__ __forceinline__ TileInfo tile_info(const xrh_tc_task* __restrict__ tasks, int n_tasks,
+                                              const xrh_tc_segment* __restrict__ segs, int64_t tile) {
+    TileInfo r;
+    r.task = find_task(tasks, n_tasks, tile);
+    const xrh_tc_task& T = tasks[r.task];
+    r.BN = (int)T.bn;
+    const int64_t tiles_m = (T.M + TC_BM - 1) / TC_BM, tiles_n = (T.N + r.BN - 1) / r.BN;
+    int64_t local = tile - T.tile_begin;
+    const int64_t split = local / (tiles_m * tiles_n);
+    local -= split * tiles_m * tiles_n;
+    r.m0 = (int)((local / tiles_n) * TC_BM);
+    r.n0 = (int)((local % tiles_n) * r.BN);
+    int64_t kc_total = 0;
+    for (int64_t s = 0; s < T.seg_count; ++s) kc_total += segs[T.seg_begin + s].kchunks;
+    const int64_t per = (kc_total + T.splitk - 1) / T.splitk;
+    r.cb = split * per;
+    const int64_t ce = (r.cb + per < kc_total) ? r.cb + per : kc_total;
+    r.nk = (int)(ce > r.cb ? ce - r.cb : 0);
+    return r;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_tc_kernel(const xrh_tc_task* __restrict__ tasks, int n_tasks, int64_t total_tiles,
@@ -143,6 +207,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint8_t* stages = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
     __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
+    __shared__ __align__(8) uint64_t ready_bar[2];
+    __shared__ __align__(8) uint64_t drained_bar[2];
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_base_sh;
     __shared__ volatile int abort_sh;
@@ -157,6 +223,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int s = 0; s < TC_STAGES; ++s) {
             mbar_init(smem_u32(&full_bar[s]), 1);
             mbar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&ready_bar[b]), 1);
+            mbar_init(smem_u32(&drained_bar[b]), TC_EPI_WARPS);
         }
         mbar_init(smem_u32(&done_bar), 1);
         abort_sh = 0;
@@ -175,90 +245,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
 
-    uint64_t it = 0;            // chunks issued so far by this CTA (ring position)
-    uint32_t tile_iter = 0;
-    uint32_t done_iter = 0;     // completed phases of done_bar (tiles with at least one chunk)
-    int64_t outstanding_from = 0, outstanding_to = 0;   // chunk loads issued but not yet consumed
-    for (int64_t tile = blockIdx.x; tile < total_tiles && !abort_sh; tile += gridDim.x, ++tile_iter) {
-        const xrh_tc_task& T = tasks[find_task(tasks, n_tasks, tile)];
-        const int BN = (int)T.bn;
-        const int64_t tiles_m = (T.M + TC_BM - 1) / TC_BM, tiles_n = (T.N + BN - 1) / BN;
-        int64_t local = tile - T.tile_begin;
-        const int64_t split = local / (tiles_m * tiles_n);
-        local -= split * tiles_m * tiles_n;
-        const int m0 = (int)((local / tiles_n) * TC_BM), n0 = (int)((local % tiles_n) * BN);
-        int64_t kc_total = 0;
-        for (int64_t s = 0; s < T.seg_count; ++s) kc_total += segs[T.seg_begin + s].kchunks;
-        const int64_t per = (kc_total + T.splitk - 1) / T.splitk;
-        const int64_t cb = split * per;
-        const int64_t ce = (cb + per < kc_total) ? cb + per : kc_total;
-        const int nk = (int)(ce > cb ? ce - cb : 0);
-
-        if (tid == 0 && nk > 0) {
-            const uint32_t b_bytes = (uint32_t)BN * 128u;
-            const uint32_t tx = 2u * TC_A_BYTES + 2u * b_bytes;
-            auto load = [&](int q) -> bool {
-                const uint64_t g = it + q;
-                const int s = (int)(g % TC_STAGES);
-                if (g >= TC_STAGES &&
-                    !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((g / TC_STAGES) - 1) & 1u, &abort_sh))
-                    return false;
-                int64_t c = cb + q, si = T.seg_begin;
-                while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
-                const xrh_tc_segment& S = segs[si];
-                const int kcoord = (int)(c * KCH);
-                uint8_t* st = stages + (size_t)s * TC_STAGE_BYTES;
-                const uint32_t bar = smem_u32(&full_bar[s]);
-                mbar_expect_tx(bar, tx);
-                tma_load_2d(smem_u32(st), maps + S.tmA, bar, kcoord, m0);
-                tma_load_2d(smem_u32(st + TC_A_BYTES), maps + S.tmA + 1, bar, kcoord, m0);
-                tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), maps + S.tmB, bar, kcoord, n0);
-                tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + b_bytes), maps + S.tmB + 1, bar, kcoord, n0);
-                outstanding_to = (int64_t)g + 1;
-                return true;
-            };
-            bool ok = true;
-            const int pre = nk < TC_STAGES ? nk : TC_STAGES;
-            outstanding_from = (int64_t)it;
-            for (int q = 0; q < pre && ok; ++q) ok = load(q);
-            for (int q = 0; q < nk && ok; ++q) {
-                const uint64_t g = it + q;
-                const int s = (int)(g % TC_STAGES);
-                if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(g / TC_STAGES) & 1u, &abort_sh)) { ok = false; break; }
-                outstanding_from = (int64_t)g + 1;
-                tc_fence_after();
-                int64_t c = cb + q, si = T.seg_begin;
-                while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
-                const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)BN, segs[si].negate != 0);
-                const uint32_t st = smem_u32(stages + (size_t)s * TC_STAGE_BYTES);
-                const uint32_t a_hi = st, a_lo = st + TC_A_BYTES;
-                const uint32_t b_hi = st + 2 * TC_A_BYTES, b_lo = b_hi + b_bytes;
-                const uint32_t pa[3] = {a_hi, a_hi, a_lo};
-                const uint32_t pb[3] = {b_hi, b_lo, b_hi};
-                const uint32_t acc_tmem = tmem + (uint32_t)((q % TC_NACC) * 128);
-#pragma unroll
-                for (int p = 0; p < 3; ++p) {
-                    const uint64_t da = umma_desc_sw128(pa[p]);
-                    const uint64_t db = umma_desc_sw128(pb[p]);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)          // 4 MMA K-steps of 32 bytes inside the 128-byte chunk
-                        umma<KIND>(acc_tmem, da + 2 * j, db + 2 * j, idesc,
-                                   (q >= TC_NACC || p > 0 || j > 0) ? 1u : 0u);
+    if (warp == TC_EPI_WARPS) {
+        // ------------------------------------------------------------ producer + MMA --
+        if (lane == 0) {
+            uint64_t gl = 0, gm = 0;           // chunks loaded / consumed by MMAs (global order)
+            int64_t tl = blockIdx.x, tm = blockIdx.x;
+            int ql = 0, qm = 0;
+            TileInfo L{}, Mi{};
+            bool l_ok = false, m_ok = false;
+            // next tile with at least one chunk, from tile t on
+            auto seek = [&](int64_t& t, TileInfo& I) -> bool {
+                for (; t < total_tiles; t += gridDim.x) {
+                    I = tile_info(tasks, n_tasks, segs, t);
+                    if (I.nk > 0) return true;
                 }
+                return false;
+            };
+            l_ok = seek(tl, L);
+            m_ok = seek(tm, Mi);
+            bool ok = true;
+            while (m_ok && ok) {
+                // keep the ring full, across tile boundaries
+                while (l_ok && gl < gm + TC_STAGES && ok) {
+                    const int s = (int)(gl % TC_STAGES);
+                    if (gl >= TC_STAGES &&
+                        !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((gl / TC_STAGES) - 1) & 1u, &abort_sh)) {
+                        ok = false;
+                        break;
+                    }
+                    const xrh_tc_task& T = tasks[L.task];
+                    int64_t c = L.cb + ql, si = T.seg_begin;
+                    while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
+                    const xrh_tc_segment& S = segs[si];
+                    const int kcoord = (int)(c * KCH);
+                    const uint32_t b_bytes = (uint32_t)L.BN * 128u;
+                    uint8_t* st = stages + (size_t)s * TC_STAGE_BYTES;
+                    const uint32_t bar = smem_u32(&full_bar[s]);
+                    mbar_expect_tx(bar, 2u * TC_A_BYTES + 2u * b_bytes);
+                    tma_load_2d(smem_u32(st), maps + S.tmA, bar, kcoord, L.m0);
+                    tma_load_2d(smem_u32(st + TC_A_BYTES), maps + S.tmA + 1, bar, kcoord, L.m0);
+                    tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), maps + S.tmB, bar, kcoord, L.n0);
+                    tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + b_bytes), maps + S.tmB + 1, bar, kcoord, L.n0);
+                    ++gl;
+                    if (++ql == L.nk) {
+                        ql = 0;
+                        tl += gridDim.x;
+                        l_ok = seek(tl, L);
+                    }
+                }
+                if (!ok) break;
+                // the MMAs of chunk gm into chunk buffer gm & 1
+                const int s = (int)(gm % TC_STAGES);
+                const uint32_t b = (uint32_t)(gm & 1);
+                if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(gm / TC_STAGES) & 1u, &abort_sh)) { ok = false; break; }
+                if (gm >= 2 && !mbar_wait(smem_u32(&drained_bar[b]), (uint32_t)((gm >> 1) - 1) & 1u, &abort_sh)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const xrh_tc_task& T = tasks[Mi.task];
+                int64_t c = Mi.cb + qm, si = T.seg_begin;
+                while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
+                const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)Mi.BN, segs[si].negate != 0);
+                const uint32_t b_bytes = (uint32_t)Mi.BN * 128u;
+                const uint32_t st = smem_u32(stages + (size_t)s * TC_STAGE_BYTES);
+                const uint64_t da_hi = umma_desc_sw128(st), da_lo = umma_desc_sw128(st + TC_A_BYTES);
+                const uint64_t db_hi = umma_desc_sw128(st + 2 * TC_A_BYTES);
+                const uint64_t db_lo = umma_desc_sw128(st + 2 * TC_A_BYTES + b_bytes);
+                const uint32_t t_main = tmem + b * 256u, t_corr = t_main + 128u;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)              // 4 MMA K-steps of 32 bytes inside the chunk
+                    umma<KIND>(t_main, da_hi + 2 * j, db_hi + 2 * j, idesc, j > 0 ? 1u : 0u);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_hi + 2 * j, db_lo + 2 * j, idesc, j > 0 ? 1u : 0u);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_lo + 2 * j, db_hi + 2 * j, idesc, 1u);
                 umma_commit(smem_u32(&empty_bar[s]));
-                if (q + TC_STAGES < nk) ok = load(q + TC_STAGES);
+                umma_commit(smem_u32(&ready_bar[b]));
+                ++gm;
+                if (++qm == Mi.nk) {
+                    qm = 0;
+                    tm += gridDim.x;
+                    m_ok = seek(tm, Mi);
+                }
             }
-            umma_commit(smem_u32(&done_bar));
-            it += nk;
             if (!ok) {
                 abort_sh = 1;
                 atomicExch(status, XRH_ERR_TIMEOUT);
             }
+            // before TMEM and shared memory go away: every MMA issued has completed, and every
+            // copy issued has landed (bounded waits)
+            if (gm > 0) {
+                umma_commit(smem_u32(&done_bar));
+                mbar_wait(smem_u32(&done_bar), 0u, nullptr);
+            }
+            for (uint64_t g = gm; g < gl; ++g)
+                mbar_wait(smem_u32(&full_bar[g % TC_STAGES]), (uint32_t)(g / TC_STAGES) & 1u, nullptr);
         }
-        if (nk > 0) {
-            // all threads: per-column scatter metadata of this tile into shared memory
+    } else {
+        // ------------------------------------------------------------------ epilogue --
+        const int quarter = warp & 3, half = warp >> 2;      // TMEM lanes 32*quarter.., column half
+        uint64_t ge = 0;
+        bool aborted = false;
+        for (int64_t tile = blockIdx.x; tile < total_tiles && !aborted; tile += gridDim.x) {
+            const TileInfo I = tile_info(tasks, n_tasks, segs, tile);
+            if (I.nk == 0) continue;
+            const xrh_tc_task& T = tasks[I.task];
+            const int BN = I.BN, m0 = I.m0, n0 = I.n0;
             if (T.mode == 2) {
-                for (int j = tid; j < BN; j += TC_THREADS) {
+                for (int j = tid; j < BN; j += TC_EPI_THREADS) {
                     const int n = n0 + j;
                     const bool ok = n < T.N;
                     s_rowB[j] = ok ? T.rowB[n] : 0;
@@ -267,82 +362,88 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     s_DB[j] = (ok && T.DB) ? T.DB[n] : 0.0;
                 }
             }
-            // accumulator complete -> FP64 epilogue
-            const bool done = mbar_wait(smem_u32(&done_bar), done_iter & 1u, nullptr);
-            ++done_iter;
-            if (!done) {
+            float acc[2][32];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 32; ++j) acc[i][j] = 0.f;
+            for (int q = 0; q < I.nk; ++q, ++ge) {
+                const uint32_t b = (uint32_t)(ge & 1);
+                const bool got = mbar_wait(smem_u32(&ready_bar[b]), (uint32_t)(ge >> 1) & 1u, &abort_sh);
+                if (epi_bar_or(!got)) {
+                    aborted = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int cc = half * 32 + 64 * i;
+                    if (cc < BN) {
+                        float vm[32], vc[32];
+                        tmem_ld_pair(tmem + lane_base + b * 256u + (uint32_t)cc,
+                                     tmem + lane_base + b * 256u + 128u + (uint32_t)cc, vm, vc);
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) acc[i][j] += vm[j] + vc[j];
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&drained_bar[b]));
+            }
+            if (aborted) {
                 abort_sh = 1;
-                atomicExch(status, XRH_ERR_TIMEOUT);
+                if (tid == 0) atomicExch(status, XRH_ERR_TIMEOUT);
+                break;
             }
-            tc_fence_after();
-            __syncthreads();
-            if (done) {
-                const int quarter = warp & 3, half = warp >> 2;      // TMEM lanes 32*quarter.., column half
-                const int m = m0 + quarter * 32 + lane;
-                const bool row_ok = m < T.M;
-                int64_t rbase = 0, cbase = 0;
-                bool dA = false;
-                double DAm = 0.0;
-                if (row_ok) {
-                    if (T.mode == 2) {
-                        rbase = T.rowA[m];
-                        cbase = T.colA[m];
-                        dA = T.diagA[m] != 0;
-                        DAm = T.DA ? T.DA[m] : 0.0;
-                    } else {
-                        rbase = (int64_t)m * T.ldc;
-                    }
+            // FP64 epilogue (the column metadata is visible: the chunk barriers ordered it)
+            const int m = m0 + quarter * 32 + lane;
+            const bool row_ok = m < T.M;
+            int64_t rbase = 0, cbase = 0;
+            bool dA = false;
+            double DAm = 0.0;
+            if (row_ok) {
+                if (T.mode == 2) {
+                    rbase = T.rowA[m];
+                    cbase = T.colA[m];
+                    dA = T.diagA[m] != 0;
+                    DAm = T.DA ? T.DA[m] : 0.0;
+                } else {
+                    rbase = (int64_t)m * T.ldc;
                 }
-                double* C = T.C;
-                const int n_acc = nk < TC_NACC ? nk : TC_NACC;
-                // 32-column chunks of the tile alternate between the two warps of a lane quarter
-                for (int cc = half * 32; cc < BN; cc += 64) {
-                    double sum[32];
+            }
+            double* C = T.C;
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) sum[j] = 0.0;
-                    for (int a = 0; a < n_acc; ++a) {
-                        float v[32];
-                        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128 + cc), v);
+            for (int i = 0; i < 2; ++i) {
+                const int cc = half * 32 + 64 * i;
+                if (cc >= BN || !row_ok) continue;
+                if (T.mode == 2) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) sum[j] += (double)v[j];
-                    }
-                    if (!row_ok) continue;
-                    if (T.mode == 2) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int jj = cc + j;
-                            if (n0 + jj < T.N) {
-                                double x = sum[j];
-                                if (s_diagB[jj]) x += DAm;
-                                if (dA) x += s_DB[jj];
-                                C[(rbase + s_rowB[jj]) * T.ldc + cbase + s_colB[jj]] = x;
-                            }
+                    for (int j = 0; j < 32; ++j) {
+                        const int jj = cc + j;
+                        if (n0 + jj < T.N) {
+                            double x = (double)acc[i][j];
+                            if (s_diagB[jj]) x += DAm;
+                            if (dA) x += s_DB[jj];
+                            C[(rbase + s_rowB[jj]) * T.ldc + cbase + s_colB[jj]] = x;
                         }
-                    } else if (T.mode == 0) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            if (n0 + cc + j < T.N) C[rbase + n0 + cc + j] = sum[j];
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            if (n0 + cc + j < T.N) atomicAdd(C + rbase + n0 + cc + j, sum[j]);
                     }
+                } else if (T.mode == 0) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (n0 + cc + j < T.N) C[rbase + n0 + cc + j] = (double)acc[i][j];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (n0 + cc + j < T.N) atomicAdd(C + rbase + n0 + cc + j, (double)acc[i][j]);
                 }
             }
+            epi_bar();          // metadata reads done before the next tile overwrites it
         }
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-    }
-    // drain: loads issued but never consumed (only after an abort) - bounded waits
-    if (tid == 0) {
-        for (int64_t g = outstanding_from; g < outstanding_to; ++g)
-            mbar_wait(smem_u32(&full_bar[g % TC_STAGES]), (uint32_t)(g / TC_STAGES) & 1u, nullptr);
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    __syncwarp();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
     }

@@ -149,64 +149,128 @@ class SplitRegistry:
                      ptr(op["hi"]), ptr(op["lo"]), s)
 
 
+_TUNE_CACHE = {}
+
+
 class TCGroupedGemm:
-    """Task tables for xrh_gemm_tc_grouped (split precision on tcgen05)."""
+    """Task tables for xrh_gemm_tc_grouped (split precision on tcgen05).
+
+    Tile policy: each task gets an N tile bn in {32, 64, 128} (capped by the policy) and, for
+    accumulating tasks (mode 1), a split-K factor kc_total // div (1..32).  autotune() times
+    every (cap, div) pair on the device with CUDA events and keeps the fastest; results are
+    cached per problem signature, so later plans of the same shapes reuse them."""
+
+    BN_CAPS = (128, 64, 32)
+    SK_DIVS = (16, 4, 8, 32)
 
     def __init__(self, registry):
         self.reg = registry
         self.device = registry.device
-        self._tasks, self._segs, self._keep = [], [], []
+        self._logical = []
         self.flops = 0.0
+        self.policy = (128, 16)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.tuning = None
 
     def add(self, M, N, segments, C, ldc, mode=0, splitk=None, maps=None, DA=None, DB=None, groups=None):
         if M <= 0 or N <= 0:
             return
-        bn = 32 if N <= 32 else (64 if N <= 64 else 128)
-        seg_begin = len(self._segs)
-        kc_total = 0
+        segs = []
         for i, (A, lda, B, ldb, K, alpha) in enumerate(segments):
             assert abs(abs(alpha) - 1.0) < 1e-15, "tensor-core segments take alpha = +-1 (fold scales into operands)"
             ga, gb = (groups[i] if groups else ("in", "in"))
-            opA = self.reg.operand(A, M, K, lda, ga)
-            opB = self.reg.operand(B, N, K, ldb, gb)
-            tmA = self.reg.map_for(A, 128)
-            tmB = self.reg.map_for(B, bn)
-            kch = opA["Kp"] // self.reg.kch
-            self._segs.append((tmA, tmB, kch, 1 if alpha < 0 else 0))
-            kc_total += kch
+            self.reg.operand(A, M, K, lda, ga)
+            self.reg.operand(B, N, K, ldb, gb)
+            segs.append((A, B, 1 if alpha < 0 else 0))
             self.flops += 2.0 * M * N * K
-            self._keep += [A, B]
-        if splitk is None:
-            splitk = int(max(1, min(32, kc_total // 16))) if mode == 1 else 1
-        t = dict(M=M, N=N, seg_begin=seg_begin, seg_count=len(segments), mode=mode, splitk=splitk, bn=bn,
-                 C=C.data_ptr(), ldc=ldc)
-        self._keep.append(C)
-        if mode == 2:
-            for nm, tt in zip(("rowA", "colA", "rowB", "colB", "diagA", "diagB"), maps):
-                t[nm] = tt.data_ptr()
-                self._keep.append(tt)
-            t["DA"] = DA.data_ptr() if DA is not None else 0
-            t["DB"] = DB.data_ptr() if DB is not None else 0
-            self._keep += [x for x in (DA, DB) if x is not None]
-        self._tasks.append(t)
+        self._logical.append(dict(M=M, N=N, segs=segs, C=C, ldc=ldc, mode=mode, splitk=splitk, maps=maps,
+                                  DA=DA, DB=DB))
 
-    def finalize(self):
-        tasks = np.zeros(len(self._tasks), dtype=TC_TASK_DTYPE)
+    def _bn(self, N, cap):
+        bn = 32 if N <= 32 else (64 if N <= 64 else 128)
+        return min(bn, cap)
+
+    def _materialize(self, policy):
+        cap, div = policy
+        tasks = np.zeros(len(self._logical), dtype=TC_TASK_DTYPE)
+        seg_rows = []
         begin = 0
-        for i, t in enumerate(self._tasks):
-            for k, v in t.items():
-                tasks[i][k] = v
-            tasks[i]["tile_begin"] = begin
-            begin += ((t["M"] + TC_BM - 1) // TC_BM) * ((t["N"] + t["bn"] - 1) // t["bn"]) * t["splitk"]
-        self.total_tiles = begin
-        segs = np.zeros(max(len(self._segs), 1), dtype=TC_SEG_DTYPE)
-        for i, s in enumerate(self._segs):
-            segs[i] = s
+        for i, L in enumerate(self._logical):
+            bn = self._bn(L["N"], cap)
+            seg_begin = len(seg_rows)
+            kc_total = 0
+            for (A, B, neg) in L["segs"]:
+                kch = self.reg.ops[A.data_ptr()]["Kp"] // self.reg.kch
+                seg_rows.append((self.reg.map_for(A, TC_BM), self.reg.map_for(B, bn), kch, neg))
+                kc_total += kch
+            sk = L["splitk"]
+            if sk is None:
+                sk = int(max(1, min(32, kc_total // div))) if L["mode"] == 1 else 1
+            t = tasks[i]
+            t["M"], t["N"], t["seg_begin"], t["seg_count"] = L["M"], L["N"], seg_begin, len(L["segs"])
+            t["mode"], t["splitk"], t["bn"], t["C"], t["ldc"] = L["mode"], sk, bn, L["C"].data_ptr(), L["ldc"]
+            if L["mode"] == 2:
+                for nm, tt in zip(("rowA", "colA", "rowB", "colB", "diagA", "diagB"), L["maps"]):
+                    t[nm] = tt.data_ptr()
+                t["DA"] = L["DA"].data_ptr() if L["DA"] is not None else 0
+                t["DB"] = L["DB"].data_ptr() if L["DB"] is not None else 0
+            t["tile_begin"] = begin
+            begin += ((L["M"] + TC_BM - 1) // TC_BM) * ((L["N"] + bn - 1) // bn) * sk
+        segs = np.zeros(max(len(seg_rows), 1), dtype=TC_SEG_DTYPE)
+        for i, r in enumerate(seg_rows):
+            segs[i] = r
+        return tasks, segs, begin
+
+    def finalize(self, policy=None):
+        """Build and upload the task tables for a policy (default: the current one).  The
+        registry's maps must be uploaded (again) when this adds a box height: finalize
+        does it itself when needed."""
+        if policy is not None:
+            self.policy = policy
+        n_maps = len(self.reg.maps)
+        tasks, segs, total = self._materialize(self.policy)
+        if len(self.reg.maps) != n_maps or self.reg.maps_dev is None:
+            self.reg.upload()
+        self.total_tiles = total
         self.tasks_dev = torch.from_numpy(tasks.view(np.uint8).copy()).to(self.device)
         self.segs_dev = torch.from_numpy(segs.view(np.uint8).copy()).to(self.device)
-        self.n_tasks = len(self._tasks)
+        self.n_tasks = len(self._logical)
         return self
+
+    def signature(self):
+        return (self.reg.prec,) + tuple((L["M"], L["N"], L["mode"], L["splitk"],
+                                         tuple(self.reg.ops[A.data_ptr()]["Kp"] for (A, _, _) in L["segs"]))
+                                        for L in self._logical)
+
+    def autotune(self, reps=3):
+        """Time every tile policy on the device (the launch writes its own outputs; call it
+        before the first build, which clears accumulation targets itself) and keep the best."""
+        if not self._logical:
+            return self
+        key = self.signature()
+        if key in _TUNE_CACHE:
+            return self.finalize(_TUNE_CACHE[key])
+        has_acc = any(L["mode"] == 1 and L["splitk"] is None for L in self._logical)
+        caps = [c for c in self.BN_CAPS if c == 128 or any(L["N"] > c for L in self._logical)]
+        divs = self.SK_DIVS if has_acc else self.SK_DIVS[:1]
+        results = []
+        for cap in caps:
+            for div in divs:
+                self.finalize((cap, div))
+                self.run()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    self.run()
+                e1.record()
+                torch.cuda.synchronize()
+                results.append((e0.elapsed_time(e1) / reps, (cap, div)))
+        self.check()
+        results.sort()
+        self.tuning = [(p, round(ms, 4)) for ms, p in results]
+        _TUNE_CACHE[key] = results[0][1]
+        return self.finalize(results[0][1])
 
     def run(self, stream=None):
         if self.n_tasks == 0:

@@ -52,6 +52,23 @@ class DeviceIntegrals:
         self._V = torch.as_tensor(np.asarray(V, dtype=np.float64), device=self.device)
         self._src = None
 
+    @classmethod
+    def from_tensors(cls, h, V, Ns, U=None):
+        """Device tensors in (no host round trip): h (tot x tot, U folded in when U is None),
+        V (tot^4), U (n_frag x tot x tot) or None."""
+        self = cls.__new__(cls)
+        self.device = h.device
+        self._cache = {}
+        self.Ns = list(Ns)
+        self.off = np.concatenate([[0], np.cumsum(self.Ns)]).astype(int)
+        tot = int(self.off[-1])
+        self._h = h
+        self._U = torch.zeros((len(self.Ns), tot, tot), dtype=h.dtype, device=h.device) if U is None else U
+        self._Tfull = h - self._U.sum(0)
+        self._V = V
+        self._src = None
+        return self
+
     def _sl(self, m):
         return slice(int(self.off[m]), int(self.off[m + 1]))
 
@@ -154,6 +171,8 @@ class XRDimerPlan:
     ints:     DeviceIntegrals
     output:   'split' -> (H1 list, H2) as get_xr_H returns them;
               'full'  -> H = H2 + H1 x 1 + 1 x H1 (mains/workflow.py:216-230)
+    autotune: time the tile policies of the tensor-core launches on the device once per
+              problem shape and keep the fastest (TCGroupedGemm.autotune).
     convention: 'hermitian' (diagram phases of hermitian-XRCC) or 'general' (the sign
               convention of general-XRCC/build_H.py:68, charge-transfer blocks differ by
               the gauge (-1)^(n_i1 + n_j0)).
@@ -164,7 +183,8 @@ class XRDimerPlan:
     """
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
-                 convention="hermitian", layout="product", dens_precision=None, sigma_precision=None):
+                 convention="hermitian", layout="product", dens_precision=None, sigma_precision=None,
+                 autotune=True):
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
         self.ints = ints
@@ -187,16 +207,7 @@ class XRDimerPlan:
         chg, ns = self.charges, self.n_states
 
         # ---- integral matrices in B-role layout [x, y] (y contracted, contiguous) ----
-        W = {}
-        W["v0101"] = (4.0 * ints.V(0, 1, 0, 1).permute(1, 3, 0, 2).reshape(N[1] ** 2, N[0] ** 2)).contiguous()
-        for m, o in ((0, 1), (1, 0)):
-            h_mo = ints.T(m, o) + ints.U(m, m, o) + ints.U(o, m, o)
-            W[("h1", m)] = h_mo.t().contiguous()                                                   # [q, p]
-            W[("cca", m)] = (-2.0 * ints.V(m, m, m, o).permute(3, 0, 1, 2).reshape(N[o], N[m] ** 3)).contiguous()
-            W[("caa", m)] = (2.0 * ints.V(m, o, m, m).permute(1, 0, 3, 2).reshape(N[o], N[m] ** 3)).contiguous()
-            W[("cc", m)] = ints.V(m, m, o, o).permute(3, 2, 0, 1).reshape(N[o] ** 2, N[m] ** 2).contiguous()
-            W[("hmm", m)] = (ints.T(m, m) + ints.U(m, m, m)).reshape(1, N[m] ** 2).contiguous()
-            W[("u100", m)] = ints.U(o, m, m).reshape(1, N[m] ** 2).contiguous()
+        W = self._integral_matrices(ints)
         self.W = W
 
         # ---- accumulation targets (one arena, cleared by one memset per build) ----
@@ -410,8 +421,42 @@ class XRDimerPlan:
             reg.upload()
             reg.split("W")
             self.reg, self.pre_tc, self.pre64, self.fin_tc = reg, pre_tc.finalize(), pre64.finalize(), fin_tc.finalize()
+            if autotune:
+                self.pre_tc.autotune()
+                self.fin_tc.autotune()
 
     # ------------------------------------------------------------------------------------
+    def _integral_matrices(self, ints):
+        """Integral blocks with the diagram prefactors folded in, in B-role layout [x, y]
+        (y contracted, contiguous): v0101 (4 V_0101, hermitian-XRCC/diagrams/SV_2mer_0.py:28),
+        h1 (T + U of t01/u001-type transfers, ST_2mer_0.py:28, SU_2mer_0.py:37-118), cca and
+        caa (2 V of v0001/v0100 with their phases, SV_2mer_0.py:39,50), cc (v0011,
+        SV_2mer_0.py:61), hmm and u100 (the monomer and u100 terms)."""
+        N = self.N
+        W = {}
+        W["v0101"] = (4.0 * ints.V(0, 1, 0, 1).permute(1, 3, 0, 2).reshape(N[1] ** 2, N[0] ** 2)).contiguous()
+        for m, o in ((0, 1), (1, 0)):
+            h_mo = ints.T(m, o) + ints.U(m, m, o) + ints.U(o, m, o)
+            W[("h1", m)] = h_mo.t().contiguous()                                                   # [q, p]
+            W[("cca", m)] = (-2.0 * ints.V(m, m, m, o).permute(3, 0, 1, 2).reshape(N[o], N[m] ** 3)).contiguous()
+            W[("caa", m)] = (2.0 * ints.V(m, o, m, m).permute(1, 0, 3, 2).reshape(N[o], N[m] ** 3)).contiguous()
+            W[("cc", m)] = ints.V(m, m, o, o).permute(3, 2, 0, 1).reshape(N[o] ** 2, N[m] ** 2).contiguous()
+            W[("hmm", m)] = (ints.T(m, m) + ints.U(m, m, m)).reshape(1, N[m] ** 2).contiguous()
+            W[("u100", m)] = ints.U(o, m, m).reshape(1, N[m] ** 2).contiguous()
+        return W
+
+    def set_integrals(self, ints):
+        """Replace the integrals in place: every launch table keeps its pointers, so a captured
+        CUDA graph stays valid.  Enqueued on the current stream (no host synchronisation)."""
+        for k, w in self._integral_matrices(ints).items():
+            self.W[k].copy_(w)
+        for m in (0, 1):
+            for c, sg in self.sigma[m].items():
+                sg.V.copy_(ints.V(m, m, m, m))
+        if self.tc:
+            self.reg.split("W")
+        self.ints = ints
+
     def set_coeffs(self, coeffs):
         """Copy new state coefficients {charge: (n_states, n_conf)} per fragment into the plan."""
         for m in (0, 1):

@@ -69,3 +69,35 @@ def test_tc_dimer_H_close_to_oracle(prec):
     print(f"{prec}: max|dH| = {err:.3e}, |dE0| = {abs(e_gpu - e_ref):.3e}")
     assert err < {"bf16x3": 1e-3, "tf32x3": 2e-5}[prec]
     assert abs(e_gpu - e_ref) < 1e-6 if prec == "tf32x3" else abs(e_gpu - e_ref) < 1e-4
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_tc_gemm_every_tile_policy(prec):
+    """Every (N-tile cap, split-K divisor) the autotuner may pick gives the same result."""
+    from qodeapplications_gb300.gemm import SplitRegistry, TCGroupedGemm
+    g = torch.Generator().manual_seed(4)
+    A = torch.randn(260, 512, generator=g, dtype=torch.float64).cuda()
+    B = torch.randn(200, 512, generator=g, dtype=torch.float64).cuda()
+    B2 = torch.randn(40, 512, generator=g, dtype=torch.float64).cuda()
+    reg = SplitRegistry(prec)
+    C = torch.zeros(260, 200, dtype=torch.float64, device="cuda")
+    C2 = torch.zeros(260, 40, dtype=torch.float64, device="cuda")
+    tc = TCGroupedGemm(reg)
+    tc.add(260, 200, [(A, 512, B, 512, 512, 1.0)], C, 200, mode=1)
+    tc.add(260, 40, [(A, 512, B2, 512, 512, -1.0)], C2, 40, mode=1)
+    reg.upload()
+    reg.split("in")
+    ref, ref2 = A @ B.t(), -(A @ B2.t())
+    for cap in TCGroupedGemm.BN_CAPS:
+        for div in TCGroupedGemm.SK_DIVS:
+            tc.finalize((cap, div))
+            reg.split("in")
+            C.zero_()
+            C2.zero_()
+            tc.run()
+            torch.cuda.synchronize()
+            tc.check()
+            assert _rel(C, ref) < TOL[prec], (cap, div, _rel(C, ref))
+            assert _rel(C2, ref2) < TOL[prec], (cap, div, _rel(C2, ref2))
+    tc.autotune()
+    assert tc.tuning is not None and tc.policy in [p for p, _ in tc.tuning]
