@@ -485,18 +485,18 @@ def gen_trimer_block(rho, T, U, V, n_elec, m, chg_i, chg_j):
 
     # 2min1pls1pls: 2 sum V[p1 q1 r2 s3] Rcc1[q1,p1] Ra2[r2] Ra3[s3]  (H_contractions.c:184-204)
     def t2m(Rcc, Ra, Rb, Vb):
-        return 2 * np.einsum("pqrs,xaqp,ybr,zcs->xyzabc", Vb, Rcc, Ra, Rb)
+        return 2 * np.einsum("pqrs,xaqp,ybr,zcs->xyzabc", Vb, Rcc, Ra, Rb, optimize=True)
 
     # 2pls1min1min: 2 sum V[r2 s3 p1 q1] Raa1[q1,p1] Rc2[r2] Rc3[s3]  (:208-228)
     def t2p(Raa, Rc, Rd, Vb):
-        return 2 * np.einsum("rspq,xaqp,ybr,zcs->xyzabc", Vb, Raa, Rc, Rd)
+        return 2 * np.einsum("rspq,xaqp,ybr,zcs->xyzabc", Vb, Raa, Rc, Rd, optimize=True)
 
     # Ex1min1pls: 4 sum V[p1 r2 q1 s3] Rca1[p1,q1] Rc2[r2] Ra3[s3]  (:232-252)
     def tex(Rca, Rc, Ra, Vb):
-        return 4 * np.einsum("prqs,xapq,ybr,zcs->xyzabc", Vb, Rca, Rc, Ra)
+        return 4 * np.einsum("prqs,xapq,ybr,zcs->xyzabc", Vb, Rca, Rc, Ra, optimize=True)
 
     def ext(Rc, Ra, Ub, nI):   # dimer_1min1pls_1e(Rc, Ra, U) times delta on the Ex fragment
-        return np.einsum("pq,ybp,zcq,xa->xyzabc", Ub, Rc, Ra, np.eye(nI))
+        return np.einsum("pq,ybp,zcq,xa->xyzabc", Ub, Rc, Ra, np.eye(nI), optimize=True)
 
     def perm(x, order):
         # x indexed (f_order[0], f_order[1], f_order[2]) for bra then ket -> absolute (1,2,3)
@@ -548,6 +548,90 @@ def gen_trimer_block(rho, T, U, V, n_elec, m, chg_i, chg_j):
 # ----------------------------------------------------------------------------------------
 # supersystem FCI in the product-determinant basis (known-answer test)
 # ----------------------------------------------------------------------------------------
+
+def general_xr_H_full(dens, ints, n_ref, charges, n_frag):
+    """Order-0 general-XRCC Hamiltonian of n_frag fragments (2 or 3) in the full product
+    basis |I_0 I_1 ... > = C_0 C_1 ... |0> (fragment-major, charge blocks in `charges` order):
+    monomer terms (build_H.py:38-47), pair blocks (build_H.py:48-102) and triple blocks
+    (build_H.py:103-188), each embedded with identity on the other fragments.
+
+    The embedding carries the fermionic phase of spectator fragments that the reference's
+    own embedding (general-XRCC/hamiltonian.py:18-80) leaves out: moving the operators of a
+    term past the creation string C_O of a spectator O costs (-1)^(n_O * p), p = parity of
+    the number of the term's operators on fragments after O.  With it, complete fragment
+    bases reproduce the supersystem FCI spectrum (exact for 3 fragments; without it, odd
+    charge transfers between fragments 0 and 2 take the wrong sign).  Small systems only."""
+    ns = [dens[0]["n_states"][c] for c in charges]          # identical state counts on every fragment
+    tot = sum(ns)
+    off = np.concatenate([[0], np.cumsum(ns)]).astype(int)
+    chg_of = np.concatenate([[c] * n for c, n in zip(charges, ns)])
+    par_n = ((n_ref - chg_of) % 2).astype(int)              # electron-count parity of each state
+    T, U, V = ints.T, ints.U, ints.V
+    nel = [n_ref] * n_frag
+    nuc = np.zeros((n_frag, n_frag))
+    eye = np.eye(tot)
+    dim = tot ** n_frag
+    H = np.zeros((tot,) * (2 * n_frag))
+    letters = "abcdefghijkl"
+
+    dq = (np.abs(chg_of[:, None] - chg_of[None, :]) % 2).astype(int)   # charge-change parity (bra, ket)
+
+    def axes_shape(pairs):
+        shape = [1] * (2 * n_frag)
+        for ax in pairs:
+            shape[ax] = tot
+        return shape
+
+    def embed(block, frags):
+        """block indexed (bra of frags..., ket of frags...) -> full product space."""
+        others = [o for o in range(n_frag) if o not in frags]
+        bra = [letters[f] for f in range(n_frag)]
+        ket = [letters[n_frag + f] for f in range(n_frag)]
+        spec = "".join(bra[f] for f in frags) + "".join(ket[f] for f in frags)
+        terms = [spec] + [bra[o] + ket[o] for o in others]
+        out = np.einsum(",".join(terms) + "->" + "".join(bra + ket), block, *[eye] * len(others))
+        for o in others:
+            p = 0
+            for f in frags:
+                if f > o:
+                    p = p + dq.reshape(axes_shape([f, n_frag + f]))
+            if np.ndim(p) == 0:
+                continue
+            n_o = par_n.reshape(axes_shape([o]))
+            out = out * (1.0 - 2.0 * ((p * n_o) % 2))
+        return out
+
+    for m in range(n_frag):
+        h1 = np.zeros((tot, tot))
+        for a_, ch in enumerate(charges):
+            sl = slice(off[a_], off[a_ + 1])
+            h1[sl, sl] = (np.einsum("pq,ijpq->ij", T[m, m] + U[m, m, m], dens[m]["ca"][(ch, ch)]) +
+                          gen_monomer_2e(dens[m]["ccaa"][(ch, ch)], V[m, m, m, m]))
+        H += embed(h1, [m])
+    for m1 in range(n_frag):
+        for m2 in range(m1 + 1, n_frag):
+            blk = np.zeros((tot,) * 4)
+            for a_, ci1 in enumerate(charges):
+                for b_, ci2 in enumerate(charges):
+                    for c_, cj1 in enumerate(charges):
+                        for d_, cj2 in enumerate(charges):
+                            x = gen_dimer_block(dens, T, U, V, nel, nuc, m1, m2, ci1, cj1, ci2, cj2)
+                            if x is not None:
+                                blk[off[a_]:off[a_ + 1], off[b_]:off[b_ + 1], off[c_]:off[c_ + 1],
+                                    off[d_]:off[d_ + 1]] += x
+            H += embed(blk, [m1, m2])
+    if n_frag == 3:
+        blk = np.zeros((tot,) * 6)
+        for ci in np.ndindex(*(len(charges),) * 3):
+            for cj in np.ndindex(*(len(charges),) * 3):
+                x = gen_trimer_block(dens, T, U, V, nel, (0, 1, 2), tuple(charges[i] for i in ci),
+                                     tuple(charges[j] for j in cj))
+                if x is not None:
+                    sl = tuple(slice(off[i], off[i + 1]) for i in ci) + tuple(slice(off[j], off[j + 1]) for j in cj)
+                    blk[sl] += x
+        H += blk          # all three fragments take part: no spectator
+    return H.reshape(dim, dim)
+
 
 def fci_hamiltonian(h, V, masks):
     """<P|H|Q> for H = sum h_pq c+_p a_q + sum V_pqrs c+_p c+_q a_s a_r over global

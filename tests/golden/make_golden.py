@@ -18,6 +18,11 @@ general-XRCC/density_tensors.c ranks by.  Outputs come from the compiled referen
 * be_dimer_elements.npz: dimer matrix elements of a Be2 system (fixture states on both
   fragments, seeded synthetic integrals, n_core = 1) computed element by element with the
   reference C kernels exactly as general-XRCC/build_H.py:56-102 dispatches them.
+* be_trimer_elements.npz: trimer matrix elements of a Be3 system (fixture states on all
+  three fragments, seeded synthetic integrals with nonzero nuclear potentials U) computed
+  element by element with the reference C trimer kernels (H_contractions.c:184-252) as
+  general-XRCC/build_H.py:103-188 dispatches them.  Only this file:
+      python tests/golden/make_golden.py [REFERENCE_ROOT] --trimer
 """
 import os
 import pickle
@@ -174,5 +179,90 @@ def main(ref_root):
     print("golden fixtures written to", HERE)
 
 
+def trimer_elements(ref_root, n_el=300):
+    assert R.available(), "run oracle/build_ref.sh first"
+    from qodeapplications_gb300 import synthetic as S
+    N = 2 * N_ORBS
+    sectors = load_be_sectors(ref_root)
+    secs = [(sectors[c][0], O.masks_to_occ(sectors[c][1], N)) for c in CHARGES]
+    rho = {}
+    for bi, bc in enumerate(CHARGES):
+        for ki, kc in enumerate(CHARGES):
+            for op in O.OPS_FOR_DCHG.get(bc - kc, ()):
+                if op in ("a", "c", "ca", "aa", "cc"):
+                    rho.setdefault(op, {})[(bc, kc)] = R.ref_density(op, secs, bi, ki, N_ORBS, N_CORE)
+    ns = {c: sectors[c][0].shape[0] for c in CHARGES}
+    rng = np.random.default_rng(777)
+    nsp = 3 * N_ORBS
+    a = rng.normal(0, 0.1, (nsp, nsp))
+    h_sp = np.triu(a) + np.triu(a, 1).T
+    L = rng.normal(0, 0.05, (20, nsp, nsp))
+    L = 0.5 * (L + L.transpose(0, 2, 1))
+    u_sp = []
+    U = []
+    for _k in range(3):
+        b = rng.normal(0, 0.05, (nsp, nsp))
+        b = np.triu(b) + np.triu(b, 1).T
+        u_sp.append(b)
+        U.append(S.spin_orbital_integrals(b, np.zeros((nsp,) * 4), [N_ORBS] * 3)[0])
+    U = np.array(U)
+    h, V = S.spin_orbital_integrals(h_sp, np.einsum("kpq,krs->pqrs", L, L), [N_ORBS] * 3)
+    ints = O.FragInts(h + U.sum(0), V, [N, N, N], U=U)
+    Ub, Vb = ints.U, ints.V
+    el = []
+    rng2 = np.random.default_rng(6)
+    m1, m2, m3 = 0, 1, 2
+    while len(el) < n_el:
+        ci = [int(x) for x in rng2.choice(CHARGES, 3)]
+        cj = [int(x) for x in rng2.choice(CHARGES, 3)]
+        d = sorted(x - y for x, y in zip(ci, cj))
+        if d not in ([-2, 1, 1], [-1, 0, 1], [-1, -1, 2]):
+            continue
+        I = [int(rng2.integers(ns[c])) for c in ci]
+        J = [int(rng2.integers(ns[c])) for c in cj]
+        k = [(ci[x], cj[x]) for x in range(3)]
+
+        def r(op, x):
+            return rho[op][k[x]][I[x], J[x]]
+        s2 = (-1) ** ((N_ELEC_REF - ci[1]) % 2)
+        s3 = (-1) ** ((N_ELEC_REF - ci[2]) % 2)
+        t2m, t2p, tex, ext = "trimer_2min1pls1pls", "trimer_2pls1min1min", "trimer_Ex1min1pls", "dimer_1min1pls_1e"
+        if ci[0] == cj[0] - 2:
+            v = s3 * R.ref_h(t2m, N, N, N, r("cc", 0), r("a", 1), r("a", 2), Vb[m1, m1, m2, m3])
+        elif ci[1] == cj[1] - 2:
+            v = s2 * s3 * R.ref_h(t2m, N, N, N, r("cc", 1), r("a", 0), r("a", 2), Vb[m2, m2, m1, m3])
+        elif ci[2] == cj[2] - 2:
+            v = s2 * R.ref_h(t2m, N, N, N, r("cc", 2), r("a", 0), r("a", 1), Vb[m3, m3, m1, m2])
+        elif ci[0] == cj[0] + 2:
+            v = s3 * R.ref_h(t2p, N, N, N, r("aa", 0), r("c", 1), r("c", 2), Vb[m2, m3, m1, m1])
+        elif ci[1] == cj[1] + 2:
+            v = s2 * s3 * R.ref_h(t2p, N, N, N, r("aa", 1), r("c", 0), r("c", 2), Vb[m1, m3, m2, m2])
+        elif ci[2] == cj[2] + 2:
+            v = s2 * R.ref_h(t2p, N, N, N, r("aa", 2), r("c", 0), r("c", 1), Vb[m1, m2, m3, m3])
+        else:
+            # one fragment keeps its charge (Rca), one gains and one loses an electron
+            ex = [x for x in range(3) if ci[x] == cj[x]][0]
+            cr = [x for x in range(3) if ci[x] == cj[x] - 1][0]
+            an = [x for x in range(3) if ci[x] == cj[x] + 1][0]
+            mm = (m1, m2, m3)
+            tmp = R.ref_h(tex, N, N, N, r("ca", ex), r("c", cr), r("a", an), Vb[mm[ex], mm[cr], mm[ex], mm[an]])
+            if I[ex] == J[ex]:
+                tmp += R.ref_h(ext, N, N, r("c", cr), r("a", an), Ub[mm[ex], mm[cr], mm[an]])
+            # the phase of build_H.py:146-187 for each (Ex, creating, annihilating) placement
+            sgn = {(0, 1, 2): s3, (0, 2, 1): -s3, (1, 0, 2): s2 * s3, (1, 2, 0): -s2 * s3,
+                   (2, 0, 1): s2, (2, 1, 0): -s2}[(ex, cr, an)]
+            v = sgn * tmp
+        el.append(tuple(ci) + tuple(cj) + tuple(I) + tuple(J) + (v,))
+    np.savez_compressed(os.path.join(HERE, "be_trimer_elements.npz"), h_sp=h_sp, L=L, u_sp=np.array(u_sp),
+                        elements=np.array(el, dtype=np.float64))
+    print("trimer fixture written to", HERE)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--trimer" in sys.argv:
+        trimer_elements(root)
+    else:
+        main(root)
+        trimer_elements(root)

@@ -192,3 +192,68 @@ def test_reference_kernels_direct_on_synthetic():
                 got = O.transition_density(op, osecs[bc].coeffs, osecs[bc].masks, osecs[kc].coeffs,
                                            osecs[kc].masks, N, n_orb, 0)
                 np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13)
+
+
+def test_trimer_elements_match_reference(golden_dir):
+    """Oracle trimer blocks (general-XRCC/build_H.py:103-188) against elements the compiled
+    reference kernels (H_contractions.c:184-252) produced for a Be3 system with nuclear
+    potentials, dispatched as build_H.py does."""
+    g, sectors = _be(golden_dir)
+    e = np.load(os.path.join(golden_dir, "be_trimer_elements.npz"))
+    N = 2 * N_ORBS
+    U = np.array([S.spin_orbital_integrals(u, np.zeros((3 * N_ORBS,) * 4), [N_ORBS] * 3)[0] for u in e["u_sp"]])
+    h, V = S.spin_orbital_integrals(e["h_sp"], np.einsum("kpq,krs->pqrs", e["L"], e["L"]), [N_ORBS] * 3)
+    ints = O.FragInts(h + U.sum(0), V, [N, N, N], U=U)
+    dens = O.build_densities(sectors, N_ORBS, N_CORE, N_REF, ops=("a", "c", "ca", "aa", "cc"))
+    rho = [dens, dens, dens]
+    cache = {}
+    for row in e["elements"]:
+        ci, cj = tuple(int(x) for x in row[0:3]), tuple(int(x) for x in row[3:6])
+        I, J = [int(x) for x in row[6:9]], [int(x) for x in row[9:12]]
+        v = row[12]
+        if (ci, cj) not in cache:
+            cache[(ci, cj)] = O.gen_trimer_block(rho, ints.T, ints.U, ints.V, [N_REF] * 3, (0, 1, 2), ci, cj)
+        got = cache[(ci, cj)][I[0], I[1], I[2], J[0], J[1], J[2]]
+        assert abs(got - v) <= 1e-12 * max(1.0, abs(v)), (ci, cj, got, v)
+
+
+def _complete_basis_system(n_frag, seed=3, n_orb=2, n_ref=2):
+    rng = np.random.default_rng(seed)
+    N = 2 * n_orb
+    nsp = n_frag * n_orb
+    a = rng.normal(0, 0.3, (nsp, nsp))
+    L = rng.normal(0, 0.2, (5, nsp, nsp))
+    L = L + L.transpose(0, 2, 1)
+    h, V = S.spin_orbital_integrals(a + a.T, np.einsum("kpq,krs->pqrs", L, L), [n_orb] * n_frag)
+    U = np.zeros((n_frag, n_frag * N, n_frag * N))
+    for k in range(n_frag):
+        b = rng.normal(0, 0.2, (nsp, nsp))
+        U[k], _ = S.spin_orbital_integrals(b + b.T, np.zeros((nsp,) * 4), [n_orb] * n_frag)
+    htot = h + U.sum(0)
+    ints = O.FragInts(htot, V, [N] * n_frag, U=U)
+    charges = [2, 1, 0, -1, -2]
+    secs, dens = [], []
+    for _m in range(n_frag):
+        sec = {c: O.Sector(np.eye(len(O.all_configs(n_orb, 0, n_ref - c))), O.all_configs(n_orb, 0, n_ref - c))
+               for c in charges}
+        secs.append(sec)
+        dens.append(O.build_densities(sec, n_orb, 0, n_ref))
+    masks = [np.concatenate([secs[m][c].masks for c in charges]) for m in range(n_frag)]
+    G, ntot = masks[0], O.popcount(masks[0])
+    for m in range(1, n_frag):
+        G = (G[:, None] | (masks[m][None, :] << np.uint64(m * N))).reshape(-1)
+        ntot = (ntot[:, None] + O.popcount(masks[m])[None, :]).reshape(-1)
+    sel = np.nonzero(ntot == n_frag * n_ref)[0]
+    return ints, dens, charges, O.fci_hamiltonian(htot, V, G), sel, n_ref
+
+
+def test_three_fragment_complete_basis_reproduces_fci():
+    """Known answer for the trimer terms: with complete fragment bases the order-0
+    general-XRCC Hamiltonian of three fragments (monomers, the three pairs and the triple,
+    build_H.py:38-188) is the supersystem Hamiltonian in another basis phase convention."""
+    ints, dens, charges, Hf, sel, n_ref = _complete_basis_system(3)
+    Hx = O.general_xr_H_full(dens, ints, n_ref, charges, 3)
+    assert len(sel) == 924
+    Hs, Fs = Hx[np.ix_(sel, sel)], Hf[np.ix_(sel, sel)]
+    np.testing.assert_allclose(np.abs(Hs), np.abs(Fs), atol=1e-12)
+    np.testing.assert_allclose(np.linalg.eigvalsh(Hs), np.linalg.eigvalsh(Fs), atol=1e-11)
