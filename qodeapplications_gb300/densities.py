@@ -103,6 +103,18 @@ class FragmentSpace:
                         continue
                     self.couplings[(op, bc, kc)] = self._build(op, bc, kc)
 
+    def pair_list(self, c):
+        """Device copy of build_pair_list for charge c (cached), or None."""
+        if not hasattr(self, "_pairs"):
+            self._pairs = {}
+        if c not in self._pairs:
+            pl = build_pair_list(self.masks_np[c], self.n_orbs)
+            if pl is not None:
+                for k in ("X", "off", "sign", "xptr"):
+                    pl[k + "_dev"] = torch.from_numpy(pl[k]).to(self.device)
+            self._pairs[c] = pl
+        return self._pairs[c]
+
     def _build(self, op, bc, kc):
         n_ket, n_bra = self.n_conf[kc], self.n_conf[bc]
         K = self.N ** len(op)
@@ -130,6 +142,65 @@ class FragmentSpace:
         if total:
             idx_ptr[1:] = torch.cumsum(torch.bincount(idx.to(torch.int64), minlength=K), 0)
         return Couplings(op, K, idx_ptr, P, Q, sign)
+
+
+def _popcount64(x):
+    x = x.astype(np.uint64)
+    out = np.zeros(x.shape, dtype=np.int64)
+    for sh in range(0, 64, 8):
+        out += _POP8[((x >> np.uint64(sh)) & np.uint64(0xFF)).astype(np.int64)]
+    return out
+
+
+_POP8 = np.array([bin(i).count("1") for i in range(256)], dtype=np.int64)
+
+
+def build_pair_list(masks, n_orbs):
+    """Pair list of one determinant space for the two-electron terms through (n-2)-electron
+    intermediates (the layout of include/xrh.h, xrh_pair_scatter / xrh_pair_gather).
+
+    For every determinant X (uint64 masks over N = 2 n_orbs spin orbitals, alpha block then
+    beta block) and occupied pair u < v: K = X - u - v, sign of <K| a_v a_u |X> (parity of
+    the occupied orbitals above u plus those above v), spin class c = number of beta
+    orbitals in (u, v).  Pairs and intermediates are numbered inside their class; a class
+    block holds nK_c x np_c positions, blocks concatenated: off = base_c + k * np_c + pair.
+    A spin-conserving two-electron operator only couples pairs of the same class, so the
+    classes need not be tied to one Sz: the space may mix Sz values.  Returns None for
+    fewer than two electrons or mixed electron counts."""
+    masks = np.asarray(masks, dtype=np.uint64)
+    n_conf = len(masks)
+    if n_conf == 0:
+        return None
+    ne = int(_popcount64(masks[:1])[0])
+    if ne < 2 or (_popcount64(masks) != ne).any():
+        return None
+    N = 2 * n_orbs
+    occ = np.zeros((n_conf, ne), dtype=np.int64)
+    for j, row in enumerate(((masks[:, None] >> np.arange(N, dtype=np.uint64)[None, :]) & np.uint64(1)).astype(bool)):
+        occ[j] = np.nonzero(row)[0]
+    iu, iv = np.triu_indices(ne, 1)
+    u, v = occ[:, iu].ravel(), occ[:, iv].ravel()
+    X = np.repeat(np.arange(n_conf, dtype=np.int64), len(iu))
+    mX = masks[X]
+    K = mX & ~(np.uint64(1) << u.astype(np.uint64)) & ~(np.uint64(1) << v.astype(np.uint64))
+    par = (_popcount64(mX >> (u + 1).astype(np.uint64)) + _popcount64(mX >> (v + 1).astype(np.uint64))) & 1
+    cls = (u >= n_orbs).astype(np.int64) + (v >= n_orbs).astype(np.int64)
+    off = np.zeros(len(X), dtype=np.int64)
+    classes = []
+    base = 0
+    for c in range(3):
+        sel = np.nonzero(cls == c)[0]
+        if len(sel) == 0:
+            continue
+        pair_key = u[sel] * N + v[sel]
+        pairs, pidx = np.unique(pair_key, return_inverse=True)
+        Ks, kidx = np.unique(K[sel], return_inverse=True)
+        n_p, n_k = len(pairs), len(Ks)
+        off[sel] = base + kidx * n_p + pidx
+        classes.append(dict(base=base, n_K=n_k, n_p=n_p, u=pairs // N, v=pairs % N))
+        base += n_k * n_p
+    return dict(X=X.astype(np.int32), off=off, sign=np.where(par == 1, -1, 1).astype(np.int8),
+                xptr=np.arange(n_conf + 1, dtype=np.int64) * len(iu), L=base, classes=classes, n_conf=n_conf)
 
 
 class DensityBuilder:

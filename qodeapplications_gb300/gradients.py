@@ -70,6 +70,10 @@ class XRDimerAdjoint:
                 if c in plan.H1blk[m]:
                     want(("gblk", m, c), (ns[m][c], ns[m][c]))
                     want(("YT", m, c), (plan.spaces[m].n_conf[c], ns[m][c]))
+                    sg = plan.sigma[m][c]
+                    if sg.pl is not None:
+                        for k, cl in enumerate(sg.pl["classes"]):
+                            want(("Gpair", m, c, k), (cl["n_p"], cl["n_p"]))
         for i, t in enumerate(plan.final_tasks):
             ni0, nj0, ni1, nj1 = t["dims"]
             for s, (A, lda, B, ldb, K, a) in enumerate(t["segs"]):
@@ -164,6 +168,32 @@ class XRDimerAdjoint:
             self.gz32 = [{c: torch.zeros((plan.spaces[m].n_conf[c], ns[m][c]), dtype=torch.float32, device=dev)
                           for c in plan.charges[m]} for m in (0, 1)]
             self.Gamma32 = [torch.zeros(N[m] ** 4, dtype=torch.float32, device=dev) for m in (0, 1)]
+        # ---- two-particle density of the monomer two-electron term through (n-2)-electron
+        # intermediates: Gamma[pq, rs] = sum_(I, K) D_zb[I, (K, pq)] D_Y[I, (K, rs)] per spin
+        # class (D_zb is the forward pass's pair scatter of the same coefficients) ----
+        self.gamma_ri, self.gamma_old = [], []
+        Lg = GroupedGemm(dev, gprec)
+        for m in (0, 1):
+            for c in plan.H1blk[m]:
+                sg = plan.sigma[m][c]
+                if sg.pl is None:
+                    self.gamma_old.append((m, c))
+                    continue
+                Lc = sg.pl["L"]
+                Dy = torch.zeros_like(sg.D)
+                n = plan.n_states[m][c]
+                Nm = N[m]
+                parts = []
+                for k, cl in enumerate(sg.pl["classes"]):
+                    b, nK, npr = cl["base"], cl["n_K"], cl["n_p"]
+                    Gp = self.G[("Gpair", m, c, k)]
+                    Lg.add(npr, npr, [(sg.D.view(-1)[b:], npr, Dy.view(-1)[b:], npr, nK, 1.0, 3, Lc, Lc)], Gp, npr,
+                           mode=1, batch=n, sC=0)
+                    flat = torch.as_tensor(cl["u"] * Nm + cl["v"], device=dev)
+                    parts.append((Gp, flat[:, None], flat[None, :]))
+                self.gamma_ri.append((m, c, sg, Dy, parts))
+        self.Lgamma = Lg.finalize()
+
         self.dens_adj = []
         for m in (0, 1):
             b = plan.builders[m]
@@ -199,14 +229,20 @@ class XRDimerAdjoint:
             zb_, zk_ = ((bld.zbT32[bc], bld.zT32[kc]) if self.prec32 else (bld.zbT[bc], bld.zT[kc]))
             call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
                  ptr(cp.Q), ptr(cp.sign), ptr(zb_), nb, ptr(zk_), nk, ptr(gT), ptr(gb_), ptr(gk_), s)
-        for m in (0, 1):
+        for (m, c, sg, Dy, parts) in self.gamma_ri:
+            sg.scatter(self.G[("YT", m, c)], Dy)
+        self.Lgamma.run()
+        for (m, c, sg, Dy, parts) in self.gamma_ri:
+            G2 = self.G[("Gamma", m)].view(plan.N[m] ** 2, plan.N[m] ** 2)
+            for Gp, ri, ci in parts:
+                G2.index_put_((ri, ci), Gp, accumulate=True)
+        for (m, c) in self.gamma_old:
             sp = plan.spaces[m]
-            for c in plan.H1blk[m]:
-                call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
-                     sp.n_conf[c], ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c],
-                     ptr(sp.rank_table[c]), sp.table_size[c], ptr(sp.binom),
-                     ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]), plan.n_states[m][c],
-                     ptr(self.Gamma32[m] if self.prec32 else self.G[("Gamma", m)]), s)
+            call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
+                 sp.n_conf[c], ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c],
+                 ptr(sp.rank_table[c]), sp.table_size[c], ptr(sp.binom),
+                 ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]), plan.n_states[m][c],
+                 ptr(self.Gamma32[m] if self.prec32 else self.G[("Gamma", m)]), s)
 
     # ---------------------------------------------------------------------- results ---
     def state_gradient(self):
@@ -243,7 +279,8 @@ class XRDimerAdjoint:
             dT[sl[m], sl[m]] += g1
             dU[m][sl[m], sl[m]] += g1
             dU[o][sl[m], sl[m]] += g1
-            Gm = (self.Gamma32[m].to(torch.float64) if self.prec32 else G[("Gamma", m)]).view(Ns[m], Ns[m], Ns[m], Ns[m])
+            Gm = G[("Gamma", m)] + self.Gamma32[m].to(torch.float64) if self.prec32 else G[("Gamma", m)]
+            Gm = Gm.view(Ns[m], Ns[m], Ns[m], Ns[m])
             Gf = Gm - Gm.permute(1, 0, 2, 3) - Gm.permute(0, 1, 3, 2) + Gm.permute(1, 0, 3, 2)
             dV[sl[m], sl[m], sl[m], sl[m]] += Gf
         return dT, dU, dV

@@ -94,21 +94,80 @@ class DeviceIntegrals:
 
 
 class SigmaTwoElectron:
-    """E2[I,J] = sum_PQ zb[I,P] <P|V|Q> zk[J,Q] for one fragment and charge (v0000)."""
+    """E2[I,J] = sum_PQ zb[I,P] <P|V|Q> zk[J,Q] for one fragment and charge (v0000).
+
+    run_sigma(zT) fills sigmaT[J, P] = sum_Q <P| sum V_pqrs c+_p c+_q a_s a_r |Q> zk[J, Q].
+    With a spin-conserving V the space goes through (n-2)-electron intermediates (its pair list):
+    D = pair scatter of zk, E = D . W^T per spin class (one grouped GEMM, W = 4 V over pairs),
+    sigma = pair gather of E; D is kept for the two-particle density of the adjoint.  Otherwise
+    xrh_sigma2e (every double excitation of every determinant).  The adjoint's two-particle
+    density then holds the same-class blocks only: the entries between pairs of different
+    spin classes multiply integrals that vanish by spin symmetry."""
 
     def __init__(self, space, charge, n_states, V_block, precision=_lib.FP64):
         self.space, self.c, self.n = space, charge, n_states
         self.V = V_block.contiguous()
         self.precision = precision if precision in (_lib.FP64, _lib.FP32) else _lib.FP32
+        dev = space.device
         nconf = space.n_conf[charge]
-        self.sigmaT = torch.empty((n_states, nconf), dtype=torch.float64, device=space.device)
+        self.sigmaT = torch.empty((n_states, nconf), dtype=torch.float64, device=dev)
+        self.pl = space.pair_list(charge)
+        if self.pl is not None and not self._spin_conserving(space):
+            self.pl = None
+        if self.pl is not None:
+            pl = self.pl
+            L = pl["L"]
+            f64 = dict(dtype=torch.float64, device=dev)
+            self.D = torch.zeros((n_states, L), **f64)     # positions never written stay zero
+            self.E = torch.zeros((n_states, L), **f64)
+            self.W, self._uv = [], []
+            g = GroupedGemm(dev, precision="fp32" if self.precision == _lib.FP32 else "fp64")
+            Df, Ef = self.D.view(-1), self.E.view(-1)
+            for cl in pl["classes"]:
+                u = torch.as_tensor(cl["u"], device=dev)
+                v = torch.as_tensor(cl["v"], device=dev)
+                self._uv.append((u, v))
+                W = (4.0 * self.V[u[:, None], v[:, None], u[None, :], v[None, :]]).contiguous()
+                self.W.append(W)
+                b, nK, npr = cl["base"], cl["n_K"], cl["n_p"]
+                # E[s][(K, pq)] = sum_rs D[s][(K, rs)] W[pq, rs], batched over the states s
+                g.add(nK, npr, [(Df[b:], npr, W, npr, npr, 1.0, 0, L, 0)], Ef[b:], npr, mode=0, batch=n_states,
+                      sC=L)
+            self.gemm = g.finalize()
+
+    def set_V(self, V_block):
+        """New integrals in place (the launch tables keep their pointers)."""
+        self.V.copy_(V_block)
+        if self.pl is not None:
+            for W, (u, v) in zip(self.W, self._uv):
+                W.copy_(4.0 * self.V[u[:, None], v[:, None], u[None, :], v[None, :]])
+
+    def _spin_conserving(self, space):
+        """V couples only pairs with the same number of beta orbitals (checked once)."""
+        N, no = space.N, space.n_orbs
+        nb = (torch.arange(N, device=self.V.device) >= no).to(torch.int64)
+        cls = nb[:, None] + nb[None, :]
+        cross = cls[:, :, None, None] != cls[None, None, :, :]
+        return float(self.V.abs().masked_fill(~cross, 0.0).max()) == 0.0
+
+    def scatter(self, zT, D):
+        pl = self.pl
+        call("xrh_pair_scatter", len(pl["X"]), ptr(pl["X_dev"]), ptr(pl["off_dev"]), ptr(pl["sign_dev"]), ptr(zT),
+             self.n, pl["L"], ptr(D), stream_ptr())
 
     def run_sigma(self, zT):
         sp = self.space
         c = self.c
-        call("xrh_sigma2e", self.precision, sp.n_orbs, ptr(self.V), ptr(sp.masks[c]), sp.n_conf[c],
-             ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(sp.rank_table[c]),
-             sp.table_size[c], ptr(sp.binom), ptr(zT), self.n, ptr(self.sigmaT), stream_ptr())
+        if self.pl is None:
+            call("xrh_sigma2e", self.precision, sp.n_orbs, ptr(self.V), ptr(sp.masks[c]), sp.n_conf[c],
+                 ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(sp.rank_table[c]),
+                 sp.table_size[c], ptr(sp.binom), ptr(zT), self.n, ptr(self.sigmaT), stream_ptr())
+            return
+        pl = self.pl
+        self.scatter(zT, self.D)
+        self.gemm.run()
+        call("xrh_pair_gather", sp.n_conf[c], ptr(pl["xptr_dev"]), ptr(pl["off_dev"]), ptr(pl["sign_dev"]),
+             ptr(self.E), self.n, pl["L"], ptr(self.sigmaT), stream_ptr())
 
 
 def monomer_two_electron(space, coeffs, V_block, c):
@@ -291,6 +350,11 @@ class XRDimerPlan:
                 for tgt in targets_du:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))
+        # one-column terms (rho^ca . h) are row GEMVs: a 64 x 64 FP64 tile would spend 64x the
+        # FMAs of the result on them, and an FP64 tile is slow on this part
+        self.mono_gemv = [(sg_[0][0], sg_[0][2], out_, M_, sg_[0][4]) for (M_, N_, sg_, out_, _l, _s) in mono if N_ == 1]
+        mono = [t for t in mono if t[1] != 1]
+        self.mono_flops = sum(2.0 * M_ * K_ for (_a, _w, _o, M_, K_) in self.mono_gemv)
         for (M_, N_, segs_, out_, ldc_, sk_) in mono:
             pre.add(M_, N_, segs_, out_, ldc_, mode=1, splitk=sk_)
         self.pre = pre.finalize()
@@ -452,7 +516,7 @@ class XRDimerPlan:
             self.W[k].copy_(w)
         for m in (0, 1):
             for c, sg in self.sigma[m].items():
-                sg.V.copy_(ints.V(m, m, m, m))
+                sg.set_V(ints.V(m, m, m, m))
         if self.tc:
             self.reg.split("W")
         self.ints = ints
@@ -470,6 +534,9 @@ class XRDimerPlan:
             for c, sg in self.sigma[m].items():
                 sg.run_sigma(self.builders[m].zT[c])
         self.arena.buf.zero_()
+        s = stream_ptr()
+        for (A_, w_, out_, M_, K_) in self.mono_gemv:
+            call("xrh_gemv_rows", M_, K_, ptr(A_), K_, ptr(w_), 1.0, 1.0, ptr(out_), s)
         if self.tc:
             self.reg.split("in")
             self.pre_tc.run()
@@ -503,7 +570,7 @@ class XRDimerPlan:
 
     @property
     def flops(self):
-        return self.pre.flops + self.fin.flops
+        return self.pre.flops + self.fin.flops + self.mono_flops
 
     def check_status(self):
         """Raise if a bounded device wait of the tensor-core kernels timed out (syncs)."""
