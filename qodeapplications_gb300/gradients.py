@@ -21,7 +21,7 @@ import torch
 
 from . import _lib
 from ._lib import call, ptr, stream_ptr
-from .gemm import GroupedGemm
+from .gemm import GroupedGemm, SplitRegistry, TCGroupedGemm
 from .hamiltonian import _Arena, _splitk
 
 
@@ -145,20 +145,69 @@ class XRDimerAdjoint:
         self.L2 = L2.finalize()
 
         # ---- launch 3: precontraction adjoint ----
-        L3 = GroupedGemm(dev, gprec)
+        # every gradient buffer's writers: outputs written by this launch alone take plain stores
+        writers = {}
+        for (A, B, K, Y, Z, Dj, _dims) in self.final_adj:
+            for t_ in (A, B):
+                writers[t_.data_ptr()] = writers.get(t_.data_ptr(), 0) + 1
+        for m in (0, 1):
+            for c in plan.H1blk[m]:
+                p_ = plan.builders[m].rho["ca"][(c, c)].data_ptr()
+                writers[p_] = writers.get(p_, 0) + 1
         for out, segs in plan.pre_specs:
-            gP = grad_of[out.data_ptr()]
-            M, X = out.shape
             for rho_t, wk in segs:
-                Wt = plan.W[wk]
-                Yk = Wt.shape[1]
-                grho = grad_of[rho_t.data_ptr()]
-                # d rho[m, y] += sum_x dP[m, x] W[x, y]
-                L3.add(M, Yk, [(gP, X, Wt, Yk, X, 1.0, 2, 0, 0)], grho, Yk, mode=1)
-                # dW[x, y] += sum_m dP[m, x] rho[m, y]
-                L3.add(X, Yk, [(gP, X, rho_t, Yk, M, 1.0, 3, 0, 0)], G[("gW", wk)], Yk, mode=1,
-                       splitk=_splitk(M, 256, 32))
-        self.L3 = L3.finalize()
+                writers[rho_t.data_ptr()] = writers.get(rho_t.data_ptr(), 0) + 1
+        self.l3_tc = plan.tc
+        self.l3_T = []
+        if plan.tc:
+            # tensor cores (split precision, FP32 chunk sums): d rho = dP W on K-major W^T; dW = dP^T rho
+            # on rho^T, which the density build leaves in its pre-transpose buffer
+            rhoT_of = {}
+            for m in (0, 1):
+                b = plan.builders[m]
+                for (op, bc, kc), tmp in b._tmp.items():
+                    rt = b.rho[op][(bc, kc)]
+                    rhoT_of[rt.data_ptr()] = tmp.view(plan.spaces[m].couplings[(op, bc, kc)].K, -1)
+            pname = {v: k for k, v in _lib.PRECISIONS.items()}[plan.precision]
+            self.reg3 = SplitRegistry(pname, dev)
+            L3 = TCGroupedGemm(self.reg3)
+            WT, gPT = {}, {}
+            for out, segs in plan.pre_specs:
+                gP = grad_of[out.data_ptr()]
+                M, X = out.shape
+                if gP.data_ptr() not in gPT:
+                    gPT[gP.data_ptr()] = torch.empty((X, M), **f64)
+                    self.l3_T.append((gP, gPT[gP.data_ptr()]))
+                gpt = gPT[gP.data_ptr()]
+                for rho_t, wk in segs:
+                    Wt = plan.W[wk]
+                    Yk = Wt.shape[1]
+                    if wk not in WT:
+                        WT[wk] = torch.empty((Yk, X), **f64)
+                        self.l3_T.append((Wt, WT[wk]))
+                    grho = grad_of[rho_t.data_ptr()]
+                    mode = 0 if writers[rho_t.data_ptr()] == 1 else 1
+                    L3.add(M, Yk, [(gP, X, WT[wk], X, X, 1.0)], grho, Yk, mode=mode, groups=[("g", "g")])
+                    L3.add(X, Yk, [(gpt, M, rhoT_of[rho_t.data_ptr()], M, M, 1.0)], G[("gW", wk)], Yk, mode=1,
+                           groups=[("g", "rhoT")])
+            self.reg3.upload()
+            self.L3 = L3.finalize().autotune()
+        else:
+            L3 = GroupedGemm(dev, gprec)
+            for out, segs in plan.pre_specs:
+                gP = grad_of[out.data_ptr()]
+                M, X = out.shape
+                for rho_t, wk in segs:
+                    Wt = plan.W[wk]
+                    Yk = Wt.shape[1]
+                    grho = grad_of[rho_t.data_ptr()]
+                    # d rho[m, y] += sum_x dP[m, x] W[x, y]
+                    mode = 0 if writers[rho_t.data_ptr()] == 1 else 1
+                    L3.add(M, Yk, [(gP, X, Wt, Yk, X, 1.0, 2, 0, 0)], grho, Yk, mode=mode)
+                    # dW[x, y] += sum_m dP[m, x] rho[m, y]
+                    L3.add(X, Yk, [(gP, X, rho_t, Yk, M, 1.0, 3, 0, 0)], G[("gW", wk)], Yk, mode=1,
+                           splitk=_splitk(M, 256, 32))
+            self.L3 = L3.finalize()
 
         # ---- launch 4 inputs: transposed density gradients for the coupling-list adjoint ----
         # (FP32 accumulation buffers on the split-precision paths)
@@ -205,6 +254,20 @@ class XRDimerAdjoint:
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
 
     # ------------------------------------------------------------------------------------
+    def launch_L3(self):
+        """The precontraction adjoint (after launches 1 and 2)."""
+        if self.l3_tc:
+            for src, dst in self.l3_T:
+                dst.copy_(src.t())
+            self.reg3.split("g")
+            self.reg3.split("rhoT")
+        self.L3.run()
+
+    def check_status(self):
+        """Raise if a bounded device wait of the tensor-core launch timed out (syncs)."""
+        if self.l3_tc:
+            self.L3.check()
+
     def launch(self, d):
         """Enqueue the reverse pass for ground-state vector d (device, product order)."""
         plan = self.plan
@@ -219,7 +282,7 @@ class XRDimerAdjoint:
                 self.Gamma32[m].zero_()
         self.L1.run()
         self.L2.run()
-        self.L3.run()
+        self.launch_L3()
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)

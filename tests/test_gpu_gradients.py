@@ -129,6 +129,8 @@ def test_split_precision_gradients_close_to_fp64(prec):
                            precision=p)
         adj = XRDimerAdjoint(plan)
         E, d, _ = _gpu_energy_and_grad(plan, adj, coeffs)
+        plan.check_status()
+        adj.check_status()
         g = adj.state_gradient()
         gt = torch.cat([tangent_project(g[m][c], coeffs[m][c]).reshape(-1) for m in range(2) for c in CHG])
         T = torch.as_tensor(sysd["h"], device="cuda")
