@@ -218,6 +218,32 @@ int xrh_pair_gather(int n_X, const int64_t* xptr_dev, const int64_t* off_dev,
                     const int8_t* sign_dev, const double* E_dev, int n, int64_t L,
                     double* sigmaT_dev, void* stream);
 
+/* Transition densities through intermediate determinants K (no reference counterpart; they
+ * replace the per-coupling outer products of density_tensors.c:142-556 on the split-precision
+ * paths).  rho^op[I, J, cre, ann] = sum_K C[K, cre, I] A[K, ann, J] with C, A index scatters
+ * of the coefficients; X[(I, ci), (J, ai)] = sum_K Ct[(I, ci), K] At[(J, ai), K] is a GEMM.
+ *   xrh_im_scatter: for entries e (determinant x_e, index idx_e < nidx, intermediate k_e < nK,
+ *       sign_e) and states s < n:  v = sign_e zT[x_e * n + s];
+ *       Dt[(s * nidx + idx_e) * nK + k_e] = v  and, when D_dev is not NULL,
+ *       D[k_e * (n * nidx) + s * nidx + idx_e] = v.  Unwritten positions keep their value.
+ *   xrh_im_expand:  rho[(I * nk + J) * F + f] = sign_f X[(I * ncre + ci_f) * (nk * nann)
+ *       + J * nann + ai_f]  (0 where sign_f = 0).
+ *   xrh_im_fold:    gX[((I * ncre + c) * nk + J) * nann + a] = sum_{h < 2} sign[2 q + h]
+ *       grho[(I * nk + J) * F + src[2 q + h]],  q = c * nann + a  (sign 0: no source).
+ *   xrh_im_gather:  gzT[x * n + s] += sum_{e = ptr[x]}^{ptr[x+1]-1} sign_e
+ *       gDt[(s * nidx + idx_e) * nK + k_e]. */
+int xrh_im_scatter(int64_t n_entries, const int32_t* x_dev, const int32_t* idx_dev, const int32_t* k_dev,
+                   const int8_t* sign_dev, const double* zT_dev, int n, int64_t nK, int nidx,
+                   double* Dt_dev, double* D_dev, void* stream);
+int xrh_im_expand(int nb, int nk, int64_t F, const int32_t* ci_dev, const int32_t* ai_dev,
+                  const int8_t* sign_dev, int ncre, int nann, const double* X_dev, double* rho_dev,
+                  void* stream);
+int xrh_im_fold(int nb, int nk, int64_t F, int ncre, int nann, const int32_t* src_dev,
+                const int8_t* sign_dev, const double* grho_dev, double* gX_dev, void* stream);
+int xrh_im_gather(int n_x, const int64_t* ptr_dev, const int32_t* idx_dev, const int32_t* k_dev,
+                  const int8_t* sign_dev, int n, int64_t nK, int nidx, const double* gDt_dev,
+                  double* gzT_dev, void* stream);
+
 /* Two-particle density of a weighted ensemble for the monomer two-electron term:
  *   Gamma[p,q,r,s] += sum_{P,Q} W[P,Q] <P| c+_p c+_q a_s a_r |Q>,  p<q and r<s only,
  *   W[P,Q] = sum_I zbT[P, I] YT[Q, I]   (Y = G . z for weights G over state pairs)

@@ -87,7 +87,7 @@ class XRDimerAdjoint:
         self.grad_of = grad_of
 
         # the adjoint contractions run in FP32 (FP64 sums) on the split-precision paths
-        gprec = "fp32" if plan.dens_precision == "fp32" else "fp64"
+        gprec = "fp64" if plan.dens_precision == "fp64" else "fp32"
         # ---- launch 1: G blocks, Y and Z per final segment ----
         L1 = GroupedGemm(dev, gprec)
         for m in (0, 1):
@@ -244,8 +244,18 @@ class XRDimerAdjoint:
         self.Lgamma = Lg.finalize()
 
         self.dens_adj = []
+        self.im_adj = []          # intermediate-determinant builders: (builder, density gradients, gzT)
         for m in (0, 1):
             b = plan.builders[m]
+            if plan.dens_precision == "im":
+                grads = {}
+                for op, blocks in b.rho.items():
+                    for key, rt in blocks.items():
+                        if rt.data_ptr() in grad_of:
+                            grads[(op,) + key] = grad_of[rt.data_ptr()]
+                b.setup_adjoint()
+                self.im_adj.append((b, grads, {c: G[("gzT", m, c)] for c in plan.charges[m]}))
+                continue
             for (op, bc, kc), cp in plan.spaces[m].couplings.items():
                 rt = b.rho[op][(bc, kc)]
                 if rt.data_ptr() not in grad_of:
@@ -283,6 +293,8 @@ class XRDimerAdjoint:
         self.L1.run()
         self.L2.run()
         self.launch_L3()
+        for (b, grads, gz) in self.im_adj:
+            b.adjoint(grads, gz)
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)

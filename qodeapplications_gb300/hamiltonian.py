@@ -257,9 +257,22 @@ class XRDimerPlan:
         # densities and sigma vectors: FP64 on the fp64 path; FP32 products with FP64 sums on the
         # split-precision paths unless requested otherwise
         tc_mode = self.precision in (_lib.BF16X3, _lib.TF32X3)
+        # densities: coupling-list kernels with FP32 products on the split-precision paths;
+        # "im" builds them through intermediate determinants on the tensor cores instead (dense
+        # over the intermediates: at 2 x 14 orbitals / 60 states its GEMMs, scatters and operand
+        # splits cost about what the coupling lists do, so it is not the default)
         self.dens_precision = dens_precision or ("fp32" if tc_mode else "fp64")
         self.sigma_precision = sigma_precision or ("fp32" if tc_mode else "fp64")
-        self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=self.dens_precision) for m in (0, 1)]
+        if self.dens_precision == "im":
+            assert tc_mode, "the intermediate-determinant densities run on the split-precision paths"
+            from .intermediates import IntermediateDensityBuilder
+            # the density GEMMs multiply state coefficients: 3 x TF32 (22-bit products) keeps them
+            # near FP32 accuracy; 3 x BF16 (16-bit) would cost about 1e-5 relative per element
+            self.builders = [IntermediateDensityBuilder(spaces[m], self.n_states[m], precision="tf32x3",
+                                                        autotune=autotune) for m in (0, 1)]
+        else:
+            self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=self.dens_precision)
+                             for m in (0, 1)]
         N = [spaces[0].N, spaces[1].N]
         self.N = N
         rho = [b.rho for b in self.builders]
@@ -577,6 +590,9 @@ class XRDimerPlan:
         if self.tc:
             self.pre_tc.check()
             self.fin_tc.check()
+        for b in self.builders:
+            if hasattr(b, "check"):
+                b.check()
 
 
 def lowest_eigenpairs(H, k=5):

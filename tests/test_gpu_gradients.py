@@ -112,8 +112,8 @@ def test_orbital_gradient_matches_finite_differences():
         assert abs(fd - pred) <= 1e-6 * max(1.0, abs(fd)), (trial, fd, pred)
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
-def test_split_precision_gradients_close_to_fp64(prec):
+@pytest.mark.parametrize("prec,dens", [("bf16x3", "fp32"), ("tf32x3", "fp32"), ("bf16x3", "im")])
+def test_split_precision_gradients_close_to_fp64(prec, dens):
     """The split-precision adjoint (FP32 density adjoint, tensor-core build) against the FP64
     adjoint: relative error of the tangent state gradient and of dE/dkappa below 1e-5."""
     from qodeapplications_gb300.densities import FragmentSpace
@@ -126,7 +126,7 @@ def test_split_precision_gradients_close_to_fp64(prec):
     out = {}
     for p in ("fp64", prec):
         plan = XRDimerPlan(spaces, ns, [list(CHG)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
-                           precision=p)
+                           precision=p, dens_precision=None if p == "fp64" else dens)
         adj = XRDimerAdjoint(plan)
         E, d, _ = _gpu_energy_and_grad(plan, adj, coeffs)
         plan.check_status()
@@ -139,3 +139,34 @@ def test_split_precision_gradients_close_to_fp64(prec):
         out[p] = (gt, kg)
     for a, b in zip(out[prec], out["fp64"]):
         assert float((a - b).norm() / b.norm()) < 1e-5
+
+
+def test_adjoint_built_after_the_build_matches_adjoint_built_before():
+    """The reverse pass may be set up after a build (the intermediate-determinant density
+    route splits its adjoint GEMM operands in every build from the plan's construction on):
+    same gradient either way."""
+    from qodeapplications_gb300.densities import FragmentSpace
+    from qodeapplications_gb300.gradients import XRDimerAdjoint
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+    from qodeapplications_gb300.eigen import Lanczos
+    sysd = S.make_system(n_frag=2, n_orb=4, n_states=3, charges=CHG, seed=33)
+    spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in CHG}, 4, 0, 4) for m in range(2)]
+    ns = [{c: 3 for c in CHG}] * 2
+    coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in CHG} for m in range(2)]
+    out = []
+    for adj_first in (True, False):
+        plan = XRDimerPlan(spaces, ns, [list(CHG)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
+                           precision="bf16x3", dens_precision="im")
+        adj = XRDimerAdjoint(plan) if adj_first else None
+        H = plan.build(coeffs)
+        lz = Lanczos(H.shape[0], m=min(120, H.shape[0]))
+        lz.krylov(H)
+        lz.stage_to_host()
+        torch.cuda.synchronize()
+        lz.solve(1)
+        d = lz.ground_vector().clone()
+        adj = adj or XRDimerAdjoint(plan)
+        adj.launch(d)
+        g = adj.state_gradient()
+        out.append(torch.cat([g[m][c].reshape(-1) for m in range(2) for c in CHG]).clone())
+    assert float((out[0] - out[1]).abs().max()) <= 1e-12 * float(out[0].abs().max())

@@ -166,3 +166,33 @@ def test_build_is_repeatable_and_tracks_new_states():
     H_b = plan.build(coeffs2).cpu().numpy()
     np.testing.assert_allclose(H_b, O.full_H(H1, H2), rtol=0, atol=1e-12)
     assert np.abs(H_a - H_b).max() > 1e-3
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_intermediate_densities_match_coupling_lists(prec):
+    """Densities through intermediate determinants on the tensor cores (split precision)
+    against the FP64 coupling-list build, every operator string and charge pair, frozen core
+    included.  Tolerance of the largest element: 2e-6 for 3 x TF32 (22-bit split products,
+    FP32 chunk sums; the route the plans use), 5e-5 for 3 x BF16 (16-bit split products)."""
+    from qodeapplications_gb300.densities import DensityBuilder, FragmentSpace
+    from qodeapplications_gb300.intermediates import IntermediateDensityBuilder
+    chg = (+1, 0, -1)
+    sysd = S.make_system(n_frag=1, n_orb=5, n_states=4, charges=chg, n_core=1, seed=17)
+    st = sysd["states"][0]
+    sp = FragmentSpace({c: st[c][1] for c in chg}, 5, 1, 4)
+    ns = {c: 4 for c in chg}
+    coeffs = {c: torch.as_tensor(st[c][0], device="cuda") for c in chg}
+    ref = DensityBuilder(sp, ns).build(coeffs)
+    im = IntermediateDensityBuilder(sp, ns, precision=prec)
+    got = im.build(coeffs)
+    torch.cuda.synchronize()
+    im.check()
+    n = 0
+    for op, blocks in ref.items():
+        for key, r in blocks.items():
+            g = got[op][key]
+            scale = max(float(r.abs().max()), 1e-30)
+            tol = 2e-6 if prec == "tf32x3" else 5e-5
+            assert float((g - r).abs().max()) <= tol * scale, (op, key, float((g - r).abs().max()) / scale)
+            n += 1
+    assert n == 13          # 3 ca, 4 a/caa, 4 c/cca, 1 aa, 1 cc over charges (+1, 0, -1)
