@@ -203,19 +203,19 @@ int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev,
 /* Two-electron terms through (n-2)-electron intermediates K (no reference counterpart: the
  * reference builds rho^ccaa element by element, density_tensors.c:493-556, and contracts it,
  * H_contractions.c:61-78).  A pair list holds, for every determinant X of a space and every
- * occupied pair u < v, the sign of <K| a_v a_u |X> and the flat position off of (K, pair)
- * inside a row of L doubles (pairs and K grouped by spin class, class blocks concatenated).
- *   xrh_pair_scatter:  D[s * L + off_e] = sign_e * zT[X_e * n + s]  for s < n
+ * occupied pair u < v, the sign of <K| a_v a_u |X> and the position of (K, pair) in a
+ * class-major array [spin class][state][K][pair]: off_e for state 0 and stride_e per state.
+ *   xrh_pair_scatter:  D[off_e + s * stride_e] = sign_e * zT[X_e * n + s]  for s < n
  *   xrh_pair_gather:   sigmaT[s * n_X + x] = sum over x's entries e (xptr[x] .. xptr[x+1])
- *                      of sign_e * E[s * L + off_e]
+ *                      of sign_e * E[off_e + s * stride_e]
  * With E = D . W^T per class (W[pq, rs] = 4 V_pqrs), gather gives xrh_sigma2e's sigmaT, and
- * sum_s D_zb[s]^T D_Y[s] per class gives xrh_ccaa_weighted's Gamma for p<q, r<s.  Positions
- * of D never written stay as the caller initialised them (zero). */
+ * D_zb^T D_Y per class gives xrh_ccaa_weighted's Gamma for p<q, r<s.  Positions of D never
+ * written stay as the caller initialised them (zero). */
 int xrh_pair_scatter(int64_t n_entries, const int32_t* X_dev, const int64_t* off_dev,
-                     const int8_t* sign_dev, const double* zT_dev, int n, int64_t L,
+                     const int8_t* sign_dev, const double* zT_dev, int n, const int64_t* stride_dev,
                      double* D_dev, void* stream);
 int xrh_pair_gather(int n_X, const int64_t* xptr_dev, const int64_t* off_dev,
-                    const int8_t* sign_dev, const double* E_dev, int n, int64_t L,
+                    const int8_t* sign_dev, const double* E_dev, int n, const int64_t* stride_dev,
                     double* sigmaT_dev, void* stream);
 
 /* Transition densities through intermediate determinants K (no reference counterpart; they

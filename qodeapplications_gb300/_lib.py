@@ -24,12 +24,12 @@ _i32, _i64, _vp, _dbl = ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes
 
 _SIGS = {
     "xrh_abi_version": (_i32, []),
-    "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _i64, _vp, _vp]),
+    "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_im_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),
     "xrh_im_expand": (_i32, [_i32, _i32, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     "xrh_im_fold": (_i32, [_i32, _i32, _i64, _i32, _i32, _vp, _vp, _vp, _vp, _vp]),
     "xrh_im_gather": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),
-    "xrh_pair_gather": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _i64, _vp, _vp]),
+    "xrh_pair_gather": (_i32, [_i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_status_string": (ctypes.c_char_p, [_i32]),
     "xrh_last_cuda_error": (_i32, []),
     "xrh_couplings_count": (_i32, [_i32, _i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _vp]),

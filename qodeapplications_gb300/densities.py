@@ -110,7 +110,7 @@ class FragmentSpace:
         if c not in self._pairs:
             pl = build_pair_list(self.masks_np[c], self.n_orbs)
             if pl is not None:
-                for k in ("X", "off", "sign", "xptr"):
+                for k in ("X", "sign", "xptr"):
                     pl[k + "_dev"] = torch.from_numpy(pl[k]).to(self.device)
             self._pairs[c] = pl
         return self._pairs[c]
@@ -186,6 +186,7 @@ def build_pair_list(masks, n_orbs):
     par = (_popcount64(mX >> (u + 1).astype(np.uint64)) + _popcount64(mX >> (v + 1).astype(np.uint64))) & 1
     cls = (u >= n_orbs).astype(np.int64) + (v >= n_orbs).astype(np.int64)
     off = np.zeros(len(X), dtype=np.int64)
+    ent_cls, ent_k, ent_p = np.zeros(len(X), dtype=np.int64), np.zeros(len(X), dtype=np.int64), np.zeros(len(X), dtype=np.int64)
     classes = []
     base = 0
     for c in range(3):
@@ -197,10 +198,22 @@ def build_pair_list(masks, n_orbs):
         Ks, kidx = np.unique(K[sel], return_inverse=True)
         n_p, n_k = len(pairs), len(Ks)
         off[sel] = base + kidx * n_p + pidx
+        ent_cls[sel], ent_k[sel], ent_p[sel] = len(classes), kidx, pidx
         classes.append(dict(base=base, n_K=n_k, n_p=n_p, u=pairs // N, v=pairs % N))
         base += n_k * n_p
     return dict(X=X.astype(np.int32), off=off, sign=np.where(par == 1, -1, 1).astype(np.int8),
-                xptr=np.arange(n_conf + 1, dtype=np.int64) * len(iu), L=base, classes=classes, n_conf=n_conf)
+                xptr=np.arange(n_conf + 1, dtype=np.int64) * len(iu), L=base, classes=classes, n_conf=n_conf,
+                cls=ent_cls, k=ent_k, p=ent_p)
+
+
+def pair_offsets(pl, n):
+    """Per-entry position (state 0) and state stride of a pair list in the class-major array
+    [class][state][K][pair] for n states."""
+    base = np.array([n * cl["base"] for cl in pl["classes"]], dtype=np.int64)
+    n_p = np.array([cl["n_p"] for cl in pl["classes"]], dtype=np.int64)
+    stride = np.array([cl["n_K"] * cl["n_p"] for cl in pl["classes"]], dtype=np.int64)
+    c = pl["cls"]
+    return base[c] + pl["k"] * n_p[c] + pl["p"], stride[c]
 
 
 class DensityBuilder:

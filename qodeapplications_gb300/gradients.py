@@ -221,27 +221,42 @@ class XRDimerAdjoint:
         # intermediates: Gamma[pq, rs] = sum_(I, K) D_zb[I, (K, pq)] D_Y[I, (K, rs)] per spin
         # class (D_zb is the forward pass's pair scatter of the same coefficients) ----
         self.gamma_ri, self.gamma_old = [], []
-        Lg = GroupedGemm(dev, gprec)
+        Lg = GroupedGemm(dev, "fp64")
+        self.gam_reg = SplitRegistry("tf32x3", dev)
+        Lgt = TCGroupedGemm(self.gam_reg)
+        self.gam_T = []
         for m in (0, 1):
             for c in plan.H1blk[m]:
                 sg = plan.sigma[m][c]
                 if sg.pl is None:
                     self.gamma_old.append((m, c))
                     continue
-                Lc = sg.pl["L"]
                 Dy = torch.zeros_like(sg.D)
                 n = plan.n_states[m][c]
                 Nm = N[m]
                 parts = []
                 for k, cl in enumerate(sg.pl["classes"]):
-                    b, nK, npr = cl["base"], cl["n_K"], cl["n_p"]
+                    nK, npr = cl["n_K"], cl["n_p"]
+                    b = n * cl["base"]
+                    Dyc = Dy[b:b + n * nK * npr].view(n * nK, npr)
                     Gp = self.G[("Gpair", m, c, k)]
-                    Lg.add(npr, npr, [(sg.D.view(-1)[b:], npr, Dy.view(-1)[b:], npr, nK, 1.0, 3, Lc, Lc)], Gp, npr,
-                           mode=1, batch=n, sC=0)
+                    if sg.tc:
+                        # Gamma_c = D^T Dy on the tensor cores, from K-major transposed copies
+                        DT = torch.empty((npr, n * nK), **f64)
+                        DyT = torch.empty((npr, n * nK), **f64)
+                        self.gam_T += [(sg.Dc[k], DT), (Dyc, DyT)]
+                        # (n states x n_K intermediates is a long K: split-K, atomic FP64 sums)
+                        Lgt.add(npr, npr, [(DT, n * nK, DyT, n * nK, n * nK, 1.0)], Gp, npr, mode=1,
+                                groups=[("gam", "gam")])
+                    else:
+                        Lg.add(npr, npr, [(sg.Dc[k], npr, Dyc, npr, n * nK, 1.0, 3, 0, 0)], Gp, npr, mode=1,
+                               splitk=_splitk(n * nK, 256, 64))
                     flat = torch.as_tensor(cl["u"] * Nm + cl["v"], device=dev)
                     parts.append((Gp, flat[:, None], flat[None, :]))
                 self.gamma_ri.append((m, c, sg, Dy, parts))
         self.Lgamma = Lg.finalize()
+        self.gam_reg.upload()
+        self.Lgamma_tc = Lgt.finalize().autotune()
 
         self.dens_adj = []
         self.im_adj = []          # intermediate-determinant builders: (builder, density gradients, gzT)
@@ -273,10 +288,36 @@ class XRDimerAdjoint:
             self.reg3.split("rhoT")
         self.L3.run()
 
+    def launch_gamma(self):
+        """Two-particle densities of the monomer two-electron terms (after launch 2)."""
+        plan = self.plan
+        s = stream_ptr()
+        for (m, c, sg, Dy, parts) in self.gamma_ri:
+            sg.scatter(self.G[("YT", m, c)], Dy)
+        for src, dst in self.gam_T:
+            dst.copy_(src.t())
+        if self.gam_T:
+            self.gam_reg.split("gam")
+        self.Lgamma.run()
+        self.Lgamma_tc.run()
+        for (m, c, sg, Dy, parts) in self.gamma_ri:
+            G2 = self.G[("Gamma", m)].view(plan.N[m] ** 2, plan.N[m] ** 2)
+            for Gp, ri, ci in parts:
+                # positions are distinct within a class: gather, add, scatter (no sort)
+                G2[ri, ci] = G2[ri, ci] + Gp
+        for (m, c) in self.gamma_old:
+            sp = plan.spaces[m]
+            call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
+                 sp.n_conf[c], ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c],
+                 ptr(sp.rank_table[c]), sp.table_size[c], ptr(sp.binom),
+                 ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]), plan.n_states[m][c],
+                 ptr(self.Gamma32[m] if self.prec32 else self.G[("Gamma", m)]), s)
+
     def check_status(self):
         """Raise if a bounded device wait of the tensor-core launch timed out (syncs)."""
         if self.l3_tc:
             self.L3.check()
+        self.Lgamma_tc.check()
 
     def launch(self, d):
         """Enqueue the reverse pass for ground-state vector d (device, product order)."""
@@ -304,20 +345,8 @@ class XRDimerAdjoint:
             zb_, zk_ = ((bld.zbT32[bc], bld.zT32[kc]) if self.prec32 else (bld.zbT[bc], bld.zT[kc]))
             call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
                  ptr(cp.Q), ptr(cp.sign), ptr(zb_), nb, ptr(zk_), nk, ptr(gT), ptr(gb_), ptr(gk_), s)
-        for (m, c, sg, Dy, parts) in self.gamma_ri:
-            sg.scatter(self.G[("YT", m, c)], Dy)
-        self.Lgamma.run()
-        for (m, c, sg, Dy, parts) in self.gamma_ri:
-            G2 = self.G[("Gamma", m)].view(plan.N[m] ** 2, plan.N[m] ** 2)
-            for Gp, ri, ci in parts:
-                G2.index_put_((ri, ci), Gp, accumulate=True)
-        for (m, c) in self.gamma_old:
-            sp = plan.spaces[m]
-            call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
-                 sp.n_conf[c], ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c],
-                 ptr(sp.rank_table[c]), sp.table_size[c], ptr(sp.binom),
-                 ptr(plan.builders[m].zbT[c]), ptr(self.G[("YT", m, c)]), plan.n_states[m][c],
-                 ptr(self.Gamma32[m] if self.prec32 else self.G[("Gamma", m)]), s)
+        self.launch_gamma()
+
 
     # ---------------------------------------------------------------------- results ---
     def state_gradient(self):

@@ -114,26 +114,49 @@ class SigmaTwoElectron:
         self.pl = space.pair_list(charge)
         if self.pl is not None and not self._spin_conserving(space):
             self.pl = None
+        self.tc = False
         if self.pl is not None:
+            from .densities import pair_offsets
             pl = self.pl
-            L = pl["L"]
+            n = n_states
+            off, stride = pair_offsets(pl, n)
+            self.off_dev = torch.from_numpy(off).to(dev)
+            self.stride_dev = torch.from_numpy(stride).to(dev)
             f64 = dict(dtype=torch.float64, device=dev)
-            self.D = torch.zeros((n_states, L), **f64)     # positions never written stay zero
-            self.E = torch.zeros((n_states, L), **f64)
-            self.W, self._uv = [], []
-            g = GroupedGemm(dev, precision="fp32" if self.precision == _lib.FP32 else "fp64")
-            Df, Ef = self.D.view(-1), self.E.view(-1)
+            # class-major [class][state][K][pair]; positions never written stay zero
+            self.D = torch.zeros(n * pl["L"], **f64)
+            self.E = torch.zeros(n * pl["L"], **f64)
+            self.W, self._uv, self.Dc, self.Ec = [], [], [], []
+            # split-precision plans: 3 x TF32 on the tensor cores (sigma feeds the monomer
+            # energies, the largest entries of H); FP64 plans: the FP64 grouped GEMM
+            self.tc = self.precision == _lib.FP32
+            if self.tc:
+                self.reg = SplitRegistry("tf32x3", dev)
+                g = TCGroupedGemm(self.reg)
+            else:
+                g = GroupedGemm(dev, precision="fp64")
             for cl in pl["classes"]:
                 u = torch.as_tensor(cl["u"], device=dev)
                 v = torch.as_tensor(cl["v"], device=dev)
                 self._uv.append((u, v))
                 W = (4.0 * self.V[u[:, None], v[:, None], u[None, :], v[None, :]]).contiguous()
                 self.W.append(W)
-                b, nK, npr = cl["base"], cl["n_K"], cl["n_p"]
-                # E[s][(K, pq)] = sum_rs D[s][(K, rs)] W[pq, rs], batched over the states s
-                g.add(nK, npr, [(Df[b:], npr, W, npr, npr, 1.0, 0, L, 0)], Ef[b:], npr, mode=0, batch=n_states,
-                      sC=L)
-            self.gemm = g.finalize()
+                b, nK, npr = n * cl["base"], cl["n_K"], cl["n_p"]
+                Dc = self.D[b:b + n * nK * npr].view(n * nK, npr)
+                Ec = self.E[b:b + n * nK * npr].view(n * nK, npr)
+                self.Dc.append(Dc)
+                self.Ec.append(Ec)
+                # E[c][(s, K)][pq] = sum_rs D[c][(s, K)][rs] W_c[pq, rs]
+                if self.tc:
+                    g.add(n * nK, npr, [(Dc, npr, W, npr, npr, 1.0)], Ec, npr, mode=0, groups=[("sig", "sigW")])
+                else:
+                    g.add(n * nK, npr, [(Dc, npr, W, npr, npr, 1.0)], Ec, npr, mode=0)
+            if self.tc:
+                self.reg.upload()
+                self.reg.split("sigW")
+                self.gemm = g.finalize().autotune()
+            else:
+                self.gemm = g.finalize()
 
     def set_V(self, V_block):
         """New integrals in place (the launch tables keep their pointers)."""
@@ -141,6 +164,8 @@ class SigmaTwoElectron:
         if self.pl is not None:
             for W, (u, v) in zip(self.W, self._uv):
                 W.copy_(4.0 * self.V[u[:, None], v[:, None], u[None, :], v[None, :]])
+            if self.tc:
+                self.reg.split("sigW")
 
     def _spin_conserving(self, space):
         """V couples only pairs with the same number of beta orbitals (checked once)."""
@@ -152,8 +177,8 @@ class SigmaTwoElectron:
 
     def scatter(self, zT, D):
         pl = self.pl
-        call("xrh_pair_scatter", len(pl["X"]), ptr(pl["X_dev"]), ptr(pl["off_dev"]), ptr(pl["sign_dev"]), ptr(zT),
-             self.n, pl["L"], ptr(D), stream_ptr())
+        call("xrh_pair_scatter", len(pl["X"]), ptr(pl["X_dev"]), ptr(self.off_dev), ptr(pl["sign_dev"]), ptr(zT),
+             self.n, ptr(self.stride_dev), ptr(D), stream_ptr())
 
     def run_sigma(self, zT):
         sp = self.space
@@ -165,9 +190,11 @@ class SigmaTwoElectron:
             return
         pl = self.pl
         self.scatter(zT, self.D)
+        if self.tc:
+            self.reg.split("sig")
         self.gemm.run()
-        call("xrh_pair_gather", sp.n_conf[c], ptr(pl["xptr_dev"]), ptr(pl["off_dev"]), ptr(pl["sign_dev"]),
-             ptr(self.E), self.n, pl["L"], ptr(self.sigmaT), stream_ptr())
+        call("xrh_pair_gather", sp.n_conf[c], ptr(pl["xptr_dev"]), ptr(self.off_dev), ptr(pl["sign_dev"]),
+             ptr(self.E), self.n, ptr(self.stride_dev), ptr(self.sigmaT), stream_ptr())
 
 
 def monomer_two_electron(space, coeffs, V_block, c):
@@ -593,6 +620,10 @@ class XRDimerPlan:
         for b in self.builders:
             if hasattr(b, "check"):
                 b.check()
+        for m in (0, 1):
+            for sg in self.sigma[m].values():
+                if sg.tc:
+                    sg.gemm.check()
 
 
 def lowest_eigenpairs(H, k=5):

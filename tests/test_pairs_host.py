@@ -20,8 +20,11 @@ def test_pair_list_reproduces_two_electron_operator(n_orb, n_elec, sz2):
     pl = build_pair_list(masks, n_orb)
     assert pl is not None
     n = len(masks)
+    from qodeapplications_gb300.densities import pair_offsets
+    off, stride = pair_offsets(pl, 1)                   # one state: the class-major offsets
+    np.testing.assert_array_equal(off, pl["off"])
     D = np.zeros((n, pl["L"]))
-    D[pl["X"], pl["off"]] = pl["sign"]
+    D[pl["X"], off] = pl["sign"]
     assert len(np.unique(pl["off"] + pl["X"].astype(np.int64) * pl["L"])) == len(pl["off"])   # no collisions
     M2 = np.zeros((n, n))
     for cl in pl["classes"]:
