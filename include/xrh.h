@@ -86,6 +86,27 @@ int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* idx_ptr_dev
                                const int32_t* Q_dev, const int8_t* sign_dev, const float* zb32_dev, int n_b,
                                const float* zk32_dev, int n_k, double* rhoT_dev, void* stream);
 
+/* Every density block of a fragment in one launch (same product as
+ * xrh_density_accumulate_f32 per block).  tasks_dev: n_tasks entries sorted by cta_begin,
+ * task t owning CTAs [cta_begin, cta_begin + K * splits); total_ctas = sum of K * splits;
+ * max_nb / max_nk bound the tasks' state counts (shared-memory size).  rhoT of a task with
+ * splits > 1 must be zeroed by the caller. */
+typedef struct {
+    const int64_t* idx_ptr;
+    const int32_t* P;
+    const int32_t* Q;
+    const int8_t* sign;
+    const float* zb32;
+    const float* zk32;
+    double* rhoT;
+    int64_t K;
+    int32_t nb, nk;
+    int32_t splits, reserved;
+    int64_t cta_begin;
+} xrh_dens_task;   /* 88 bytes */
+int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                                       int max_nb, int max_nk, void* stream);
+
 /* Allocation-free transition densities (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- for example code running
  * inside another application's CUDA context whose allocator owns all device memory, or a
@@ -186,6 +207,13 @@ int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, 
 int xrh_gemv_cols(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* c_dev,
                   double scale, double* y_dev, void* stream);
 int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double* beta_dev, void* stream);
+/* The whole Krylov loop of a small sector (n <= 4096) in one launch (one CTA): V[0] = v0,
+ * then for j < m: w = H V[j]; two classical Gram-Schmidt passes against V[0..j];
+ * alpha[j] = the two passes' coefficients of V[j] summed; beta[j] = |w|;
+ * V[j+1] = w / beta[j] (0 when beta[j] = 0).  V is (m+1) x n.  Same arithmetic as
+ * xrh_gemv_rows / xrh_gemv_cols / xrh_lanczos_normalize step by step. */
+int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                      double* V_dev, double* alpha_dev, double* beta_dev, void* stream);
 
 /* Adjoint of the density build (dE/dz from dE/drho), the reverse of xrh_density_accumulate
  * over the same coupling lists; replaces the determinant-bra density rebuild plus second H
@@ -199,6 +227,27 @@ int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev,
                         const int32_t* P_dev, const int32_t* Q_dev, const int8_t* sign_dev,
                         const void* zbT_dev, int n_b, const void* zkT_dev, int n_k,
                         const double* gT_dev, void* gzbT_dev, void* gzkT_dev, void* stream);
+
+/* xrh_density_adjoint (XRH_FP32) for every density block of a fragment in one launch:
+ * task t owns CTAs [cta_begin, cta_begin + K) (one per operator index), gT its transposed
+ * density gradient [K, nb, nk], gzb / gzk the FP32 gradient rows of its bra / ket charge
+ * (several tasks may share them: vector atomics). */
+typedef struct {
+    const int64_t* idx_ptr;
+    const int32_t* P;
+    const int32_t* Q;
+    const int8_t* sign;
+    const float* zb32;
+    const float* zk32;
+    const double* gT;
+    float* gzb;
+    float* gzk;
+    int64_t K;
+    int32_t nb, nk;
+    int64_t cta_begin;
+} xrh_dens_adj_task;   /* 96 bytes */
+int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                                    int max_nb, int max_nk, void* stream);
 
 /* Two-electron terms through (n-2)-electron intermediates K (no reference counterpart: the
  * reference builds rho^ccaa element by element, density_tensors.c:493-556, and contracts it,

@@ -24,6 +24,9 @@ _i32, _i64, _vp, _dbl = ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes
 
 _SIGS = {
     "xrh_abi_version": (_i32, []),
+    "xrh_density_accumulate_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
+    "xrh_density_adjoint_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
+    "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_im_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),
     "xrh_im_expand": (_i32, [_i32, _i32, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
@@ -126,6 +129,16 @@ def op_code(op):
 SEGMENT_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("lda", np.int64), ("ldb", np.int64),
                           ("K", np.int64), ("alpha", np.float64), ("flags", np.int64), ("sA", np.int64),
                           ("sB", np.int64)])
+DENS_ADJ_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.uint64), ("sign", np.uint64),
+                                ("zb32", np.uint64), ("zk32", np.uint64), ("gT", np.uint64), ("gzb", np.uint64),
+                                ("gzk", np.uint64), ("K", np.int64), ("nb", np.int32), ("nk", np.int32),
+                                ("cta_begin", np.int64)])
+assert DENS_ADJ_TASK_DTYPE.itemsize == 96
+DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.uint64), ("sign", np.uint64),
+                            ("zb32", np.uint64), ("zk32", np.uint64), ("rhoT", np.uint64), ("K", np.int64),
+                            ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
+                            ("cta_begin", np.int64)])
+assert DENS_TASK_DTYPE.itemsize == 88
 TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
                        ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("C", np.uint64),
                        ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64), ("rowB", np.uint64),

@@ -90,14 +90,13 @@ __device__ __forceinline__ void atomic_add4(float* dst, const float (&v)[4], int
     }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
-    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+__device__ __forceinline__ void density_adjoint_f32_body(
+    int64_t idx, const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
-    const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT) {
+    const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT, unsigned char* smem_raw) {
     // coefficient rows come pre-converted to FP32 and padded to nbp/nkp (16-byte rows), so the
     // z rows of a chunk are gathered with cp.async into a double-buffered ring while the
     // previous chunk is multiplied
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
     float* g = reinterpret_cast<float*>(smem_raw);          // [nbp][nkp]
     float* gt = g + nbp * nkp;                              // [nkp][nbp]
@@ -105,7 +104,6 @@ __global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
     float* zk_s = zb_s + 2 * kAdjChunk * nbp;               // [2][chunk][nkp]
     __shared__ int sP[2][kAdjChunk], sQ[2][kAdjChunk];
     __shared__ float sS[2][kAdjChunk];
-    const int64_t idx = blockIdx.x;
     const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
     if (c_begin == c_end) return;
     const double* gi = gT + idx * (int64_t)nb * nk;
@@ -214,6 +212,29 @@ __global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
     }
 }
 
+__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
+    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+    const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
+    const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    density_adjoint_f32_body(blockIdx.x, idx_ptr, P, Q, sgn, zb32, nb, zk32, nk, gT, gzbT, gzkT, smem_raw);
+}
+
+// Every block of a task table in one launch (one CTA per operator index).
+__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_grouped_kernel(
+    const xrh_dens_adj_task* __restrict__ tasks, int n_tasks) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    int lo = 0, hi = n_tasks - 1;
+    const int64_t cta = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const xrh_dens_adj_task& T = tasks[lo];
+    density_adjoint_f32_body(cta - T.cta_begin, T.idx_ptr, T.P, T.Q, T.sign, T.zb32, T.nb, T.zk32, T.nk, T.gT, T.gzb,
+                             T.gzk, smem_raw);
+}
+
 constexpr int kWThreads = 128;
 
 template <typename T>
@@ -282,6 +303,24 @@ __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
 }
 
 }  // namespace
+
+extern "C" int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                                               int max_nb, int max_nk, void* stream) {
+    if (n_tasks < 0 || total_ctas < 0 || max_nb <= 0 || max_nk <= 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    const int nbp = (max_nb + 3) & ~3, nkp = (max_nk + 3) & ~3;
+    const size_t smem = sizeof(float) * (2 * (size_t)nbp * nkp + 2 * (size_t)kAdjChunk * (nbp + nkp));
+    if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(density_adjoint_f32_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    density_adjoint_f32_grouped_kernel<<<(unsigned)total_ctas, kAdjThreads, smem, (cudaStream_t)stream>>>(tasks_dev,
+                                                                                                         n_tasks);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
 
 extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_ptr_dev, const int32_t* P_dev,
                                    const int32_t* Q_dev, const int8_t* sign_dev, const void* zbT_dev, int n_b,

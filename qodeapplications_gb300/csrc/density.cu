@@ -324,21 +324,22 @@ namespace {
 
 constexpr int kF32Chunk = 64;
 
-__global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
-    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
-    const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
-    double* __restrict__ rhoT, int splits) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+// One operator index (and one split of its couplings) per CTA: a 4 x 4 register tile of the
+// n_b x n_k block per thread over a double-buffered ring of gathered coefficient rows.
+__device__ __forceinline__ void density_f32_body(int64_t idx, int split, const int64_t* __restrict__ idx_ptr,
+                                                 const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+                                                 const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb,
+                                                 const float* __restrict__ zk32, int nk, double* __restrict__ rhoT,
+                                                 int splits, unsigned char* smem_raw) {
     const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
     float* zb_s = reinterpret_cast<float*>(smem_raw);               // [2][chunk][nbp]
     float* zk_s = zb_s + 2 * kF32Chunk * nbp;                        // [2][chunk][nkp]
     __shared__ int sP[2][kF32Chunk], sQ[2][kF32Chunk];
     __shared__ float sS[2][kF32Chunk];
-    const int64_t idx = blockIdx.x;
     const int64_t cb0 = idx_ptr[idx], ce0 = idx_ptr[idx + 1];
     const int64_t len = ce0 - cb0;
     const int64_t per = (len + splits - 1) / splits;
-    const int64_t c_begin = cb0 + blockIdx.y * per;
+    const int64_t c_begin = cb0 + split * per;
     const int64_t c_end = (c_begin + per < ce0) ? c_begin + per : ce0;
     double* out = rhoT + idx * (int64_t)nb * nk;
     const int tiles_j = nkp / 4, n_tiles = (nbp / 4) * tiles_j;
@@ -349,7 +350,6 @@ __global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
     }
     const int n_chunks = (int)((c_end - c_begin + kF32Chunk - 1) / kF32Chunk);
     const int gb = nbp / 4, gk = nkp / 4;       // 16-byte granules per row
-
     auto load_idx = [&](int k, int buf) {
         const int64_t c0 = c_begin + (int64_t)k * kF32Chunk;
         for (int t = threadIdx.x; t < kF32Chunk; t += blockDim.x) {
@@ -439,7 +439,47 @@ __global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
     }
 }
 
+__global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
+    const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
+    const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
+    double* __restrict__ rhoT, int splits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    density_f32_body(blockIdx.x, blockIdx.y, idx_ptr, P, Q, sgn, zb32, nb, zk32, nk, rhoT, splits, smem_raw);
+}
+
+// Every block of a task table in one launch: CTA -> task by binary search on cta_begin.
+__global__ void __launch_bounds__(kAccThreads) density_acc_f32_grouped_kernel(const xrh_dens_task* __restrict__ tasks,
+                                                                              int n_tasks) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    int lo = 0, hi = n_tasks - 1;
+    const int64_t cta = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const xrh_dens_task& T = tasks[lo];
+    const int64_t local = cta - T.cta_begin;
+    density_f32_body(local / T.splits, (int)(local % T.splits), T.idx_ptr, T.P, T.Q, T.sign, T.zb32, T.nb, T.zk32,
+                     T.nk, T.rhoT, T.splits, smem_raw);
+}
+
 }  // namespace
+
+extern "C" int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                                                  int max_nb, int max_nk, void* stream) {
+    if (n_tasks < 0 || total_ctas < 0 || max_nb <= 0 || max_nk <= 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    const size_t smem = sizeof(float) * 2 * (size_t)kF32Chunk * (size_t)(((max_nb + 3) & ~3) + ((max_nk + 3) & ~3));
+    if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(density_acc_f32_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    density_acc_f32_grouped_kernel<<<(unsigned)total_ctas, kAccThreads, smem, (cudaStream_t)stream>>>(tasks_dev,
+                                                                                                     n_tasks);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
 
 extern "C" int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* idx_ptr_dev, const int32_t* P_dev,
                                           const int32_t* Q_dev, const int8_t* sign_dev, const float* zb32_dev, int n_b,

@@ -58,7 +58,88 @@ __global__ void __launch_bounds__(1024) normalize_kernel(int64_t n, const double
     if (threadIdx.x == 0) *beta_out = b;
 }
 
+// Whole Krylov loop of a small sector in one CTA: m Lanczos steps with two classical
+// Gram-Schmidt passes, the same arithmetic as the per-step launches (gemv_rows, two CGS
+// passes of gemv_rows + gemv_cols, normalize) without 6 m launches.  H is read from global
+// memory (L2-resident for the sizes this serves); w and the CGS coefficients live in shared
+// memory.  alpha[j] = sum of both passes' coefficient of V[j]; beta[j] = |w| after them.
+__device__ __forceinline__ double block_sum(double s, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+    return t;
+}
+
+__global__ void __launch_bounds__(1024) lanczos_small_kernel(int n, int m, const double* __restrict__ H, int64_t ld,
+                                                             const double* __restrict__ v0, double* __restrict__ V,
+                                                             double* __restrict__ alpha, double* __restrict__ beta) {
+    extern __shared__ double sm[];
+    double* w = sm;               // [n]
+    double* c = w + n;            // [m + 1]
+    __shared__ double red[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    for (int k = tid; k < n; k += blockDim.x) V[k] = v0[k];
+    __syncthreads();
+    for (int j = 0; j < m; ++j) {
+        const double* vj = V + (int64_t)j * n;
+        for (int r = warp; r < n; r += nw) {
+            const double* h = H + (int64_t)r * ld;
+            double s = 0.0;
+            for (int k = lane; k < n; k += 32) s = fma(h[k], vj[k], s);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) w[r] = s;
+        }
+        __syncthreads();
+        double a = 0.0;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int i = warp; i <= j; i += nw) {
+                const double* vi = V + (int64_t)i * n;
+                double s = 0.0;
+                for (int k = lane; k < n; k += 32) s = fma(vi[k], w[k], s);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) c[i] = s;
+            }
+            __syncthreads();
+            a += c[j];
+            for (int k = tid; k < n; k += blockDim.x) {
+                double s = 0.0;
+                for (int i = 0; i <= j; ++i) s = fma(c[i], V[(int64_t)i * n + k], s);
+                w[k] -= s;
+            }
+            __syncthreads();
+        }
+        double s = 0.0;
+        for (int k = tid; k < n; k += blockDim.x) s = fma(w[k], w[k], s);
+        const double b = sqrt(block_sum(s, red));
+        const double inv = b > 0.0 ? 1.0 / b : 0.0;
+        double* vn = V + (int64_t)(j + 1) * n;
+        for (int k = tid; k < n; k += blockDim.x) vn[k] = w[k] * inv;
+        if (tid == 0) {
+            alpha[j] = a;
+            beta[j] = b;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+extern "C" int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
+                                 double* alpha_dev, double* beta_dev, void* stream) {
+    if (n <= 0 || m <= 0 || ld < n) return XRH_ERR_ARG;
+    if (!H_dev || !v0_dev || !V_dev || !alpha_dev || !beta_dev) return XRH_ERR_ARG;
+    const size_t smem = sizeof(double) * ((size_t)n + (size_t)m + 1);
+    if (n > 4096 || smem > 48 * 1024) return XRH_ERR_CAPACITY;
+    lanczos_small_kernel<<<1, 1024, smem, (cudaStream_t)stream>>>(n, m, H_dev, ld, v0_dev, V_dev, alpha_dev, beta_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
 
 extern "C" int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* x_dev,
                              double alpha, double beta, double* y_dev, void* stream) {

@@ -258,6 +258,25 @@ class DensityBuilder:
                     self.splits[key] = 1
                 else:
                     self.splits[key] = int(min(64, max(1, round(cp.count / max(cp.K, 1) / 256))))
+            # every block of the fragment in one grouped launch
+            tasks = np.zeros(len(space.couplings), dtype=_lib.DENS_TASK_DTYPE)
+            begin = 0
+            self._zero_first = []
+            for i, ((op, bc, kc), cp) in enumerate(space.couplings.items()):
+                t = tasks[i]
+                t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(), cp.Q.data_ptr(),
+                                                           cp.sign.data_ptr())
+                t["zb32"], t["zk32"] = self.zbT32[bc].data_ptr(), self.zT32[kc].data_ptr()
+                t["rhoT"] = self._tmp[(op, bc, kc)].data_ptr()
+                t["K"], t["nb"], t["nk"] = cp.K, self.n_states_bra[bc], self.n_states[kc]
+                t["splits"], t["cta_begin"] = self.splits[(op, bc, kc)], begin
+                begin += cp.K * self.splits[(op, bc, kc)]
+                if self.splits[(op, bc, kc)] > 1:
+                    self._zero_first.append(self._tmp[(op, bc, kc)])
+            self._dens_tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
+            self._n_dens_tasks, self._dens_ctas = len(tasks), begin
+            self._max_nb = max(self.n_states_bra.values()) if self.n_states_bra else 1
+            self._max_nk = max(self.n_states.values()) if self.n_states else 1
 
     def build(self, coeffs, bra_coeffs=None):
         """coeffs: {charge: CUDA float64 tensor (n_states, n_conf)}."""
@@ -269,16 +288,15 @@ class DensityBuilder:
             for c in self.space.charges:
                 self.zT32[c][:, :self.n_states[c]].copy_(self.zT[c])
                 self.zbT32[c][:, :self.n_states_bra[c]].copy_(self.zbT[c])
+        if self.f32:
+            for t in self._zero_first:
+                t.zero_()
+            call("xrh_density_accumulate_f32_grouped", ptr(self._dens_tasks), self._n_dens_tasks, self._dens_ctas,
+                 self._max_nb, self._max_nk, s)
         for (op, bc, kc), cp in self.space.couplings.items():
             nb, nk = self.n_states_bra[bc], self.n_states[kc]
             tmp = self._tmp[(op, bc, kc)]
-            if self.f32:
-                sp_ = self.splits[(op, bc, kc)]
-                if sp_ > 1:
-                    tmp.zero_()
-                call("xrh_density_accumulate_f32", cp.K, sp_, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q), ptr(cp.sign),
-                     ptr(self.zbT32[bc]), nb, ptr(self.zT32[kc]), nk, ptr(tmp), s)
-            else:
+            if not self.f32:
                 call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
                      ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
             call("xrh_transpose", ptr(tmp), cp.K, nb * nk, ptr(self.rho[op][(bc, kc)]), s)

@@ -12,6 +12,8 @@ import torch
 
 from ._lib import call, ptr, stream_ptr
 
+SMALL_SECTOR = 2048
+
 
 class Lanczos:
     def __init__(self, n, m=96, device="cuda", seed=7):
@@ -29,13 +31,20 @@ class Lanczos:
         self.beta = torch.zeros(self.m, **f64)
         self.y = torch.zeros(self.m + 1, **f64)
         self.vec = torch.zeros(self.n, **f64)
+        self.ab = torch.zeros(2 * self.m, **f64)          # alpha_j, beta_j
         self._host = torch.empty(3 * self.m, dtype=torch.float64).pin_memory() if torch.cuda.is_available() else None
+        # sectors up to this size run the whole Krylov loop in one launch
+        self.small = self.n <= SMALL_SECTOR
 
     def krylov(self, H, ld=None):
         """Device-only part: m Lanczos steps on H (n x n, row stride ld)."""
         s = stream_ptr()
         n, m = self.n, self.m
         ld = n if ld is None else ld
+        if self.small:
+            call("xrh_lanczos_small", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab),
+                 ptr(self.ab[m:]), s)
+            return
         self.V[0].copy_(self.v0)
         for j in range(m):
             call("xrh_gemv_rows", n, n, ptr(H), ld, ptr(self.V[j]), 1.0, 0.0, ptr(self.w), s)
@@ -47,10 +56,11 @@ class Lanczos:
     def stage_to_host(self):
         """Queue the copy of the tridiagonal coefficients (alpha_j, beta_j) to pinned memory."""
         m = self.m
-        idx = torch.arange(m, device=self.CC.device)
-        alpha = self.CC[idx, idx] + self.CC2[idx, idx]
-        self._host[:m].copy_(alpha, non_blocking=True)
-        self._host[m:2 * m].copy_(self.beta, non_blocking=True)
+        if not self.small:
+            idx = torch.arange(m, device=self.CC.device)
+            self.ab[:m].copy_(self.CC[idx, idx] + self.CC2[idx, idx])
+            self.ab[m:].copy_(self.beta)
+        self._host[:2 * m].copy_(self.ab, non_blocking=True)
 
     def solve(self, k=5):
         """Host part (after a sync): eigenpairs of the m x m tridiagonal matrix.

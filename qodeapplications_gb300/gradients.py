@@ -277,6 +277,28 @@ class XRDimerAdjoint:
                     continue
                 gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
+        # FP32 path: every block of a fragment in one grouped launch
+        self.dens_adj_groups = []
+        if self.prec32:
+            for m in (0, 1):
+                entries = [e for e in self.dens_adj if e[0] == m]
+                if not entries:
+                    continue
+                bld = plan.builders[m]
+                tasks = np.zeros(len(entries), dtype=_lib.DENS_ADJ_TASK_DTYPE)
+                begin = 0
+                for i, (_m, op, bc, kc, cp, rt, grho, gT) in enumerate(entries):
+                    t = tasks[i]
+                    t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(),
+                                                               cp.Q.data_ptr(), cp.sign.data_ptr())
+                    t["zb32"], t["zk32"] = bld.zbT32[bc].data_ptr(), bld.zT32[kc].data_ptr()
+                    t["gT"] = gT.data_ptr()
+                    t["gzb"], t["gzk"] = self.gz32[m][bc].data_ptr(), self.gz32[m][kc].data_ptr()
+                    t["K"], t["nb"], t["nk"], t["cta_begin"] = cp.K, rt.shape[0], rt.shape[1], begin
+                    begin += cp.K
+                dev_tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
+                self.dens_adj_groups.append((dev_tasks, len(entries), begin,
+                                             max(e[5].shape[0] for e in entries), max(e[5].shape[1] for e in entries)))
 
     # ------------------------------------------------------------------------------------
     def launch_L3(self):
@@ -339,12 +361,14 @@ class XRDimerAdjoint:
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
-            gb_, gk_ = ((self.gz32[m][bc], self.gz32[m][kc]) if self.prec32 else
-                        (self.G[("gzT", m, bc)], self.G[("gzT", m, kc)]))
+            if self.prec32:
+                continue
             bld = plan.builders[m]
-            zb_, zk_ = ((bld.zbT32[bc], bld.zT32[kc]) if self.prec32 else (bld.zbT[bc], bld.zT[kc]))
             call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
-                 ptr(cp.Q), ptr(cp.sign), ptr(zb_), nb, ptr(zk_), nk, ptr(gT), ptr(gb_), ptr(gk_), s)
+                 ptr(cp.Q), ptr(cp.sign), ptr(bld.zbT[bc]), nb, ptr(bld.zT[kc]), nk, ptr(gT),
+                 ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
+        for (tasks, n_t, ctas, mnb, mnk) in self.dens_adj_groups:
+            call("xrh_density_adjoint_f32_grouped", ptr(tasks), n_t, ctas, mnb, mnk, s)
         self.launch_gamma()
 
 
