@@ -38,7 +38,7 @@ METRIC = "XR-H build+grad s/iter vs plain FP64 GPU, at |dE|<=1e-6 Eh vs FP64 ora
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
@@ -189,26 +189,62 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
     return sum(ms) / 1e3 / steps, Es, it
 
 
-def dominant_kernel_roofline(it, reps=20):
-    """Live CUDA-event timing of the final grouped-GEMM launch (the dominant tensor-contraction
-    kernel), on the launching stream, buffers as left by the last iteration."""
+# DRAM bytes (read + write) per launch of the grouped FP32 density build, from one ncu
+# capture of the bench command (profiles/density_acc_f32_grouped_dimer2x9.md); None where
+# no capture exists for the workload
+DENSITY_TRAFFIC_BYTES = {1: 26_977_664}
+
+
+def density_kernel_work(builder):
+    """Algorithmic bytes and FLOPs of one grouped density launch of a fragment: coupling lists
+    read once (idx_ptr 8 B per index; P, Q 4 B and sign 1 B per coupling), the FP32 coefficient
+    rows read once, rho^T written once (8 B per element); 2 n_b n_k FLOPs per coupling."""
+    sp = builder.space
+    by, fl = 0.0, 0.0
+    for (op, bc, kc), cp in sp.couplings.items():
+        nb, nk = builder.n_states_bra[bc], builder.n_states[kc]
+        by += 8.0 * (cp.K + 1) + 9.0 * cp.count + 8.0 * cp.K * nb * nk
+        fl += 2.0 * nb * nk * cp.count
+    for c in sp.charges:
+        by += 4.0 * sp.n_conf[c] * (builder.zT32[c].shape[1] + builder.zbT32[c].shape[1])
+    return by, fl
+
+
+def dominant_kernel_roofline(it, config, reps=20):
+    """Live CUDA-event timing, on the launching stream, of the dominant kernel of the step in
+    the ncu launch list (the grouped FP32 density build: one launch per fragment), with the
+    buffers as the last iteration left them."""
     import torch
+    from qodeapplications_gb300 import _lib
     plan = it.opt.plan
-    if plan.tc:
-        g, flops, name = plan.fin_tc, plan.fin_tc.flops, f"gemm_tc_kernel<{'bf16' if plan.precision == 2 else 'tf32'}> (final blocks)"
-    else:
-        g, flops, name = plan.fin, plan.fin.flops, "gemm_fp64_kernel (final blocks)"
+    builders = [b for b in plan.builders if getattr(b, "f32", False)]
+    if not builders:
+        return None
+    work = [density_kernel_work(b) for b in builders]
+    stream = torch.cuda.current_stream()
+    s = _lib.stream_ptr(stream)
+
+    def launch(b):
+        for t in b._zero_first:
+            t.zero_()
+        _lib.call("xrh_density_accumulate_f32_grouped", _lib.ptr(b._dens_tasks), b._n_dens_tasks, b._dens_ctas,
+                  b._max_nb, b._max_nk, s)
     for _ in range(3):
-        g.run()
+        for b in builders:
+            launch(b)
     torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
     for _ in range(reps):
-        g.run()
-    e.record()
+        for b in builders:
+            launch(b)
+    e1.record(stream)
     torch.cuda.synchronize()
-    ms = s.elapsed_time(e) / reps
-    return name, flops, ms
+    ms = e0.elapsed_time(e1) / (reps * len(builders))
+    by = sum(w[0] for w in work) / len(work)
+    fl = sum(w[1] for w in work) / len(work)
+    return dict(name="density_acc_f32_grouped_kernel (FP32 density build, one launch per fragment)",
+                ms=ms, bytes=by, flops=fl, traffic=DENSITY_TRAFFIC_BYTES.get(config))
 
 
 def run_ours(args):
@@ -277,26 +313,23 @@ def run_ours(args):
         return
 
     s_per_iter = total_ms / 1e3 / args.steps
-    kname, kflops, kms = dominant_kernel_roofline(it)
     peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
-    achieved = kflops / (kms * 1e-3) / 1e12
-    if it.opt.plan.tc:
-        peak = float(peaks.get("bf16_tflops", 1900.0))
-        if args.precision == "tf32x3":
-            peak_note = "measured dense BF16 peak (MEASURED_PEAKS.json bf16_tflops) halved for kind::tf32"
-            peak = peak / 2
-        else:
-            peak_note = "measured dense BF16 peak (MEASURED_PEAKS.json bf16_tflops)"
-        roofline = {"bound": "tensor", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak, "mma_frac": 3 * achieved / peak, "traffic": None,
-                    "note": "achieved counts algorithmic FLOPs once; each costs 3 MMA FLOPs (hi*hi, hi*lo, lo*hi)",
-                    "peak_source": peak_note, "launch_ms": kms}
+    dk = dominant_kernel_roofline(it, args.config)
+    if dk is not None:
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        achieved = dk["bytes"] / (dk["ms"] * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": dk["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "traffic": dk["traffic"], "launch_ms": dk["ms"],
+                    "algorithmic_bytes_per_launch": dk["bytes"], "flops_per_launch": dk["flops"],
+                    "fp32_tflops_achieved": dk["flops"] / (dk["ms"] * 1e-3) / 1e12,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy) of measured"
+                    if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+                    "note": "sparse outer-product accumulation over coupling lists on the CUDA cores (FP32 FMA, "
+                            "coefficient rows gathered from L2): neither HBM- nor tensor-bound; the FP32 rate is "
+                            "given beside the HBM fraction"}
     else:
-        fp64_peak = measure_fp64_peak()
-        roofline = {"bound": "tensor", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "frac": achieved / fp64_peak, "traffic": None, "launch_ms": kms,
-                    "peak_source": "FP64 DGEMM (torch.matmul float64 8192^3) measured in this run"}
+        roofline = None
 
     variants = {}
     if not args.no_variants and world == 1:
@@ -329,6 +362,8 @@ def run_ours(args):
         "gpu_launches": launches, "gpu_launches_per_iteration": per_iter, "roofline": roofline, "clocks": clocks,
         "energies": energies[:3], "flops_per_build": it.opt.plan.flops, "variants": variants,
     }
+    if "fp64" in variants and args.precision != "fp64":
+        line["speedup_vs_fp64_gpu"] = variants["fp64"]["s_per_iter"] / s_per_iter
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))
@@ -353,23 +388,6 @@ def accuracy_check(sysd):
         del opt
         torch.cuda.empty_cache()
     return out
-
-
-def measure_fp64_peak():
-    import torch
-    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
-    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e9
-    for _ in range(3):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        torch.matmul(a, b)
-        e.record()
-        torch.cuda.synchronize()
-        best = min(best, s.elapsed_time(e))
-    return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
 
 
 def run_reference(args):
