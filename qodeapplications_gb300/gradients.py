@@ -62,6 +62,7 @@ class XRDimerAdjoint:
             want(("g", p_), tuple(t_.shape))
         for wk, Wt in plan.W.items():
             want(("gW", wk), tuple(Wt.shape))
+        gp_total = [0, 0]
         for m in (0, 1):
             want(("gmono1", m), (1, N[m] ** 2))
             want(("Gamma", m), (N[m] ** 4,))
@@ -73,7 +74,10 @@ class XRDimerAdjoint:
                     sg = plan.sigma[m][c]
                     if sg.pl is not None:
                         for k, cl in enumerate(sg.pl["classes"]):
-                            want(("Gpair", m, c, k), (cl["n_p"], cl["n_p"]))
+                            gp_total[m] += cl["n_p"] ** 2
+        for m in (0, 1):
+            if gp_total[m]:
+                want(("Gpairs", m), (gp_total[m],))      # the pair blocks of Gamma, one buffer per fragment
         for i, t in enumerate(plan.final_tasks):
             ni0, nj0, ni1, nj1 = t["dims"]
             for s, (A, lda, B, ldb, K, a) in enumerate(t["segs"]):
@@ -221,11 +225,14 @@ class XRDimerAdjoint:
         # intermediates: Gamma[pq, rs] = sum_(I, K) D_zb[I, (K, pq)] D_Y[I, (K, rs)] per spin
         # class (D_zb is the forward pass's pair scatter of the same coefficients) ----
         self.gamma_ri, self.gamma_old = [], []
-        Lg = GroupedGemm(dev, "fp64")
+        Lg = GroupedGemm(dev, gprec)
         self.gam_reg = SplitRegistry("tf32x3", dev)
         Lgt = TCGroupedGemm(self.gam_reg)
         self.gam_T = []
+        self.gam_scatter = []
         for m in (0, 1):
+            off = 0
+            flat_all = []
             for c in plan.H1blk[m]:
                 sg = plan.sigma[m][c]
                 if sg.pl is None:
@@ -234,26 +241,29 @@ class XRDimerAdjoint:
                 Dy = torch.zeros_like(sg.D)
                 n = plan.n_states[m][c]
                 Nm = N[m]
-                parts = []
                 for k, cl in enumerate(sg.pl["classes"]):
                     nK, npr = cl["n_K"], cl["n_p"]
                     b = n * cl["base"]
                     Dyc = Dy[b:b + n * nK * npr].view(n * nK, npr)
-                    Gp = self.G[("Gpair", m, c, k)]
-                    if sg.tc:
-                        # Gamma_c = D^T Dy on the tensor cores, from K-major transposed copies
+                    Gp = self.G[("Gpairs", m)][off:off + npr * npr].view(npr, npr)
+                    off += npr * npr
+                    if sg.tc and n * nK >= 8192:
+                        # Gamma_c = D^T Dy on the tensor cores (3 x TF32), from K-major transposed
+                        # copies; n states x n_K intermediates is a long K: split-K, FP64 atomics
                         DT = torch.empty((npr, n * nK), **f64)
                         DyT = torch.empty((npr, n * nK), **f64)
                         self.gam_T += [(sg.Dc[k], DT), (Dyc, DyT)]
-                        # (n states x n_K intermediates is a long K: split-K, atomic FP64 sums)
                         Lgt.add(npr, npr, [(DT, n * nK, DyT, n * nK, n * nK, 1.0)], Gp, npr, mode=1,
                                 groups=[("gam", "gam")])
-                    else:
+                    else:                 # short K: the SIMT GEMM reads both operands transposed
                         Lg.add(npr, npr, [(sg.Dc[k], npr, Dyc, npr, n * nK, 1.0, 3, 0, 0)], Gp, npr, mode=1,
                                splitk=_splitk(n * nK, 256, 64))
-                    flat = torch.as_tensor(cl["u"] * Nm + cl["v"], device=dev)
-                    parts.append((Gp, flat[:, None], flat[None, :]))
-                self.gamma_ri.append((m, c, sg, Dy, parts))
+                    pq = cl["u"] * Nm + cl["v"]
+                    flat_all.append((pq[:, None] * Nm * Nm + pq[None, :]).reshape(-1))
+                self.gamma_ri.append((m, c, sg, Dy))
+            if flat_all:
+                idx = torch.as_tensor(np.concatenate(flat_all), dtype=torch.int64, device=dev)
+                self.gam_scatter.append((m, idx, self.G[("Gpairs", m)][:off]))
         self.Lgamma = Lg.finalize()
         self.gam_reg.upload()
         self.Lgamma_tc = Lgt.finalize().autotune()
@@ -314,7 +324,7 @@ class XRDimerAdjoint:
         """Two-particle densities of the monomer two-electron terms (after launch 2)."""
         plan = self.plan
         s = stream_ptr()
-        for (m, c, sg, Dy, parts) in self.gamma_ri:
+        for (m, c, sg, Dy) in self.gamma_ri:
             sg.scatter(self.G[("YT", m, c)], Dy)
         for src, dst in self.gam_T:
             dst.copy_(src.t())
@@ -322,11 +332,9 @@ class XRDimerAdjoint:
             self.gam_reg.split("gam")
         self.Lgamma.run()
         self.Lgamma_tc.run()
-        for (m, c, sg, Dy, parts) in self.gamma_ri:
-            G2 = self.G[("Gamma", m)].view(plan.N[m] ** 2, plan.N[m] ** 2)
-            for Gp, ri, ci in parts:
-                # positions are distinct within a class: gather, add, scatter (no sort)
-                G2[ri, ci] = G2[ri, ci] + Gp
+        for (m, idx, vals) in self.gam_scatter:
+            # every pair block of the fragment into the N^4 Gamma in one atomic index-add
+            self.G[("Gamma", m)].index_add_(0, idx, vals)
         for (m, c) in self.gamma_old:
             sp = plan.spaces[m]
             call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
@@ -431,14 +439,13 @@ class XRDimerAdjoint:
         Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
         key = (tuple(spatial_index), T.device)
         if key not in self._spatial_cache:     # built on first use, outside any graph capture
-            idx = torch.as_tensor(np.asarray(spatial_index), device=T.device)
             n_sp = int(max(spatial_index)) + 1
-            self._spatial_cache[key] = (idx[:, None].expand(t, t).contiguous(), idx[None, :].expand(t, t).contiguous(),
-                                        _same_spin(t, spatial_index, T.device), n_sp)
-        I0, I1, same, n_sp = self._spatial_cache[key]
-        Gsp = torch.zeros((n_sp, n_sp), dtype=torch.float64, device=T.device)
+            Pm = torch.zeros((t, n_sp), dtype=torch.float64, device=T.device)
+            Pm[torch.arange(t, device=T.device), torch.as_tensor(np.asarray(spatial_index), device=T.device)] = 1.0
+            self._spatial_cache[key] = (Pm, _same_spin(t, spatial_index, T.device))
+        Pm, same = self._spatial_cache[key]
         # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs
-        Gsp.index_put_((I0, I1), Gso * same, accumulate=True)
+        Gsp = Pm.t() @ (Gso * same) @ Pm
         return Gsp - Gsp.t()
 
 

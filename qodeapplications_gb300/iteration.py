@@ -27,15 +27,39 @@ from .synthetic import spin_orbital_spatial_index
 
 
 def _inv_sqrt_newton_schulz(S, iters=6):
-    """S^-1/2 for symmetric positive definite S close to the identity (coupled Newton-Schulz)."""
-    n = S.shape[0]
-    I = torch.eye(n, dtype=S.dtype, device=S.device)
+    """S^-1/2 for symmetric positive definite S close to the identity (coupled Newton-Schulz);
+    S may be a batch (..., n, n)."""
+    n = S.shape[-1]
+    I = torch.eye(n, dtype=S.dtype, device=S.device).expand_as(S)
     Y, Z = S.clone(), I.clone()
     for _ in range(iters):
         T = 0.5 * (3.0 * I - Z @ Y)
         Y = Y @ T
         Z = T @ Z
     return Z
+
+
+def _step_and_orthonormalise(coeffs, grads, step):
+    """z <- (z' z'^T)^-1/2 z' with z' = z - step * (tangent part of g), for every (fragment,
+    charge) block; the n x n inverse square roots of blocks with equal n run as one batch.
+    Returns the squared norm of the tangent gradient (device scalar)."""
+    sq = None
+    znew, S = [], []
+    for z, g in zip(coeffs, grads):
+        gt = tangent_project(g, z)
+        part = (gt * gt).sum()
+        sq = part if sq is None else sq + part
+        zn = z - step * gt
+        znew.append(zn)
+        S.append(zn @ zn.t())
+    by_n = {}
+    for i, Si in enumerate(S):
+        by_n.setdefault(Si.shape[0], []).append(i)
+    for n, ids in by_n.items():
+        Z = _inv_sqrt_newton_schulz(torch.stack([S[i] for i in ids]))
+        for k, i in enumerate(ids):
+            coeffs[i].copy_(Z[k] @ znew[i])
+    return sq
 
 
 class XRStateOptimizer:
@@ -91,16 +115,9 @@ class XRStateOptimizer:
         self.lz_warm[t].v0.copy_(d)
         self.adj.launch(self.d_product)
         g = self.adj.state_gradient()
-        sq = torch.zeros((), dtype=torch.float64, device=self.device)
-        for m in range(2):
-            for c in self.charges:
-                z = self.plan.coeffs[m][c]
-                gt = tangent_project(g[m][c], z)
-                sq = sq + (gt * gt).sum()
-                znew = z - self.step_size * gt
-                S = znew @ znew.t()
-                z.copy_(_inv_sqrt_newton_schulz(S) @ znew)
-        self._gsq = sq
+        keys = [(m, c) for m in range(2) for c in self.charges]
+        self._gsq = _step_and_orthonormalise([self.plan.coeffs[m][c] for m, c in keys], [g[m][c] for m, c in keys],
+                                             self.step_size)
         if self.orbital:
             self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
 
@@ -188,15 +205,9 @@ class XRStateOptimizer:
         lz.v0.copy_(d)
         self.adj.launch(self.d_product)
         g = self.adj.state_gradient()
-        sq = torch.zeros((), dtype=torch.float64, device=self.device)
-        for m in range(2):
-            for c in self.charges:
-                z = self.plan.coeffs[m][c]
-                gt = tangent_project(g[m][c], z)
-                sq = sq + (gt * gt).sum()
-                znew = z - self.step_size * gt
-                z.copy_(_inv_sqrt_newton_schulz(znew @ znew.t()) @ znew)
-        self._gsq = sq
+        keys = [(m, c) for m in range(2) for c in self.charges]
+        self._gsq = _step_and_orthonormalise([self.plan.coeffs[m][c] for m, c in keys], [g[m][c] for m, c in keys],
+                                             self.step_size)
         if self.orbital:
             self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
 
