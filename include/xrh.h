@@ -127,6 +127,14 @@ int xrh_density_build_noalloc(int precision, int64_t K, const int64_t* idx_ptr_d
 /* out[c, r] = in[r, c] for a row-major [rows, cols] FP64 matrix. */
 int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_dev, void* stream);
 
+/* Mirrored density blocks (no reference counterpart: the reference builds every block):
+ * rho^cca(b, k)[I, J, p, q, r] = rho^caa(k, b)[J, I, r, q, p], and likewise cc / aa, c / a.
+ *   dst[a][b][f] = (accumulate ? dst[a][b][f] : 0) + src[b][a][reverse(f)]
+ * for a < na, b < nb and f over N^L (L <= 4 operator indices, reverse = digits in reverse
+ * order).  The adjoint uses the same map with accumulate = 1. */
+int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev,
+                       int accumulate, void* stream);
+
 /* Monomer two-electron term without the N^4 density (replaces building rho^ccaa and
  * contracting it, general-XRCC/build_density_tensors.py:122-133 + H_contractions.c:61-78):
  *   sigmaT[J, P] = sum_Q <P| sum_pqrs V_pqrs c+_p c+_q a_s a_r |Q> zk[J, Q]

@@ -26,6 +26,7 @@ _SIGS = {
     "xrh_abi_version": (_i32, []),
     "xrh_density_accumulate_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
     "xrh_density_adjoint_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
+    "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_im_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),

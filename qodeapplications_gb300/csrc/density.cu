@@ -270,6 +270,44 @@ extern "C" int xrh_sigma2e(int precision, int n_orbs, const double* V_dev, const
     return XRH_OK;
 }
 
+// ---- mirrored blocks -----------------------------------------------------------------------
+// <P| c+_p c+_q a_r |Q> = <Q| c+_r a_q a_p |P> for real states, so rho^cca(b, k)[I, J, p, q, r]
+// = rho^caa(k, b)[J, I, r, q, p]; likewise cc / aa and c / a: the creation-side blocks are the
+// annihilation-side ones with bra and ket swapped and the operator indices reversed.
+//   dst[a][b][f] = (accumulate ? dst : 0) + src[b][a][reverse(f)],  f over N^L
+__global__ void mirror_kernel(int na, int nb, int N, int L, const double* __restrict__ src, double* __restrict__ dst,
+                              int accumulate) {
+    int64_t F = 1;
+    for (int l = 0; l < L; ++l) F *= N;
+    const int64_t total = (int64_t)na * nb * F;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ab = t / F;
+        int64_t f = t - ab * F;
+        const int a = (int)(ab / nb), b = (int)(ab - (int64_t)a * nb);
+        int64_t r = 0;
+        for (int l = 0; l < L; ++l) {
+            r = r * N + f % N;
+            f /= N;
+        }
+        const double v = src[((int64_t)b * na + a) * F + r];
+        dst[t] = accumulate ? dst[t] + v : v;
+    }
+}
+
+extern "C" int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev, int accumulate,
+                                  void* stream) {
+    if (na <= 0 || nb <= 0 || N <= 0 || L < 1 || L > 4 || !src_dev || !dst_dev || src_dev == dst_dev)
+        return XRH_ERR_ARG;
+    int64_t F = 1;
+    for (int l = 0; l < L; ++l) F *= N;
+    const int64_t total = (int64_t)na * nb * F;
+    const int64_t blocks = (total + 255) / 256;
+    mirror_kernel<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, (cudaStream_t)stream>>>(
+        na, nb, N, L, src_dev, dst_dev, accumulate);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
 // ---- allocation-free density build ------------------------------------------------------
 // For callers that cannot allocate device memory: the scratch that xrh_density_accumulate's
 // callers provide (the [K, n_b, n_k] buffer before the transpose) is a fixed-size array in

@@ -216,20 +216,38 @@ def pair_offsets(pl, n):
     return base[c] + pl["k"] * n_p[c] + pl["p"], stride[c]
 
 
+# creation-side operator string -> its annihilation-side partner (bra and ket swapped,
+# operator indices reversed: rho^cca(b, k)[I, J, p, q, r] = rho^caa(k, b)[J, I, r, q, p])
+MIRROR_OF = {"c": "a", "cc": "aa", "cca": "caa"}
+
+
+def mirror_pairs(space):
+    """{derived block key: partner block key} for the blocks of a space that follow from
+    their partner by xrh_mirror_density."""
+    out = {}
+    for (op, bc, kc) in space.couplings:
+        if op in MIRROR_OF and (MIRROR_OF[op], kc, bc) in space.couplings:
+            out[(op, bc, kc)] = (MIRROR_OF[op], kc, bc)
+    return out
+
+
 class DensityBuilder:
     """Preallocated, reusable density build for one fragment and fixed state counts.
 
     build(coeffs, bra_coeffs=None) fills self.rho[op][(bra_chg, ket_chg)], each a CUDA
     float64 tensor of shape (n_bra, n_ket, N, ..., N) (the reference's layout,
-    Be-states/densities.py:167-208).  Buffers are reused by every call (CUDA-graph safe)."""
+    Be-states/densities.py:167-208).  Buffers are reused by every call (CUDA-graph safe).
+    With the same states on both sides (mirror=True, no bra_coeffs) the c, cc and cca
+    blocks are mirrored from their a, aa and caa partners instead of accumulated."""
 
-    def __init__(self, space, n_states, precision="fp64", n_states_bra=None):
+    def __init__(self, space, n_states, precision="fp64", n_states_bra=None, mirror=True):
         self.space = space
         self.precision = _lib.PRECISIONS[precision]
         if self.precision not in (_lib.FP64, _lib.FP32):
             self.precision = _lib.FP32       # tensor-core variants build densities with FP32 products
         self.n_states = dict(n_states)
         self.n_states_bra = dict(n_states_bra or n_states)
+        self.mirror = mirror_pairs(space) if (mirror and self.n_states_bra == self.n_states) else {}
         dev = space.device
         self.rho = {}
         self._tmp = {}
@@ -258,11 +276,12 @@ class DensityBuilder:
                     self.splits[key] = 1
                 else:
                     self.splits[key] = int(min(64, max(1, round(cp.count / max(cp.K, 1) / 256))))
-            # every block of the fragment in one grouped launch
-            tasks = np.zeros(len(space.couplings), dtype=_lib.DENS_TASK_DTYPE)
+            # every accumulated block of the fragment in one grouped launch
+            direct = [(key, cp) for key, cp in space.couplings.items() if key not in self.mirror]
+            tasks = np.zeros(len(direct), dtype=_lib.DENS_TASK_DTYPE)
             begin = 0
             self._zero_first = []
-            for i, ((op, bc, kc), cp) in enumerate(space.couplings.items()):
+            for i, ((op, bc, kc), cp) in enumerate(direct):
                 t = tasks[i]
                 t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(), cp.Q.data_ptr(),
                                                            cp.sign.data_ptr())
@@ -281,6 +300,8 @@ class DensityBuilder:
     def build(self, coeffs, bra_coeffs=None):
         """coeffs: {charge: CUDA float64 tensor (n_states, n_conf)}."""
         s = stream_ptr()
+        if bra_coeffs is not None and self.mirror:
+            raise ValueError("separate bra coefficients need DensityBuilder(..., mirror=False)")
         for c in self.space.charges:
             self.zT[c].copy_(coeffs[c].t())
             self.zbT[c].copy_((coeffs if bra_coeffs is None else bra_coeffs)[c].t())
@@ -294,12 +315,20 @@ class DensityBuilder:
             call("xrh_density_accumulate_f32_grouped", ptr(self._dens_tasks), self._n_dens_tasks, self._dens_ctas,
                  self._max_nb, self._max_nk, s)
         for (op, bc, kc), cp in self.space.couplings.items():
+            if (op, bc, kc) in self.mirror:
+                continue
             nb, nk = self.n_states_bra[bc], self.n_states[kc]
             tmp = self._tmp[(op, bc, kc)]
             if not self.f32:
                 call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
                      ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
             call("xrh_transpose", ptr(tmp), cp.K, nb * nk, ptr(self.rho[op][(bc, kc)]), s)
+        for (op, bc, kc), (pop, pbc, pkc) in self.mirror.items():
+            nb, nk = self.n_states_bra[bc], self.n_states[kc]
+            K = self.space.couplings[(op, bc, kc)].K
+            call("xrh_mirror_density", nb, nk, self.space.N, len(op), ptr(self.rho[pop][(pbc, pkc)]),
+                 ptr(self.rho[op][(bc, kc)]), 0, s)
+            call("xrh_transpose", ptr(self.rho[op][(bc, kc)]), nb * nk, K, ptr(self._tmp[(op, bc, kc)]), s)
         return self.rho
 
 

@@ -269,6 +269,7 @@ class XRDimerAdjoint:
         self.Lgamma_tc = Lgt.finalize().autotune()
 
         self.dens_adj = []
+        self.mirror_adj = []      # (d rho of a mirrored block, d rho of its partner, partner dims, N, L)
         self.im_adj = []          # intermediate-determinant builders: (builder, density gradients, gzT)
         for m in (0, 1):
             b = plan.builders[m]
@@ -284,6 +285,12 @@ class XRDimerAdjoint:
             for (op, bc, kc), cp in plan.spaces[m].couplings.items():
                 rt = b.rho[op][(bc, kc)]
                 if rt.data_ptr() not in grad_of:
+                    continue
+                mir = getattr(b, "mirror", {}).get((op, bc, kc))
+                if mir is not None and b.rho[mir[0]][mir[1:]].data_ptr() in grad_of:
+                    # a mirrored block: its gradient folds into the partner's before the adjoint
+                    self.mirror_adj.append((grad_of[rt.data_ptr()], grad_of[b.rho[mir[0]][mir[1:]].data_ptr()],
+                                            rt.shape[1], rt.shape[0], plan.N[m], len(op)))
                     continue
                 gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
@@ -366,6 +373,8 @@ class XRDimerAdjoint:
         self.launch_L3()
         for (b, grads, gz) in self.im_adj:
             b.adjoint(grads, gz)
+        for (gsrc, gdst, na, nb, Nm, L) in self.mirror_adj:
+            call("xrh_mirror_density", na, nb, Nm, L, ptr(gsrc), ptr(gdst), 1, s)
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
