@@ -166,14 +166,23 @@ __device__ __forceinline__ void density_adjoint_f32_body(
             float acc[4][4] = {};
             if (w < ket_tiles) {            // U[c, J] = s_c sum_I zb[c, I] G[I, J]
                 const int c4 = (w / tj) * 4, j4 = (w % tj) * 4;
-                for (int I = 0; I < nb; ++I) {
-                    const float4 b = *reinterpret_cast<const float4*>(g + I * nkp + j4);
-                    const float bv[4] = {b.x, b.y, b.z, b.w};
+                // 4 x 4 blocks of both operands per step (rows padded with zeros to nbp)
+                for (int I = 0; I < nbp; I += 4) {
+                    float4 a[4], b[4];
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) a[x] = *reinterpret_cast<const float4*>(zbb + (c4 + x) * nbp + I);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) b[i] = *reinterpret_cast<const float4*>(g + (I + i) * nkp + j4);
 #pragma unroll
                     for (int x = 0; x < 4; ++x) {
-                        const float a = zbb[(c4 + x) * nbp + I];
+                        const float av[4] = {a[x].x, a[x].y, a[x].z, a[x].w};
 #pragma unroll
-                        for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a, bv[y], acc[x][y]);
+                        for (int i = 0; i < 4; ++i) {
+                            acc[x][0] = fmaf(av[i], b[i].x, acc[x][0]);
+                            acc[x][1] = fmaf(av[i], b[i].y, acc[x][1]);
+                            acc[x][2] = fmaf(av[i], b[i].z, acc[x][2]);
+                            acc[x][3] = fmaf(av[i], b[i].w, acc[x][3]);
+                        }
                     }
                 }
                 const int valid = nk - j4 < 4 ? nk - j4 : 4;
@@ -188,14 +197,22 @@ __device__ __forceinline__ void density_adjoint_f32_body(
             } else {                        // W[c, I] = s_c sum_J G[I, J] zk[c, J]
                 const int wb = w - ket_tiles;
                 const int c4 = (wb / ti) * 4, i4 = (wb % ti) * 4;
-                for (int J = 0; J < nk; ++J) {
-                    const float4 b = *reinterpret_cast<const float4*>(gt + J * nbp + i4);
-                    const float bv[4] = {b.x, b.y, b.z, b.w};
+                for (int J = 0; J < nkp; J += 4) {
+                    float4 a[4], b[4];
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) a[x] = *reinterpret_cast<const float4*>(zkb + (c4 + x) * nkp + J);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) b[j] = *reinterpret_cast<const float4*>(gt + (J + j) * nbp + i4);
 #pragma unroll
                     for (int x = 0; x < 4; ++x) {
-                        const float a = zkb[(c4 + x) * nkp + J];
+                        const float av[4] = {a[x].x, a[x].y, a[x].z, a[x].w};
 #pragma unroll
-                        for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a, bv[y], acc[x][y]);
+                        for (int j = 0; j < 4; ++j) {
+                            acc[x][0] = fmaf(av[j], b[j].x, acc[x][0]);
+                            acc[x][1] = fmaf(av[j], b[j].y, acc[x][1]);
+                            acc[x][2] = fmaf(av[j], b[j].z, acc[x][2]);
+                            acc[x][3] = fmaf(av[j], b[j].w, acc[x][3]);
+                        }
                     }
                 }
                 const int valid = nb - i4 < 4 ? nb - i4 : 4;
