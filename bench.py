@@ -42,7 +42,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
-    p.add_argument("--precision", default="bf16x3")
+    p.add_argument("--precision", default="tf32x3")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-variants", action="store_true")
     return p.parse_args()

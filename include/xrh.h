@@ -257,6 +257,31 @@ typedef struct {
 int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_dev, int n_tasks, int64_t total_ctas,
                                     int max_nb, int max_nk, void* stream);
 
+/* The same reverse pass on the tensor cores (3 x TF32 split, tcgen05), for blocks with
+ * n_b, n_k <= 64: per operator index, tiles of 128 couplings times G (both orientations)
+ * as two 128 x 64 x 64 GEMMs with gathered coefficient rows.  zbh/zbl, zkh/zkl: the bra /
+ * ket coefficients split into TF32 hi and lo (xrh_split_operand, rows of 64 values, zero
+ * padded).  gzb / gzk receive FP32 vector atomics; *status_dev = XRH_ERR_TIMEOUT when a
+ * bounded wait expired. */
+typedef struct {
+    const int64_t* idx_ptr;
+    const int32_t* P;
+    const int32_t* Q;
+    const int8_t* sign;
+    const uint32_t* zbh;
+    const uint32_t* zbl;
+    const uint32_t* zkh;
+    const uint32_t* zkl;
+    const double* gT;
+    float* gzb;
+    float* gzk;
+    int64_t K;
+    int32_t nb, nk;
+    int64_t cta_begin;
+} xrh_dens_adj_tc_task;   /* 112 bytes */
+int xrh_density_adjoint_tc_grouped(const xrh_dens_adj_tc_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                                   int32_t* status_dev, void* stream);
+
 /* Two-electron terms through (n-2)-electron intermediates K (no reference counterpart: the
  * reference builds rho^ccaa element by element, density_tensors.c:493-556, and contracts it,
  * H_contractions.c:61-78).  A pair list holds, for every determinant X of a space and every

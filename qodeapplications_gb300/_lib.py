@@ -27,6 +27,7 @@ _SIGS = {
     "xrh_density_accumulate_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
     "xrh_density_adjoint_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
     "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
+    "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_im_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),
@@ -135,6 +136,11 @@ DENS_ADJ_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", 
                                 ("gzk", np.uint64), ("K", np.int64), ("nb", np.int32), ("nk", np.int32),
                                 ("cta_begin", np.int64)])
 assert DENS_ADJ_TASK_DTYPE.itemsize == 96
+DENS_ADJ_TC_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.uint64), ("sign", np.uint64),
+                                   ("zbh", np.uint64), ("zbl", np.uint64), ("zkh", np.uint64), ("zkl", np.uint64),
+                                   ("gT", np.uint64), ("gzb", np.uint64), ("gzk", np.uint64), ("K", np.int64),
+                                   ("nb", np.int32), ("nk", np.int32), ("cta_begin", np.int64)])
+assert DENS_ADJ_TC_TASK_DTYPE.itemsize == 112
 DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.uint64), ("sign", np.uint64),
                             ("zb32", np.uint64), ("zk32", np.uint64), ("rhoT", np.uint64), ("K", np.int64),
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),

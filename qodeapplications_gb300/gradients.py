@@ -26,7 +26,11 @@ from .hamiltonian import _Arena, _splitk
 
 
 class XRDimerAdjoint:
-    def __init__(self, plan):
+    def __init__(self, plan, density_adjoint="simt"):
+        """density_adjoint: 'simt' (the grouped CUDA-core kernel) or 'tc' (tensor cores, split-
+        precision plans with at most 64 states per side; exact to the same tolerance but slower
+        at 2 x 9 / 10 and 2 x 14 / 60 states: one CTA per SM runs its gather, MMA and atomic
+        phases in sequence)."""
         assert plan.output == "full", "the adjoint differentiates the full H (H2 + H1 x 1 + 1 x H1)"
         self.plan = plan
         self._spatial_cache = {}
@@ -294,9 +298,40 @@ class XRDimerAdjoint:
                     continue
                 gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
-        # FP32 path: every block of a fragment in one grouped launch
+        # FP32 path: every block of a fragment in one grouped launch, on the tensor cores when
+        # every block has at most 64 states per side (else the CUDA-core kernel)
         self.dens_adj_groups = []
-        if self.prec32:
+        self.dens_adj_tc = []
+        self.tc_status = torch.zeros(1, dtype=torch.int32, device=dev)
+        use_tc = (density_adjoint == "tc" and self.prec32 and plan.tc and
+                  all(e[5].shape[0] <= 64 and e[5].shape[1] <= 64 for e in self.dens_adj))
+        if density_adjoint == "tc" and not use_tc:
+            raise ValueError("the tensor-core density adjoint needs a split-precision plan and <= 64 states")
+        if use_tc:
+            self.z_split = []
+            for m in (0, 1):
+                bld = plan.builders[m]
+                zs = {c: (torch.zeros((plan.spaces[m].n_conf[c], 64), dtype=torch.int32, device=dev),
+                          torch.zeros((plan.spaces[m].n_conf[c], 64), dtype=torch.int32, device=dev))
+                      for c in plan.charges[m]}
+                self.z_split.append((bld, zs))
+                entries = [e for e in self.dens_adj if e[0] == m]
+                if not entries:
+                    continue
+                tasks = np.zeros(len(entries), dtype=_lib.DENS_ADJ_TC_TASK_DTYPE)
+                begin = 0
+                for i, (_m, op, bc, kc, cp, rt, grho, gT) in enumerate(entries):
+                    t = tasks[i]
+                    t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(),
+                                                               cp.Q.data_ptr(), cp.sign.data_ptr())
+                    t["zbh"], t["zbl"] = zs[bc][0].data_ptr(), zs[bc][1].data_ptr()
+                    t["zkh"], t["zkl"] = zs[kc][0].data_ptr(), zs[kc][1].data_ptr()
+                    t["gT"] = gT.data_ptr()
+                    t["gzb"], t["gzk"] = self.gz32[m][bc].data_ptr(), self.gz32[m][kc].data_ptr()
+                    t["K"], t["nb"], t["nk"], t["cta_begin"] = cp.K, rt.shape[0], rt.shape[1], begin
+                    begin += cp.K
+                self.dens_adj_tc.append((torch.from_numpy(tasks.view(np.uint8).copy()).to(dev), len(entries), begin))
+        elif self.prec32:
             for m in (0, 1):
                 entries = [e for e in self.dens_adj if e[0] == m]
                 if not entries:
@@ -327,6 +362,33 @@ class XRDimerAdjoint:
             self.reg3.split("rhoT")
         self.L3.run()
 
+    def launch_density_adjoint(self):
+        """dE/dz from the density gradients (after launch 3)."""
+        plan = self.plan
+        s = stream_ptr()
+        for (b, grads, gz) in self.im_adj:
+            b.adjoint(grads, gz)
+        for (gsrc, gdst, na, nb, Nm, L) in self.mirror_adj:
+            call("xrh_mirror_density", na, nb, Nm, L, ptr(gsrc), ptr(gdst), 1, s)
+        for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
+            nb, nk = rt.shape[0], rt.shape[1]
+            call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
+            if self.prec32:
+                continue
+            bld = plan.builders[m]
+            call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
+                 ptr(cp.Q), ptr(cp.sign), ptr(bld.zbT[bc]), nb, ptr(bld.zT[kc]), nk, ptr(gT),
+                 ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
+        for (tasks, n_t, ctas, mnb, mnk) in self.dens_adj_groups:
+            call("xrh_density_adjoint_f32_grouped", ptr(tasks), n_t, ctas, mnb, mnk, s)
+        if self.dens_adj_tc:
+            for (bld, zs) in self.z_split:
+                for c, (zh, zl) in zs.items():
+                    n = bld.zT[c].shape[1]
+                    call("xrh_split_operand", _lib.TF32X3, ptr(bld.zT[c]), zh.shape[0], n, n, 64, ptr(zh), ptr(zl), s)
+            for (tasks, n_t, ctas) in self.dens_adj_tc:
+                call("xrh_density_adjoint_tc_grouped", ptr(tasks), n_t, ctas, ptr(self.tc_status), s)
+
     def launch_gamma(self):
         """Two-particle densities of the monomer two-electron terms (after launch 2)."""
         plan = self.plan
@@ -355,6 +417,9 @@ class XRDimerAdjoint:
         if self.l3_tc:
             self.L3.check()
         self.Lgamma_tc.check()
+        st = int(self.tc_status.item())
+        if st != 0:
+            raise _lib.XRHError(f"tensor-core density adjoint reported status {st}")
 
     def launch(self, d):
         """Enqueue the reverse pass for ground-state vector d (device, product order)."""
@@ -371,21 +436,7 @@ class XRDimerAdjoint:
         self.L1.run()
         self.L2.run()
         self.launch_L3()
-        for (b, grads, gz) in self.im_adj:
-            b.adjoint(grads, gz)
-        for (gsrc, gdst, na, nb, Nm, L) in self.mirror_adj:
-            call("xrh_mirror_density", na, nb, Nm, L, ptr(gsrc), ptr(gdst), 1, s)
-        for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
-            nb, nk = rt.shape[0], rt.shape[1]
-            call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
-            if self.prec32:
-                continue
-            bld = plan.builders[m]
-            call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
-                 ptr(cp.Q), ptr(cp.sign), ptr(bld.zbT[bc]), nb, ptr(bld.zT[kc]), nk, ptr(gT),
-                 ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
-        for (tasks, n_t, ctas, mnb, mnk) in self.dens_adj_groups:
-            call("xrh_density_adjoint_f32_grouped", ptr(tasks), n_t, ctas, mnb, mnk, s)
+        self.launch_density_adjoint()
         self.launch_gamma()
 
 

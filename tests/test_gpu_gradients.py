@@ -170,3 +170,33 @@ def test_adjoint_built_after_the_build_matches_adjoint_built_before():
         g = adj.state_gradient()
         out.append(torch.cat([g[m][c].reshape(-1) for m in range(2) for c in CHG]).clone())
     assert float((out[0] - out[1]).abs().max()) <= 1e-12 * float(out[0].abs().max())
+
+
+def test_tensor_core_density_adjoint_matches_fp64_over_many_coupling_tiles():
+    """The tensor-core density adjoint (3 x TF32, tiles of 128 couplings) against the FP64
+    adjoint on a system whose operator indices have several hundred couplings each:
+    tangent state gradient within 1e-5 relative."""
+    from qodeapplications_gb300.densities import FragmentSpace
+    from qodeapplications_gb300.gradients import XRDimerAdjoint, tangent_project
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+    n_orb, n_st = 6, 8
+    sysd = S.make_system(n_frag=2, n_orb=n_orb, n_states=n_st, charges=CHG, seed=41)
+    spaces = [FragmentSpace({c: sysd["states"][m][c][1] for c in CHG}, n_orb, 0, 4) for m in range(2)]
+    assert max(cp.count / cp.K for cp in spaces[0].couplings.values()) > 128
+    ns = [{c: n_st for c in CHG}] * 2
+    coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in CHG} for m in range(2)]
+    out = {}
+    for p in ("fp64", "tf32x3"):
+        plan = XRDimerPlan(spaces, ns, [list(CHG)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
+                           precision=p)
+        adj = XRDimerAdjoint(plan, density_adjoint="tc" if p == "tf32x3" else "simt")
+        if p == "tf32x3":
+            assert adj.dens_adj_tc
+        E, d, _ = _gpu_energy_and_grad(plan, adj, coeffs)
+        torch.cuda.synchronize()
+        plan.check_status()
+        adj.check_status()
+        g = adj.state_gradient()
+        out[p] = torch.cat([tangent_project(g[m][c], coeffs[m][c]).reshape(-1) for m in range(2) for c in CHG])
+    rel = float((out["tf32x3"] - out["fp64"]).norm() / out["fp64"].norm())
+    assert rel < 1e-5, rel
