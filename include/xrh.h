@@ -130,8 +130,8 @@ int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_
 /* Mirrored density blocks (no reference counterpart: the reference builds every block):
  * rho^cca(b, k)[I, J, p, q, r] = rho^caa(k, b)[J, I, r, q, p], and likewise cc / aa, c / a.
  *   dst[a][b][f] = (accumulate ? dst[a][b][f] : 0) + src[b][a][reverse(f)]
- * for a < na, b < nb and f over N^L (L <= 4 operator indices, reverse = digits in reverse
- * order).  The adjoint uses the same map with accumulate = 1. */
+ * for a < na, b < nb and f over N^L (L <= 3 operator indices, N <= 64, reverse = digits in
+ * reverse order).  The adjoint uses the same map with accumulate = 1. */
 int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev,
                        int accumulate, void* stream);
 

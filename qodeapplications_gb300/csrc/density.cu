@@ -275,35 +275,47 @@ extern "C" int xrh_sigma2e(int precision, int n_orbs, const double* V_dev, const
 // = rho^caa(k, b)[J, I, r, q, p]; likewise cc / aa and c / a: the creation-side blocks are the
 // annihilation-side ones with bra and ket swapped and the operator indices reversed.
 //   dst[a][b][f] = (accumulate ? dst : 0) + src[b][a][reverse(f)],  f over N^L
-__global__ void mirror_kernel(int na, int nb, int N, int L, const double* __restrict__ src, double* __restrict__ dst,
-                              int accumulate) {
+// One CTA per (a, b[, q]) plane: reversing (p, q, r) -> (r, q, p) transposes the (p, r) plane at
+// fixed q, reversing (p, q) -> (q, p) transposes the plane; both go through shared memory so
+// that loads and stores stay coalesced (N <= 64).
+__global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int L, const double* __restrict__ src,
+                                                     double* __restrict__ dst, int accumulate) {
+    __shared__ double tile[64][65];
     int64_t F = 1;
     for (int l = 0; l < L; ++l) F *= N;
-    const int64_t total = (int64_t)na * nb * F;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t ab = t / F;
-        int64_t f = t - ab * F;
-        const int a = (int)(ab / nb), b = (int)(ab - (int64_t)a * nb);
-        int64_t r = 0;
-        for (int l = 0; l < L; ++l) {
-            r = r * N + f % N;
-            f /= N;
-        }
-        const double v = src[((int64_t)b * na + a) * F + r];
-        dst[t] = accumulate ? dst[t] + v : v;
+    const int64_t blk = blockIdx.x;
+    const int q = (L == 3) ? (int)(blk % N) : 0;
+    const int64_t ab = (L == 3) ? blk / N : blk;
+    const int a = (int)(ab / nb), b = (int)(ab - (int64_t)(ab / nb) * nb);
+    const double* sp = src + ((int64_t)b * na + a) * F;
+    double* dp = dst + ((int64_t)a * nb + b) * F;
+    if (L == 1) {
+        for (int p = threadIdx.x; p < N; p += blockDim.x) dp[p] = (accumulate ? dp[p] : 0.0) + sp[p];
+        return;
+    }
+    const int NN = N * N;
+    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+        const int p = i / N, r = i - p * N;
+        tile[p][r] = sp[L == 2 ? i : ((int64_t)p * N + q) * N + r];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+        const int r = i / N, p = i - r * N;
+        const int64_t pos = L == 2 ? i : ((int64_t)r * N + q) * N + p;
+        const double v = tile[p][r];
+        dp[pos] = accumulate ? dp[pos] + v : v;
     }
 }
 
 extern "C" int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev, int accumulate,
                                   void* stream) {
-    if (na <= 0 || nb <= 0 || N <= 0 || L < 1 || L > 4 || !src_dev || !dst_dev || src_dev == dst_dev)
+    if (na <= 0 || nb <= 0 || N <= 0 || L < 1 || L > 3 || !src_dev || !dst_dev || src_dev == dst_dev)
         return XRH_ERR_ARG;
-    int64_t F = 1;
-    for (int l = 0; l < L; ++l) F *= N;
-    const int64_t total = (int64_t)na * nb * F;
-    const int64_t blocks = (total + 255) / 256;
-    mirror_kernel<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, (cudaStream_t)stream>>>(
-        na, nb, N, L, src_dev, dst_dev, accumulate);
+    if (N > 64) return XRH_ERR_CAPACITY;
+    const int64_t blocks = (int64_t)na * nb * (L == 3 ? N : 1);
+    if (blocks > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    mirror_kernel<<<(unsigned)blocks, L == 1 ? 64 : 256, 0, (cudaStream_t)stream>>>(na, nb, N, L, src_dev, dst_dev,
+                                                                                      accumulate);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

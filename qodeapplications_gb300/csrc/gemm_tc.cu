@@ -112,6 +112,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __shared__ volatile int abort_sh;
     __shared__ int s_rowB[128], s_colB[128];
     __shared__ double s_DB[128];
+    // per-row metadata of the tile and the 32-column staging slice of the epilogue
+    __shared__ int64_t s_rbase[128], s_cbase[128];
+    __shared__ double s_DA[128];
+    __shared__ unsigned char s_diagA[128];
+    __shared__ float s_stage[128][33];
     __shared__ unsigned char s_diagB[128];
     constexpr int KCH = (KIND == 0) ? 64 : 32;          // elements of K per 128-byte chunk
     constexpr uint32_t FMT = (KIND == 0) ? 1u : 2u;
@@ -294,47 +299,57 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (tid == 0) atomicExch(status, XRH_ERR_TIMEOUT);
                 break;
             }
-            // FP64 epilogue (the column metadata is visible: the chunk barriers ordered it)
-            const int m = m0 + quarter * 32 + lane;
-            const bool row_ok = m < T.M;
-            int64_t rbase = 0, cbase = 0;
-            bool dA = false;
-            double DAm = 0.0;
-            if (row_ok) {
-                if (T.mode == 2) {
-                    rbase = T.rowA[m];
-                    cbase = T.colA[m];
-                    dA = T.diagA[m] != 0;
-                    DAm = T.DA ? T.DA[m] : 0.0;
-                } else {
-                    rbase = (int64_t)m * T.ldc;
+            // FP64 epilogue, one 32-column slice at a time: the 4 warps that hold the slice put it
+            // into shared memory (a row per lane), then every warp writes 16 rows with its lanes
+            // on consecutive columns, so that stores (and atomics) of a warp touch few cache
+            // lines.  Column metadata came with the chunk barriers; row metadata first:
+            for (int rr = tid; rr < TC_BM; rr += TC_EPI_THREADS) {
+                const int m = m0 + rr;
+                int64_t rb = 0, cb2 = 0;
+                unsigned char dgA = 0;
+                double dam = 0.0;
+                if (m < T.M) {
+                    if (T.mode == 2) {
+                        rb = T.rowA[m];
+                        cb2 = T.colA[m];
+                        dgA = T.diagA[m];
+                        dam = T.DA ? T.DA[m] : 0.0;
+                    } else {
+                        rb = (int64_t)m * T.ldc;
+                    }
                 }
+                s_rbase[rr] = rb;
+                s_cbase[rr] = cb2;
+                s_diagA[rr] = dgA;
+                s_DA[rr] = dam;
             }
             double* C = T.C;
 #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const int cc = half * 32 + 64 * i;
-                if (cc >= BN || !row_ok) continue;
-                if (T.mode == 2) {
+            for (int p = 0; p < 4; ++p) {
+                const int c0 = 32 * p;
+                if (c0 >= BN) break;                                   // uniform
+                if (half == (p & 1)) {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int jj = cc + j;
-                        if (n0 + jj < T.N) {
-                            double x = (double)acc[i][j];
-                            if (s_diagB[jj]) x += DAm;
-                            if (dA) x += s_DB[jj];
-                            C[(rbase + s_rowB[jj]) * T.ldc + cbase + s_colB[jj]] = x;
-                        }
-                    }
-                } else if (T.mode == 0) {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (n0 + cc + j < T.N) C[rbase + n0 + cc + j] = (double)acc[i][j];
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (n0 + cc + j < T.N) atomicAdd(C + rbase + n0 + cc + j, (double)acc[i][j]);
+                    for (int j = 0; j < 32; ++j) s_stage[quarter * 32 + lane][j] = acc[p >> 1][j];
                 }
+                epi_bar();
+                const int jj = c0 + lane;
+                const bool col_ok = n0 + jj < T.N;
+                for (int rr = warp * 16; rr < warp * 16 + 16; ++rr) {
+                    if (m0 + rr >= T.M) break;                         // uniform within the warp
+                    if (!col_ok) continue;
+                    double x = (double)s_stage[rr][lane];
+                    if (T.mode == 2) {
+                        if (s_diagB[jj]) x += s_DA[rr];
+                        if (s_diagA[rr]) x += s_DB[jj];
+                        C[(s_rbase[rr] + s_rowB[jj]) * T.ldc + s_cbase[rr] + s_colB[jj]] = x;
+                    } else if (T.mode == 0) {
+                        C[s_rbase[rr] + n0 + jj] = x;
+                    } else {
+                        atomicAdd(C + s_rbase[rr] + n0 + jj, x);
+                    }
+                }
+                epi_bar();                                             // slice consumed
             }
             epi_bar();          // metadata reads done before the next tile overwrites it
         }
@@ -348,25 +363,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // ---- operand split --------------------------------------------------------------------
+// One thread per group of 4 consecutive K elements of a row (one division per group), one
+// 8- or 16-byte store per group and part.
 template <int KIND>
 __global__ void split_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t ld, int64_t Kp,
                              void* __restrict__ hi, void* __restrict__ lo) {
-    const int64_t total = rows * Kp;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / Kp, k = i - r * Kp;
-        const double x = (k < K) ? src[r * ld + k] : 0.0;
-        if constexpr (KIND == 0) {
-            const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
-            const __nv_bfloat16 l = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
-            reinterpret_cast<__nv_bfloat16*>(hi)[i] = h;
-            reinterpret_cast<__nv_bfloat16*>(lo)[i] = l;
-        } else {
-            uint32_t h, l;
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
-            const double rem = x - (double)__uint_as_float(h);
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"((float)rem));
-            reinterpret_cast<uint32_t*>(hi)[i] = h;
-            reinterpret_cast<uint32_t*>(lo)[i] = l;
+    const int64_t groups = Kp >> 2;
+    const int64_t total = rows * groups;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / groups;
+        const int64_t k0 = (t - r * groups) * 4;
+        const double* srow = src + r * ld;
+        {
+            double x[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) x[t] = (k0 + t < K) ? __ldg(srow + k0 + t) : 0.0;
+            const int64_t o = r * Kp + k0;
+            if constexpr (KIND == 0) {
+                __nv_bfloat16 h[4], l[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    h[t] = __float2bfloat16_rn((float)x[t]);
+                    l[t] = __float2bfloat16_rn((float)(x[t] - (double)__bfloat162float(h[t])));
+                }
+                *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(hi) + o) = *reinterpret_cast<uint2*>(h);
+                *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(lo) + o) = *reinterpret_cast<uint2*>(l);
+            } else {
+                uint32_t h[4], l[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h[t]) : "f"((float)x[t]));
+                    const double rem = x[t] - (double)__uint_as_float(h[t]);
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l[t]) : "f"((float)rem));
+                }
+                *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(hi) + o) = make_uint4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(lo) + o) = make_uint4(l[0], l[1], l[2], l[3]);
+            }
         }
     }
 }
@@ -397,7 +429,9 @@ extern "C" int xrh_split_operand(int precision, const double* src_dev, int64_t r
     if (rows < 0 || K < 0 || ld < K || Kp < K || Kp % kch) return XRH_ERR_ARG;
     if (rows == 0 || Kp == 0) return XRH_OK;
     if (!src_dev || !hi_dev || !lo_dev) return XRH_ERR_ARG;
-    const int64_t total = rows * Kp;
+    // the hi / lo arrays are [rows, Kp] with Kp a multiple of 32 elements: 16-byte row starts
+    if ((reinterpret_cast<uintptr_t>(hi_dev) & 15) || (reinterpret_cast<uintptr_t>(lo_dev) & 15)) return XRH_ERR_ARG;
+    const int64_t total = rows * (Kp / 4);
     const int64_t blocks64 = (total + 255) / 256;
     const unsigned blocks = (unsigned)(blocks64 < 152 * 64 ? blocks64 : 152 * 64);
     if (precision == XRH_BF16X3)
