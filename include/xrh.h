@@ -223,6 +223,47 @@ int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double*
 int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
                       double* V_dev, double* alpha_dev, double* beta_dev, void* stream);
 
+/* The optimizer's state update for every (fragment, charge) block at once; replaces the
+ * per-fragment NumPy step of StateSpaceOptimizer/state_solver.py:207-453 (tangent
+ * projection, steepest-descent step, Loewdin orthonormalisation).  A block holds n <= 64
+ * row-orthonormal states z (n x K row-major), their gradient g = gT^T (+ gT32^T when gT32 is
+ * not NULL; gT, gT32 are K x n), a scratch zn (n x K) and three n x n matrices G, S, M.  Task t owns CTAs [cta_begin, cta_begin +
+ * xrh_state_ctas(K)).  In FP64 throughout:
+ *   xrh_gram_grouped(which=0): G += g z^T;   (which=1): S += zn zn^T   (G, S zeroed by the caller)
+ *   xrh_tangent_step:  zn = z - eps (g - 1/2 (G + G^T) z);  *sq_dev += |g - 1/2 (G + G^T) z|^2
+ *   xrh_inv_sqrt_small: M = S^-1/2 by `iters` coupled Newton-Schulz steps (n <= 32; one CTA
+ *                       per task, the tasks array indexed directly)
+ *   xrh_left_multiply:  z = M zn */
+typedef struct {
+    const double* gT;
+    const float* gT32;
+    double* z;
+    double* zn;
+    double* G;
+    double* S;
+    double* M;
+    int64_t K;
+    int32_t n;
+    int32_t reserved;
+    int64_t cta_begin;
+} xrh_state_task;
+
+int xrh_state_ctas(int64_t K);
+int xrh_gram_grouped(const xrh_state_task* tasks_dev, int n_tasks, int64_t total_ctas, int which,
+                     void* stream);
+int xrh_tangent_step(const xrh_state_task* tasks_dev, int n_tasks, int64_t total_ctas, double eps,
+                     double* sq_dev, void* stream);
+int xrh_inv_sqrt_small(const xrh_state_task* tasks_dev, int n_tasks, int iters, void* stream);
+int xrh_left_multiply(const xrh_state_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
+
+/* C (m x n, FP64, row-major, ld n) += alpha * A B^T for m, n <= 64 and long K: A (m x K, ld
+ * lda) and B (n x K, ld ldb) are double (XRH_FP64) or float (XRH_FP32: FP32 products summed in
+ * FP32 over 32 columns, then in FP64).  K is split over CTAs with FP64 atomic adds into C.
+ * The orbital-gradient contraction 4 V_(1) Gbar_(1)^T of the integral derivative
+ * (StateSpaceOptimizer/orb_grads.py, the two-electron term) is its main use. */
+int xrh_abt_small(int precision, int m, int n, int64_t K, const void* A_dev, int64_t lda,
+                  const void* B_dev, int64_t ldb, double alpha, double* C_dev, void* stream);
+
 /* Adjoint of the density build (dE/dz from dE/drho), the reverse of xrh_density_accumulate
  * over the same coupling lists; replaces the determinant-bra density rebuild plus second H
  * build of StateSpaceOptimizer/state_gradients.py:164-185.  gT_dev is dE/drho in

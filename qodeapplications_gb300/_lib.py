@@ -29,6 +29,12 @@ _SIGS = {
     "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "xrh_state_ctas": (_i32, [_i64]),
+    "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
+    "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),
+    "xrh_inv_sqrt_small": (_i32, [_vp, _i32, _i32, _vp]),
+    "xrh_left_multiply": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_abt_small": (_i32, [_i32, _i32, _i32, _i64, _vp, _i64, _vp, _i64, _dbl, _vp, _vp]),
     "xrh_pair_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "xrh_im_scatter": (_i32, [_i64, _vp, _vp, _vp, _vp, _vp, _i32, _i64, _i32, _vp, _vp, _vp]),
     "xrh_im_expand": (_i32, [_i32, _i32, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
@@ -146,6 +152,10 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+STATE_TASK_DTYPE = np.dtype([("gT", np.uint64), ("gT32", np.uint64), ("z", np.uint64), ("zn", np.uint64), ("G", np.uint64),
+                             ("S", np.uint64), ("M", np.uint64), ("K", np.int64), ("n", np.int32),
+                             ("reserved", np.int32), ("cta_begin", np.int64)])
+assert STATE_TASK_DTYPE.itemsize == 80
 TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
                        ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("C", np.uint64),
                        ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64), ("rowB", np.uint64),

@@ -449,6 +449,15 @@ class XRDimerAdjoint:
                      for c in self.plan.charges[m]} for m in (0, 1)]
         return [{c: self.G[("gzT", m, c)].t() for c in self.plan.charges[m]} for m in (0, 1)]
 
+    def state_gradient_parts(self):
+        """The persistent buffers the state gradient is summed from: [(m, charge, gT, gT32)]
+        with gT (n_conf x n, FP64) and gT32 (n_conf x n, FP32, or None): dE/dz = (gT + gT32)^T."""
+        out = []
+        for m in (0, 1):
+            for c in self.plan.charges[m]:
+                out.append((m, c, self.G[("gzT", m, c)], self.gz32[m][c] if self.prec32 else None))
+        return out
+
     def integral_gradients(self):
         """dE/dT, dE/dU, dE/dV as supersystem spin-orbital tensors (device)."""
         plan = self.plan
@@ -495,8 +504,24 @@ class XRDimerAdjoint:
         # orbitals), so dE/dV may be replaced by its projection on that symmetry; then the four
         # index positions of V' = R^T..R contribute equally: dE/dR = 4 V_(1) Gbar_(1)^T
         Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
-        Gbar = 0.125 * (Ga + Ga.permute(2, 3, 0, 1))
-        Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
+        # 4 V_(1) Gbar_(1)^T with Gbar = (Ga + Ga^(rs,pq)) / 8: a t x t result over t^3 terms,
+        # split over CTAs by xrh_abt_small (FP32 products on the split-precision paths)
+        if t <= 64:
+            Gso = Gso.contiguous()
+            K3 = t ** 3
+            if self.prec32:
+                B = torch.empty(V.shape, dtype=torch.float32, device=V.device)
+                torch.add(Ga, Ga.permute(2, 3, 0, 1), out=B)
+                A = V.to(torch.float32).contiguous()
+                prec = _lib.FP32
+            else:
+                B = Ga + Ga.permute(2, 3, 0, 1)
+                A = V.contiguous()
+                prec = _lib.FP64
+            call("xrh_abt_small", prec, t, t, K3, ptr(A), K3, ptr(B), K3, 0.5, ptr(Gso), stream_ptr())
+        else:
+            Gbar = 0.125 * (Ga + Ga.permute(2, 3, 0, 1))
+            Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
         key = (tuple(spatial_index), T.device)
         if key not in self._spatial_cache:     # built on first use, outside any graph capture
             n_sp = int(max(spatial_index)) + 1

@@ -11,7 +11,8 @@ and H with bra_det/ket_det densities, state_gradients.py:144-185) is done here a
   3. the reverse pass (XRDimerAdjoint): dE/dz of both fragments, projected on the tangent
      space of the orthonormal states, and dE/dkappa of the orbital rotations;
   4. a steepest-descent step on the states followed by Loewdin orthonormalisation
-     (z <- (z z^T)^-1/2 z, the inverse square root by Newton-Schulz iterations, FP64).
+     (z <- (z z^T)^-1/2 z, the inverse square root by Newton-Schulz iterations, FP64), for
+     all (fragment, charge) blocks at once in five grouped launches (StateStepper).
 
 Steps 1-2 and 3-4 are each replayed as a CUDA graph; between them the host solves the
 m x m tridiagonal Lanczos matrix (one small device-to-host copy).
@@ -19,9 +20,11 @@ m x m tridiagonal Lanczos matrix (one small device-to-host copy).
 import numpy as np
 import torch
 
+from . import _lib
+from ._lib import call, ptr, stream_ptr
 from .densities import FragmentSpace
 from .eigen import Lanczos
-from .gradients import XRDimerAdjoint, tangent_project
+from .gradients import XRDimerAdjoint
 from .hamiltonian import DeviceIntegrals, XRDimerPlan
 from .synthetic import spin_orbital_spatial_index
 
@@ -39,27 +42,80 @@ def _inv_sqrt_newton_schulz(S, iters=6):
     return Z
 
 
-def _step_and_orthonormalise(coeffs, grads, step):
-    """z <- (z' z'^T)^-1/2 z' with z' = z - step * (tangent part of g), for every (fragment,
-    charge) block; the n x n inverse square roots of blocks with equal n run as one batch.
-    Returns the squared norm of the tangent gradient (device scalar)."""
-    sq = None
-    znew, S = [], []
-    for z, g in zip(coeffs, grads):
-        gt = tangent_project(g, z)
-        part = (gt * gt).sum()
-        sq = part if sq is None else sq + part
-        zn = z - step * gt
-        znew.append(zn)
-        S.append(zn @ zn.t())
-    by_n = {}
-    for i, Si in enumerate(S):
-        by_n.setdefault(Si.shape[0], []).append(i)
-    for n, ids in by_n.items():
-        Z = _inv_sqrt_newton_schulz(torch.stack([S[i] for i in ids]))
-        for k, i in enumerate(ids):
-            coeffs[i].copy_(Z[k] @ znew[i])
-    return sq
+NS_ITERS = 6
+
+
+class StateStepper:
+    """The state update z <- (z' z'^T)^-1/2 z', z' = z - step * (tangent part of dE/dz), over
+    every (fragment, charge) block in grouped FP64 launches: G = g z^T, the tangent step with
+    its squared norm, S = z' z'^T, M = S^-1/2 (Newton-Schulz; one CTA per block for n <= 32,
+    batched torch matmuls above), z = M z'.  coeffs[i] is the n x K state block (updated in
+    place); grads[i] = (gT, gT32) with dE/dz = (gT + gT32)^T, gT32 None or FP32, both K x n.
+    All buffers are persistent, so launch() may be captured in a CUDA graph."""
+
+    def __init__(self, coeffs, grads, step):
+        self.coeffs = coeffs
+        self.step = float(step)
+        dev = coeffs[0].device
+        nb = len(coeffs)
+        ns = [int(z.shape[0]) for z in coeffs]
+        for z, (gT, gT32) in zip(coeffs, grads):
+            n, K = z.shape
+            if z.dtype != torch.float64 or not z.is_contiguous() or n > 64:
+                raise ValueError("state blocks must be contiguous FP64 with at most 64 states")
+            if gT.shape != (K, n) or gT.dtype != torch.float64 or not gT.is_contiguous():
+                raise ValueError("gradient block must be a contiguous FP64 (n_conf x n) array")
+            if gT32 is not None and (gT32.shape != (K, n) or gT32.dtype != torch.float32 or not gT32.is_contiguous()):
+                raise ValueError("FP32 gradient part must be a contiguous (n_conf x n) array")
+        self.zn = [torch.empty_like(z) for z in coeffs]
+        sq = [n * n for n in ns]
+        # G and S of every block and the squared norm are zeroed together before each step
+        self.zeroed = torch.zeros(2 * sum(sq) + 1, dtype=torch.float64, device=dev)
+        self.M = torch.zeros(sum(sq), dtype=torch.float64, device=dev)
+        self.sq = self.zeroed[-1:]
+        tasks = np.zeros(nb, dtype=_lib.STATE_TASK_DTYPE)
+        off, cta = 0, 0
+        self.S_views, self.M_views = [], []
+        for i, (z, (gT, gT32)) in enumerate(zip(coeffs, grads)):
+            n, K = z.shape
+            G = self.zeroed[off:off + n * n]
+            S = self.zeroed[sum(sq) + off:sum(sq) + off + n * n]
+            M = self.M[off:off + n * n]
+            self.S_views.append(S.view(n, n))
+            self.M_views.append(M.view(n, n))
+            t = tasks[i]
+            t["gT"], t["gT32"] = gT.data_ptr(), (gT32.data_ptr() if gT32 is not None else 0)
+            t["z"], t["zn"] = z.data_ptr(), self.zn[i].data_ptr()
+            t["G"], t["S"], t["M"] = G.data_ptr(), S.data_ptr(), M.data_ptr()
+            t["K"], t["n"], t["cta_begin"] = K, n, cta
+            cta += int(_lib.lib().xrh_state_ctas(K))
+            off += n * n
+        self.total_ctas = cta
+        self.n_tasks = nb
+        self.tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
+        self.small_ns = max(ns) <= 32
+        by_n = {}
+        for i, n in enumerate(ns):
+            by_n.setdefault(n, []).append(i)
+        self.by_n = by_n
+
+    def launch(self):
+        """One step on the current stream; returns the squared tangent-gradient norm (device)."""
+        s = stream_ptr()
+        tp = ptr(self.tasks)
+        self.zeroed.zero_()
+        call("xrh_gram_grouped", tp, self.n_tasks, self.total_ctas, 0, s)
+        call("xrh_tangent_step", tp, self.n_tasks, self.total_ctas, self.step, ptr(self.sq), s)
+        call("xrh_gram_grouped", tp, self.n_tasks, self.total_ctas, 1, s)
+        if self.small_ns:
+            call("xrh_inv_sqrt_small", tp, self.n_tasks, NS_ITERS, s)
+        else:
+            for n, ids in self.by_n.items():
+                Z = _inv_sqrt_newton_schulz(torch.stack([self.S_views[i] for i in ids]), NS_ITERS)
+                for k, i in enumerate(ids):
+                    self.M_views[i].copy_(Z[k])
+        call("xrh_left_multiply", tp, self.n_tasks, self.total_ctas, s)
+        return self.sq[0]
 
 
 class XRStateOptimizer:
@@ -81,6 +137,9 @@ class XRStateOptimizer:
             for c in chg:
                 self.plan.coeffs[m][c].copy_(torch.as_tensor(sysd["states"][m][c][0], device=dev))
         self.step_size = step
+        parts = self.adj.state_gradient_parts()
+        self.stepper = StateStepper([self.plan.coeffs[m][c] for m, c, _, _ in parts],
+                                    [(gT, gT32) for _, _, gT, gT32 in parts], step)
         self.lz = {t: Lanczos(sec["dim"], m=lanczos_m, device=dev) for t, sec in self.plan.sectors.items()}
         self.lz_warm = {t: Lanczos(sec["dim"], m=warm_m, device=dev) for t, sec in self.plan.sectors.items()}
         self.target = None
@@ -114,10 +173,7 @@ class XRStateOptimizer:
         # the warm start of the next iteration
         self.lz_warm[t].v0.copy_(d)
         self.adj.launch(self.d_product)
-        g = self.adj.state_gradient()
-        keys = [(m, c) for m in range(2) for c in self.charges]
-        self._gsq = _step_and_orthonormalise([self.plan.coeffs[m][c] for m, c in keys], [g[m][c] for m, c in keys],
-                                             self.step_size)
+        self._gsq = self.stepper.launch()
         if self.orbital:
             self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
 
@@ -204,10 +260,7 @@ class XRStateOptimizer:
         self.d_product.index_copy_(0, self.plan.sectors[t]["rows"], d)
         lz.v0.copy_(d)
         self.adj.launch(self.d_product)
-        g = self.adj.state_gradient()
-        keys = [(m, c) for m in range(2) for c in self.charges]
-        self._gsq = _step_and_orthonormalise([self.plan.coeffs[m][c] for m, c in keys], [g[m][c] for m, c in keys],
-                                             self.step_size)
+        self._gsq = self.stepper.launch()
         if self.orbital:
             self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
 
