@@ -223,6 +223,18 @@ int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double*
 int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
                       double* V_dev, double* alpha_dev, double* beta_dev, void* stream);
 
+/* The same Krylov loop for any n as ONE cooperative launch (cudaLaunchCooperativeKernel):
+ * the CTAs (about 4 rows of H each, at most one per SM) split the rows of H, V and w and meet
+ * at four grid barriers per step; cross-CTA sums run in a fixed CTA order, so results do not
+ * depend on scheduling.  work_dev holds xrh_lanczos_coop_work(m) doubles of scratch (partial
+ * sums and the barrier words, reset by this call).  A barrier wait that exceeds its poll
+ * limit sets *status_dev = XRH_ERR_TIMEOUT and the kernel returns early; *status_dev must be
+ * XRH_OK on entry. */
+int64_t xrh_lanczos_coop_work(int m);
+int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                     double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                     int64_t work_len, int32_t* status_dev, void* stream);
+
 /* The optimizer's state update for every (fragment, charge) block at once; replaces the
  * per-fragment NumPy step of StateSpaceOptimizer/state_solver.py:207-453 (tangent
  * projection, steepest-descent step, Loewdin orthonormalisation).  A block holds n <= 64

@@ -29,6 +29,8 @@ _SIGS = {
     "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "xrh_lanczos_coop_work": (_i64, [_i32]),
+    "xrh_lanczos_coop": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "xrh_state_ctas": (_i32, [_i64]),
     "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
     "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),

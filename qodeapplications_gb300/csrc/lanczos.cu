@@ -128,6 +128,161 @@ __global__ void __launch_bounds__(1024) lanczos_small_kernel(int n, int m, const
     }
 }
 
+
+// ---- the Krylov loop over many CTAs (cooperative launch) ----------------------------------
+// The FP64 rate of one SM bounds the single-CTA loop; here the rows of H, V and w are split
+// over the CTAs of one cooperative launch and every step takes three grid barriers:
+//   w_R = H_R V[j]; partial dots V[i]_R . w_R (i <= j)                     | barrier
+//   c = sum over CTAs; w_R -= c V_R; partial dots again and partial |w_R|^2 | barrier
+//   c' = sum; w_R -= c' V_R; beta^2 = |w|^2 - |c'|^2; V[j+1]_R = w_R/beta  | barrier
+// (after the first pass w is orthogonal to V[0..j] up to rounding, so the second pass removes
+// only |c'| ~ 1e-16 |w| and beta^2 = |w|^2 - |c'|^2 is the norm after it to that accuracy).
+// The CTA keeps its own rows of every V[i] in shared memory and stages V[j] whole before the
+// product, so the only global traffic per step is H_R, V[j] and the partial sums.  Partial
+// sums are reduced by warps in a fixed order, identical in every CTA, so all CTAs hold the same
+// coefficients and results do not depend on scheduling.  V is written by every CTA and read
+// by all, so its global reads bypass L1 (ld.global.cg).  Barrier k waits until a counter
+// reaches (k+1) * gridDim.x; a wait that exceeds LC_WAIT_LIMIT polls sets XRH_ERR_TIMEOUT in
+// *status and the CTA returns.
+constexpr int LC_THREADS = 256;
+constexpr int LC_WARPS = LC_THREADS / 32;
+constexpr int LC_MAX_CTAS = 256;
+constexpr int LC_ROWS_PER_CTA = 4;
+constexpr long long LC_WAIT_LIMIT = 1LL << 22;   // ~ seconds of polls
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Returns false (all threads of the CTA) when the wait gave up or another CTA already failed.
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, int32_t* status) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        atomicAdd(count, 1u);
+        long long it = 0;
+        while (ld_acquire_u32(count) < target) {
+            if (++it > LC_WAIT_LIMIT) { ok = 0; break; }
+            __nanosleep(20);
+        }
+        if (!ok) atomicExch(status, XRH_ERR_TIMEOUT);
+        if (ok && *(volatile int32_t*)status != XRH_OK) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// c[i] = sum_q part[i * nb + q] for i < cnt, warp per i, lanes over q, fixed shuffle tree.
+__device__ __forceinline__ void reduce_partials(const double* __restrict__ part, unsigned int nb, int cnt,
+                                                double* __restrict__ c) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = warp; i < cnt; i += LC_WARPS) {
+        double s = 0.0;
+        for (unsigned int q = lane; q < nb; q += 32) s += __ldcg(part + (int64_t)i * nb + q);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) c[i] = s;
+    }
+}
+
+// Dynamic shared memory: Vs [(m + 1) * rows_max] (own rows of V), w [rows_max], c [m + 2],
+// then, when stage_v, v [n] (V[j] whole).
+__global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int m, const double* __restrict__ H,
+                                                                int64_t ld, const double* __restrict__ v0,
+                                                                double* __restrict__ V, double* __restrict__ alpha,
+                                                                double* __restrict__ beta, double* __restrict__ part,
+                                                                unsigned int* count, int32_t* status, int rows_max,
+                                                                int stage_v) {
+    extern __shared__ double sm[];
+    const unsigned int nb = gridDim.x, b = blockIdx.x;
+    const int64_t r0 = (int64_t)b * n / nb, r1 = (int64_t)(b + 1) * n / nb;
+    const int nr = (int)(r1 - r0);
+    const int ms = m + 2;
+    double* Vs = sm;                                  // [m + 1][rows_max]
+    double* w = Vs + (int64_t)(m + 1) * rows_max;     // [rows_max]
+    double* c = w + rows_max;                         // [m + 2]
+    double* vst = c + ms;                             // [n] when stage_v
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double* p1 = part;                                // [m + 2][nb]: pass-1 dots
+    double* p2 = part + (int64_t)ms * nb;             // [m + 2][nb]: pass-2 dots, then |w|^2 at row j + 1
+    unsigned int bar = 0;
+    for (int r = tid; r < nr; r += LC_THREADS) {
+        const double x = v0[r0 + r];
+        V[r0 + r] = x;
+        Vs[r] = x;
+    }
+    if (!grid_barrier(count, ++bar * nb, status)) return;
+    for (int j = 0; j < m; ++j) {
+        const double* vj = V + (int64_t)j * n;
+        if (stage_v) {
+            for (int64_t k = tid; k < n; k += LC_THREADS) vst[k] = __ldcg(vj + k);
+            __syncthreads();
+        }
+        for (int r = warp; r < nr; r += LC_WARPS) {
+            const double* h = H + (r0 + r) * ld;
+            double s = 0.0;
+            if (stage_v)
+                for (int64_t k = lane; k < n; k += 32) s = fma(h[k], vst[k], s);
+            else
+                for (int64_t k = lane; k < n; k += 32) s = fma(h[k], __ldcg(vj + k), s);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) w[r] = s;
+        }
+        double a = 0.0;
+        double cc2 = 0.0;
+        for (int pass = 0; pass < 2; ++pass) {
+            double* pp = pass == 0 ? p1 : p2;
+            __syncthreads();
+            // partial dots of w_R with V[i]_R (i <= j), and after pass 1 also |w_R|^2 (row j + 1)
+            const int cnt = j + 1 + pass;
+            for (int i = warp; i < cnt; i += LC_WARPS) {
+                const double* vi = Vs + (int64_t)i * rows_max;
+                double s = 0.0;
+                if (i <= j)
+                    for (int r = lane; r < nr; r += 32) s = fma(vi[r], w[r], s);
+                else
+                    for (int r = lane; r < nr; r += 32) s = fma(w[r], w[r], s);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) pp[(int64_t)i * nb + b] = s;
+            }
+            if (!grid_barrier(count, ++bar * nb, status)) return;
+            reduce_partials(pp, nb, cnt, c);
+            __syncthreads();
+            a += c[j];
+            for (int r = tid; r < nr; r += LC_THREADS) {
+                double s = 0.0;
+                for (int i = 0; i <= j; ++i) s = fma(c[i], Vs[(int64_t)i * rows_max + r], s);
+                w[r] -= s;
+            }
+            if (pass == 1) {
+                for (int i = 0; i <= j; ++i) cc2 = fma(c[i], c[i], cc2);
+                cc2 = c[j + 1] - cc2;          // |w after pass 2|^2
+            }
+        }
+        const double bj = sqrt(cc2 > 0.0 ? cc2 : 0.0);
+        const double inv = bj > 0.0 ? 1.0 / bj : 0.0;
+        double* vn = V + (int64_t)(j + 1) * n + r0;
+        double* vsn = Vs + (int64_t)(j + 1) * rows_max;
+        for (int r = tid; r < nr; r += LC_THREADS) {
+            const double x = w[r] * inv;
+            vn[r] = x;
+            vsn[r] = x;
+        }
+        if (b == 0 && tid == 0) {
+            alpha[j] = a;
+            beta[j] = bj;
+        }
+        if (!grid_barrier(count, ++bar * nb, status)) return;
+    }
+}
+
 }  // namespace
 
 extern "C" int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
@@ -168,5 +323,60 @@ extern "C" int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_d
     if (n <= 0 || !w_dev || !v_dev || !beta_dev) return XRH_ERR_ARG;
     normalize_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(n, w_dev, v_dev, beta_dev);
     XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+// Scratch (in doubles) of xrh_lanczos_coop for m steps: partial sums of up to LC_MAX_CTAS
+// CTAs plus the barrier counter.
+extern "C" int64_t xrh_lanczos_coop_work(int m) {
+    if (m <= 0) return -1;
+    return (int64_t)LC_MAX_CTAS * 2 * (int64_t)(m + 2) + 2;
+}
+
+extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                                double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                                int64_t work_len, int32_t* status_dev, void* stream) {
+    if (n <= 0 || m <= 0 || ld < n) return XRH_ERR_ARG;
+    if (!H_dev || !v0_dev || !V_dev || !alpha_dev || !beta_dev || !work_dev || !status_dev) return XRH_ERR_ARG;
+    if (work_len < xrh_lanczos_coop_work(m)) return XRH_ERR_CAPACITY;
+    int dev = 0, sms = 0, per_sm = 0, smem_optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return XRH_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return XRH_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return XRH_ERR_CUDA;
+    int64_t nb = (n + LC_ROWS_PER_CTA - 1) / LC_ROWS_PER_CTA;
+    if (nb > sms) nb = sms;
+    if (nb > LC_MAX_CTAS) nb = LC_MAX_CTAS;
+    const int64_t rows_max = (n + nb - 1) / nb;
+    const size_t base = sizeof(double) * ((size_t)(m + 1) * rows_max + rows_max + (size_t)m + 2);
+    if (base > (size_t)smem_optin) return XRH_ERR_CAPACITY;
+    const int stage_v = base + sizeof(double) * (size_t)n <= (size_t)smem_optin ? 1 : 0;
+    const size_t smem = base + (stage_v ? sizeof(double) * (size_t)n : 0);
+    // raise the kernel's dynamic shared-memory limit once per larger size (set before any
+    // capture by the first, eager call)
+    static size_t smem_set = 48 * 1024;
+    if (smem > smem_set) {
+        if (cudaFuncSetAttribute(lanczos_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return XRH_ERR_CUDA;
+        smem_set = smem;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_coop_kernel, LC_THREADS, smem) != cudaSuccess)
+        return XRH_ERR_CUDA;
+    if ((int64_t)per_sm * sms < nb) return XRH_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* part = work_dev;
+    unsigned int* count = reinterpret_cast<unsigned int*>(work_dev + (int64_t)LC_MAX_CTAS * 2 * (int64_t)(m + 2));
+    if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return XRH_ERR_CUDA;
+    int64_t n_arg = n, ld_arg = ld;
+    int m_arg = m, rows_arg = (int)rows_max, stage_arg = stage_v;
+    void* args[] = {&n_arg, &m_arg, (void*)&H_dev, &ld_arg, (void*)&v0_dev, (void*)&V_dev, (void*)&alpha_dev,
+                    (void*)&beta_dev, (void*)&part, (void*)&count, (void*)&status_dev, &rows_arg, &stage_arg};
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_coop_kernel, dim3((unsigned)nb),
+                                                      dim3(LC_THREADS), args, smem, s);
+    if (e != cudaSuccess) {
+        xrh_set_last_cuda_error((int)e);
+        return XRH_ERR_CUDA;
+    }
     return XRH_OK;
 }

@@ -6,6 +6,10 @@ lowest eigenvalues and the ground-state eigenvector.  The Krylov loop (H x v, tw
 classical Gram-Schmidt against all previous vectors, normalisation) runs entirely on the
 device with fixed shapes, so it can be captured in a CUDA graph; only the small tridiagonal
 eigenproblem (m x m) is solved on the host.
+
+The default loop ("coop") is one cooperative launch whose CTAs split the rows of H and meet at
+four grid barriers per step (the FP64 rate of one SM would otherwise bound it); "small" is
+the one-CTA loop and "steps" six launches per step, kept as cross-checks.
 """
 import numpy as np
 import torch
@@ -13,10 +17,11 @@ import torch
 from ._lib import call, ptr, stream_ptr
 
 SMALL_SECTOR = 2048
+MODES = ("coop", "small", "steps")
 
 
 class Lanczos:
-    def __init__(self, n, m=96, device="cuda", seed=7):
+    def __init__(self, n, m=96, device="cuda", seed=7, mode="coop"):
         self.n = int(n)
         self.m = int(min(m, n))
         dev = torch.device(device)
@@ -33,15 +38,28 @@ class Lanczos:
         self.vec = torch.zeros(self.n, **f64)
         self.ab = torch.zeros(2 * self.m, **f64)          # alpha_j, beta_j
         self._host = torch.empty(3 * self.m, dtype=torch.float64).pin_memory() if torch.cuda.is_available() else None
-        # sectors up to this size run the whole Krylov loop in one launch
-        self.small = self.n <= SMALL_SECTOR
+        if mode not in MODES:
+            raise ValueError(f"mode must be one of {MODES}")
+        if mode == "small" and self.n > SMALL_SECTOR:
+            mode = "steps"
+        self.mode = mode
+        self.small = mode != "steps"      # alpha/beta written straight into self.ab
+        if mode == "coop":
+            from ._lib import lib
+            self.work = torch.zeros(int(lib().xrh_lanczos_coop_work(self.m)), **f64)
+            self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+            self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory() if torch.cuda.is_available() else None
 
     def krylov(self, H, ld=None):
         """Device-only part: m Lanczos steps on H (n x n, row stride ld)."""
         s = stream_ptr()
         n, m = self.n, self.m
         ld = n if ld is None else ld
-        if self.small:
+        if self.mode == "coop":
+            call("xrh_lanczos_coop", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab), ptr(self.ab[m:]),
+                 ptr(self.work), self.work.numel(), ptr(self.status), s)
+            return
+        if self.mode == "small":
             call("xrh_lanczos_small", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab),
                  ptr(self.ab[m:]), s)
             return
@@ -61,12 +79,18 @@ class Lanczos:
             self.ab[:m].copy_(self.CC[idx, idx] + self.CC2[idx, idx])
             self.ab[m:].copy_(self.beta)
         self._host[:2 * m].copy_(self.ab, non_blocking=True)
+        if self.mode == "coop":
+            self._host_status.copy_(self.status, non_blocking=True)
 
     def solve(self, k=5):
         """Host part (after a sync): eigenpairs of the m x m tridiagonal matrix.
         Returns (lowest k Ritz values, residual norm estimate of the lowest)."""
         from scipy.linalg import eigh_tridiagonal
         m = self.m
+        if self.mode == "coop" and int(self._host_status[0]) != 0:
+            from ._lib import lib
+            code = int(self._host_status[0])
+            raise RuntimeError(f"xrh_lanczos_coop: {lib().xrh_status_string(code).decode()}")
         a = self._host[:m].numpy().copy()
         b = self._host[m:2 * m].numpy().copy()
         # stop at an invariant subspace (tiny beta): the rest of the basis is meaningless
