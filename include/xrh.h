@@ -107,6 +107,21 @@ typedef struct {
 int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
                                        int max_nb, int max_nk, void* stream);
 
+/* Same product for blocks of few states (n_b * ceil(n_k / 4) <= max_pairs <= 128), one warp
+ * per unit: unit u covers couplings [idx_ptr[idx] + c_lo, idx_ptr[idx] + c_hi) of operator
+ * index idx of task `task` (cta_begin and splits of the tasks are not used).  A unit with
+ * c_lo = 0 and c_hi = the index's coupling count stores rhoT[idx] (an index with no
+ * couplings needs such a unit, it writes zeros); the units of an index split into several
+ * ranges ADD atomically, so the rhoT of their tasks must be zeroed by the caller. */
+typedef struct {
+    int32_t task;
+    int32_t idx;
+    int32_t c_lo, c_hi;
+} xrh_dens_unit;   /* 16 bytes */
+int xrh_density_accumulate_f32_units(const xrh_dens_task* tasks_dev, int n_tasks,
+                                     const xrh_dens_unit* units_dev, int64_t n_units, int max_pairs,
+                                     void* stream);
+
 /* Allocation-free transition densities (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- for example code running
  * inside another application's CUDA context whose allocator owns all device memory, or a

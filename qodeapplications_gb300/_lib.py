@@ -25,6 +25,7 @@ _i32, _i64, _vp, _dbl = ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes
 _SIGS = {
     "xrh_abi_version": (_i32, []),
     "xrh_density_accumulate_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
+    "xrh_density_accumulate_f32_units": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
     "xrh_density_adjoint_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
     "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
@@ -154,6 +155,8 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+DENS_UNIT_DTYPE = np.dtype([("task", np.int32), ("idx", np.int32), ("c_lo", np.int32), ("c_hi", np.int32)])
+assert DENS_UNIT_DTYPE.itemsize == 16
 STATE_TASK_DTYPE = np.dtype([("gT", np.uint64), ("gT32", np.uint64), ("z", np.uint64), ("zn", np.uint64), ("G", np.uint64),
                              ("S", np.uint64), ("M", np.uint64), ("K", np.int64), ("n", np.int32),
                              ("reserved", np.int32), ("cta_begin", np.int64)])

@@ -31,5 +31,6 @@ static_assert(sizeof(xrh_tc_segment) == 32, "xrh_tc_segment layout is part of th
 static_assert(sizeof(xrh_dens_task) == 88, "xrh_dens_task layout is part of the ABI");
 static_assert(sizeof(xrh_dens_adj_task) == 96, "xrh_dens_adj_task layout is part of the ABI");
 static_assert(sizeof(xrh_dens_adj_tc_task) == 112, "xrh_dens_adj_tc_task layout is part of the ABI");
+static_assert(sizeof(xrh_dens_unit) == 16, "xrh_dens_unit layout is part of the ABI");
 static_assert(sizeof(xrh_state_task) == 80, "xrh_state_task layout is part of the ABI");
 static_assert(sizeof(xrh_tc_task) == 144, "xrh_tc_task layout is part of the ABI");

@@ -513,6 +513,109 @@ __global__ void __launch_bounds__(kAccThreads) density_acc_f32_grouped_kernel(co
                      T.nk, T.rhoT, T.splits, smem_raw);
 }
 
+
+// ---- small blocks: one warp per coupling range ----------------------------------------------
+// For blocks with n_b * ceil(n_k / 4) <= 32 R output quads, a CTA per operator index leaves
+// most threads idle and pays three barriers per chunk.  Here a warp owns one unit (an
+// operator index, or a range of at most a few hundred of its couplings): lane l holds the
+// quads (I, 4 jq .. 4 jq + 3) with I * ceil(n_k/4) + jq = l + 32 r, r < R.  The warp reads 32
+// couplings at a time (one per lane, coalesced), then broadcasts each (P with the sign packed
+// in, Q) by shuffle; every lane loads zb[P][I] and the float4 zk[Q][4 jq..] (L1/L2 gathers)
+// and does four FMAs.  FP32 partial sums over each 32 couplings, FP64 running sums.  Units
+// covering a whole index store rhoT[idx] directly; units of a split index add atomically
+// (rhoT zeroed by the caller).
+template <int R>
+__global__ void __launch_bounds__(256) density_f32_units_kernel(const xrh_dens_task* __restrict__ tasks,
+                                                               const xrh_dens_unit* __restrict__ units,
+                                                               int64_t n_units) {
+    const int lane = threadIdx.x & 31;
+    const int64_t u = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (u >= n_units) return;
+    const xrh_dens_unit U = units[u];
+    const xrh_dens_task& T = tasks[U.task];
+    const int nb = T.nb, nk = T.nk;
+    const int nkq = (nk + 3) >> 2, nkp = nkq * 4, nbp = (nb + 3) & ~3;
+    const int pairs = nb * nkq;
+    if (pairs > 32 * R) return;                      // the host never builds such a unit
+    const int64_t base = T.idx_ptr[U.idx];
+    const int64_t len = T.idx_ptr[U.idx + 1] - base;
+    const int64_t c_lo = base + U.c_lo, c_hi = base + U.c_hi;
+    const bool whole = U.c_lo == 0 && (int64_t)U.c_hi == len;
+    int Iu[R], jq[R];
+    bool act[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int pr = lane + 32 * r;
+        act[r] = pr < pairs;
+        Iu[r] = act[r] ? pr / nkq : 0;
+        jq[r] = act[r] ? pr - (pr / nkq) * nkq : 0;
+    }
+    double acc[R][4];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[r][k] = 0.0;
+    const float* __restrict__ zb = T.zb32;
+    const float* __restrict__ zk = T.zk32;
+    for (int64_t c0 = c_lo; c0 < c_hi; c0 += 32) {
+        const int64_t c = c0 + lane;
+        int ps = 0, q = 0;                           // padding couplings: row 0 times a zero sign
+        float pad = 0.f;
+        if (c < c_hi) {
+            const int p = T.P[c];
+            q = T.Q[c];
+            ps = T.sign[c] < 0 ? ~p : p;
+            pad = 1.f;
+        }
+        const int cnt = (int)((c_hi - c0) < 32 ? (c_hi - c0) : 32);
+        const int cnt4 = (cnt + 3) & ~3;
+        float part[R][4];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) part[r][k] = 0.f;
+        for (int t = 0; t < cnt4; t += 4) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int pst = __shfl_sync(0xffffffffu, ps, t + e);
+                const int qt = __shfl_sync(0xffffffffu, q, t + e);
+                const float live = __shfl_sync(0xffffffffu, pad, t + e);
+                const int pt = pst < 0 ? ~pst : pst;
+                const float st = pst < 0 ? -live : live;
+                const float* zbr = zb + (int64_t)pt * nbp;
+                const float4* zkr = reinterpret_cast<const float4*>(zk + (int64_t)qt * nkp);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (act[r]) {
+                        const float a = st * __ldg(zbr + Iu[r]);
+                        const float4 b4 = __ldg(zkr + jq[r]);
+                        part[r][0] = fmaf(a, b4.x, part[r][0]);
+                        part[r][1] = fmaf(a, b4.y, part[r][1]);
+                        part[r][2] = fmaf(a, b4.z, part[r][2]);
+                        part[r][3] = fmaf(a, b4.w, part[r][3]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[r][k] += (double)part[r][k];
+    }
+    double* out = T.rhoT + (int64_t)U.idx * nb * nk;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (!act[r]) continue;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int J = 4 * jq[r] + k;
+            if (J >= nk) continue;
+            double* o = out + (int64_t)Iu[r] * nk + J;
+            if (whole) *o = acc[r][k];
+            else atomicAdd(o, acc[r][k]);
+        }
+    }
+}
 }  // namespace
 
 extern "C" int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
@@ -547,6 +650,27 @@ extern "C" int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* 
     density_acc_f32_kernel<<<grid, kAccThreads, smem, (cudaStream_t)stream>>>(idx_ptr_dev, P_dev, Q_dev, sign_dev,
                                                                              zb32_dev, n_b, zk32_dev, n_k, rhoT_dev,
                                                                              splits);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_density_accumulate_f32_units(const xrh_dens_task* tasks_dev, int n_tasks,
+                                                const xrh_dens_unit* units_dev, int64_t n_units, int max_pairs,
+                                                void* stream) {
+    if (n_tasks < 0 || n_units < 0 || max_pairs <= 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || n_units == 0) return XRH_OK;
+    if (!tasks_dev || !units_dev) return XRH_ERR_ARG;
+    const int64_t ctas = (n_units + 7) / 8;
+    if (ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (max_pairs <= 32)
+        density_f32_units_kernel<1><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
+    else if (max_pairs <= 64)
+        density_f32_units_kernel<2><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
+    else if (max_pairs <= 128)
+        density_f32_units_kernel<4><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
+    else
+        return XRH_ERR_CAPACITY;
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -231,6 +231,28 @@ def mirror_pairs(space):
     return out
 
 
+UNIT_MAX_PAIRS = 128     # n_b * ceil(n_k / 4) up to which a block takes the warp-per-unit kernel
+UNIT_COUPLINGS = 256     # couplings per unit at most
+
+
+def _coupling_units(cp):
+    """Unit table of one coupling list for xrh_density_accumulate_f32_units: every operator
+    index as one unit, or as ranges of at most UNIT_COUPLINGS couplings.  Returns (units,
+    any index split)."""
+    ip = cp.idx_ptr.cpu().numpy().astype(np.int64)
+    lens = np.diff(ip)
+    nu = np.maximum(1, (lens + UNIT_COUPLINGS - 1) // UNIT_COUPLINGS)
+    total = int(nu.sum())
+    units = np.zeros(total, dtype=_lib.DENS_UNIT_DTYPE)
+    idx = np.repeat(np.arange(len(lens), dtype=np.int64), nu)
+    first = np.repeat(np.cumsum(nu) - nu, nu)
+    part = np.arange(total, dtype=np.int64) - first
+    units["idx"] = idx
+    units["c_lo"] = part * UNIT_COUPLINGS
+    units["c_hi"] = np.minimum((part + 1) * UNIT_COUPLINGS, lens[idx])
+    return units, bool((nu > 1).any())
+
+
 class DensityBuilder:
     """Preallocated, reusable density build for one fragment and fixed state counts.
 
@@ -251,17 +273,36 @@ class DensityBuilder:
         dev = space.device
         self.rho = {}
         self._tmp = {}
+        # FP32 path: blocks with few states (nb * ceil(nk / 4) <= 128) go to the warp-per-unit
+        # kernel; units of split operator indices add atomically into a zeroed arena
+        self.f32 = self.precision == _lib.FP32
+        self._unit_keys = set()
+        if self.f32:
+            self._unit_keys = {key for key in space.couplings if key not in self.mirror and
+                               self.n_states_bra[key[1]] * ((self.n_states[key[2]] + 3) // 4) <= UNIT_MAX_PAIRS}
+        unit_units, split_keys = {}, []
+        for key in sorted(self._unit_keys, key=str):
+            cp = space.couplings[key]
+            unit_units[key] = _coupling_units(cp)
+            if unit_units[key][1]:
+                split_keys.append(key)
+        arena_n = sum(space.couplings[k].K * self.n_states_bra[k[1]] * self.n_states[k[2]] for k in split_keys)
+        self._unit_zero = torch.zeros(arena_n, dtype=torch.float64, device=dev) if arena_n else None
+        arena_off = 0
         for (op, bc, kc), cp in space.couplings.items():
             nb, nk = self.n_states_bra[bc], self.n_states[kc]
             shape = (nb, nk) + (space.N,) * len(op)
             self.rho.setdefault(op, {})[(bc, kc)] = torch.empty(shape, dtype=torch.float64, device=dev)
-            self._tmp[(op, bc, kc)] = torch.empty(cp.K * nb * nk, dtype=torch.float64, device=dev)
+            if (op, bc, kc) in split_keys:
+                self._tmp[(op, bc, kc)] = self._unit_zero[arena_off:arena_off + cp.K * nb * nk]
+                arena_off += cp.K * nb * nk
+            else:
+                self._tmp[(op, bc, kc)] = torch.empty(cp.K * nb * nk, dtype=torch.float64, device=dev)
         self.zT = {c: torch.empty((space.n_conf[c], self.n_states[c]), dtype=torch.float64, device=dev)
                    for c in space.charges}
         self.zbT = {c: torch.empty((space.n_conf[c], self.n_states_bra[c]), dtype=torch.float64, device=dev)
                     for c in space.charges}
         # FP32 path: coefficients converted once per build, rows padded to 16 bytes
-        self.f32 = self.precision == _lib.FP32
         if self.f32:
             pad = lambda n: (n + 3) // 4 * 4
             self.zT32 = {c: torch.zeros((space.n_conf[c], pad(self.n_states[c])), dtype=torch.float32, device=dev)
@@ -276,8 +317,9 @@ class DensityBuilder:
                     self.splits[key] = 1
                 else:
                     self.splits[key] = int(min(64, max(1, round(cp.count / max(cp.K, 1) / 256))))
-            # every accumulated block of the fragment in one grouped launch
-            direct = [(key, cp) for key, cp in space.couplings.items() if key not in self.mirror]
+            # every accumulated block of the fragment in one grouped launch (CTA per operator index)
+            direct = [(key, cp) for key, cp in space.couplings.items()
+                      if key not in self.mirror and key not in self._unit_keys]
             tasks = np.zeros(len(direct), dtype=_lib.DENS_TASK_DTYPE)
             begin = 0
             self._zero_first = []
@@ -294,6 +336,28 @@ class DensityBuilder:
                     self._zero_first.append(self._tmp[(op, bc, kc)])
             self._dens_tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
             self._n_dens_tasks, self._dens_ctas = len(tasks), begin
+            # the warp-per-unit blocks: tasks (cta_begin unused) and their unit table
+            ukeys = sorted(self._unit_keys, key=str)
+            utasks = np.zeros(len(ukeys), dtype=_lib.DENS_TASK_DTYPE)
+            ulist, self._max_pairs = [], 1
+            for i, (op, bc, kc) in enumerate(ukeys):
+                cp = space.couplings[(op, bc, kc)]
+                t = utasks[i]
+                t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(), cp.Q.data_ptr(),
+                                                           cp.sign.data_ptr())
+                t["zb32"], t["zk32"] = self.zbT32[bc].data_ptr(), self.zT32[kc].data_ptr()
+                t["rhoT"] = self._tmp[(op, bc, kc)].data_ptr()
+                nb, nk = self.n_states_bra[bc], self.n_states[kc]
+                t["K"], t["nb"], t["nk"], t["splits"] = cp.K, nb, nk, 1
+                self._max_pairs = max(self._max_pairs, nb * ((nk + 3) // 4))
+                un = unit_units[(op, bc, kc)][0].copy()
+                un["task"] = i
+                ulist.append(un)
+            self._n_unit_tasks = len(ukeys)
+            self._unit_tasks = torch.from_numpy(utasks.view(np.uint8).copy()).to(dev) if ukeys else None
+            units = np.concatenate(ulist) if ulist else np.zeros(0, dtype=_lib.DENS_UNIT_DTYPE)
+            self._n_units = len(units)
+            self._units = torch.from_numpy(units.view(np.uint8).copy()).to(dev) if len(units) else None
             self._max_nb = max(self.n_states_bra.values()) if self.n_states_bra else 1
             self._max_nk = max(self.n_states.values()) if self.n_states else 1
 
@@ -312,8 +376,14 @@ class DensityBuilder:
         if self.f32:
             for t in self._zero_first:
                 t.zero_()
-            call("xrh_density_accumulate_f32_grouped", ptr(self._dens_tasks), self._n_dens_tasks, self._dens_ctas,
-                 self._max_nb, self._max_nk, s)
+            if self._n_dens_tasks:
+                call("xrh_density_accumulate_f32_grouped", ptr(self._dens_tasks), self._n_dens_tasks,
+                     self._dens_ctas, self._max_nb, self._max_nk, s)
+            if self._n_units:
+                if self._unit_zero is not None:
+                    self._unit_zero.zero_()
+                call("xrh_density_accumulate_f32_units", ptr(self._unit_tasks), self._n_unit_tasks, ptr(self._units),
+                     self._n_units, self._max_pairs, s)
         for (op, bc, kc), cp in self.space.couplings.items():
             if (op, bc, kc) in self.mirror:
                 continue

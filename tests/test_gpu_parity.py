@@ -68,6 +68,38 @@ def test_density_fp32_variant_close():
     np.testing.assert_allclose(rho["caa"][(0, -1)].cpu().numpy(), ref, rtol=0, atol=2e-6)
 
 
+@pytest.mark.parametrize("path", ["units", "cta"])
+@pytest.mark.parametrize("n_states", [10, 7, 40])
+def test_density_fp32_paths_match_fp64(path, n_states, monkeypatch):
+    """Every FP32 block (warp-per-unit kernel, including operator indices split over several
+    units, or the CTA-per-index kernel) against the FP64 build, to FP32 accuracy: 2e-6 of
+    the block's largest element (64 couplings or fewer per FP32 partial sum)."""
+    from qodeapplications_gb300 import densities as D
+    if path == "cta":
+        monkeypatch.setattr(D, "UNIT_MAX_PAIRS", 0)
+    sysd = S.make_system(n_frag=2, n_orb=9, n_states=n_states, charges=(+1, 0, -1), seed=5)
+    st = sysd["states"][0]
+    charges = (+1, 0, -1)
+    space = D.FragmentSpace({c: st[c][1] for c in charges}, sysd["n_orb"], sysd["n_core"], sysd["n_elec_ref"])
+    ns = {c: st[c][0].shape[0] for c in charges}
+    co = {c: torch.as_tensor(st[c][0], device="cuda") for c in charges}
+    b32 = D.DensityBuilder(space, ns, precision="fp32")
+    if path == "units" and n_states <= 20:
+        assert b32._n_units > 0
+        assert b32._unit_zero is not None          # some index has more than one unit
+    r32 = {op: {k: t.clone() for k, t in blocks.items()} for op, blocks in b32.build(co).items()}
+    r64 = D.DensityBuilder(space, ns, precision="fp64").build(co)
+    for op, blocks in r64.items():
+        for key, t in blocks.items():
+            scale = max(t.abs().max().item(), 1e-30)
+            assert (r32[op][key] - t).abs().max().item() <= 2e-6 * scale, (op, key)
+    # a second build with the same buffers gives the same result (the split arena is re-zeroed)
+    again = b32.build(co)
+    for op, blocks in again.items():
+        for key, t in blocks.items():
+            assert torch.equal(t, r32[op][key]) or (t - r32[op][key]).abs().max().item() < 1e-12
+
+
 def test_monomer_two_electron_matches_oracle():
     from qodeapplications_gb300.densities import FragmentSpace
     from qodeapplications_gb300.hamiltonian import DeviceIntegrals, monomer_two_electron
