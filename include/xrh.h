@@ -324,6 +324,14 @@ typedef struct {
 } xrh_dens_adj_task;   /* 96 bytes */
 int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_dev, int n_tasks, int64_t total_ctas,
                                     int max_nb, int max_nk, void* stream);
+/* The same adjoint for blocks with n_b, n_k <= max_n <= 16 over a unit table (one warp per
+ * unit, one lane per coupling; xrh_dens_unit as for xrh_density_accumulate_f32_units, every
+ * unit adds atomically so split indices need nothing extra; cta_begin is not used).
+ * g_layout 0: gT is dE/drho in [K, n_b, n_k] layout (as above); 1: in the density's own
+ * [n_b, n_k, K] layout (no transposed copy needed). */
+int xrh_density_adjoint_f32_units(const xrh_dens_adj_task* tasks_dev, int n_tasks,
+                                  const xrh_dens_unit* units_dev, int64_t n_units, int max_n,
+                                  int g_layout, void* stream);
 
 /* The same reverse pass on the tensor cores (3 x TF32 split, tcgen05), for blocks with
  * n_b, n_k <= 64: per operator index, tiles of 128 couplings times G (both orientations)

@@ -27,6 +27,7 @@ _SIGS = {
     "xrh_density_accumulate_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
     "xrh_density_accumulate_f32_units": (_i32, [_vp, _i32, _vp, _i64, _i32, _vp]),
     "xrh_density_adjoint_f32_grouped": (_i32, [_vp, _i32, _i64, _i32, _i32, _vp]),
+    "xrh_density_adjoint_f32_units": (_i32, [_vp, _i32, _vp, _i64, _i32, _i32, _vp]),
     "xrh_mirror_density": (_i32, [_i32, _i32, _i32, _i32, _vp, _vp, _i32, _vp]),
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),

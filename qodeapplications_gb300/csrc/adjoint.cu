@@ -319,6 +319,108 @@ __global__ void __launch_bounds__(kWThreads) ccaa_weighted_kernel(
     }
 }
 
+
+// ---- small blocks: lane per coupling ------------------------------------------------------
+// For blocks of few states (n_b, n_k <= 4 * MAXQ) a warp owns one unit (an operator index, or a
+// range of its couplings, as in the forward units kernel) and stages G = dE/drho[idx]
+// (n_b x n_k, FP32, rows padded with zeros to 4 * MAXQ) in its shared memory; lane l takes
+// couplings c = c_lo + l, c_lo + l + 32, ...: it gathers the padded FP32 rows zb[P_c] and
+// zk[Q_c] (padding entries are zero), reads G by broadcast, forms
+//   U[J] = s_c sum_I zb[P_c, I] G[I, J]   and   W[I] = s_c sum_J G[I, J] zk[Q_c, J]
+// and adds them to gzk[Q_c] and gzb[P_c] with vector atomics (float4 when 16-byte aligned,
+// else float2 when 8-byte aligned, else scalar).
+template <int MP>
+__device__ __forceinline__ void atomic_add_row(float* dst, const float (&v)[MP], int n) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
+    const bool a16 = (a & 15) == 0, a8 = (a & 7) == 0;
+#pragma unroll
+    for (int k = 0; k < MP; k += 4) {
+        if (k >= n) break;
+        if (a16 && k + 3 < n) {
+            atomicAdd(reinterpret_cast<float4*>(dst + k), make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]));
+            continue;
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            const int kk = k + h;
+            if (kk >= n) break;
+            if (kk + 1 < n && a8) {
+                atomicAdd(reinterpret_cast<float2*>(dst + kk), make_float2(v[kk], v[kk + 1]));
+            } else {
+                atomicAdd(dst + kk, v[kk]);
+                if (kk + 1 < n) atomicAdd(dst + kk + 1, v[kk + 1]);
+            }
+        }
+    }
+}
+
+template <int MAXQ>
+__global__ void __launch_bounds__(256) density_adjoint_units_kernel(const xrh_dens_adj_task* __restrict__ tasks,
+                                                                   const xrh_dens_unit* __restrict__ units,
+                                                                   int64_t n_units, int g_layout) {
+    constexpr int MP = 4 * MAXQ;
+    __shared__ __align__(16) float gsm[8][MP][MP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t u = (int64_t)blockIdx.x * 8 + warp;
+    if (u >= n_units) return;
+    const xrh_dens_unit U = units[u];
+    const xrh_dens_adj_task& T = tasks[U.task];
+    const int nb = T.nb, nk = T.nk;
+    if (nb > MP || nk > MP) return;                  // the host never builds such a unit
+    const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
+    float (*g)[MP] = gsm[warp];
+    for (int e = lane; e < MP * MP; e += 32) {
+        const int I = e / MP, J = e - I * MP;
+        float v = 0.f;
+        if (I < nb && J < nk)
+            v = (float)(g_layout == 0 ? T.gT[((int64_t)U.idx * nb + I) * nk + J]
+                                      : T.gT[((int64_t)I * nk + J) * T.K + U.idx]);
+        g[I][J] = v;
+    }
+    __syncwarp();
+    const int64_t base = T.idx_ptr[U.idx];
+    const int64_t c_lo = base + U.c_lo, c_hi = base + U.c_hi;
+    for (int64_t c = c_lo + lane; c < c_hi; c += 32) {
+        const int p = T.P[c], q = T.Q[c];
+        const float s = T.sign[c] < 0 ? -1.f : 1.f;
+        float zb[MP], zk[MP];
+        const float4* zbr = reinterpret_cast<const float4*>(T.zb32 + (int64_t)p * nbp);
+        const float4* zkr = reinterpret_cast<const float4*>(T.zk32 + (int64_t)q * nkp);
+#pragma unroll
+        for (int x = 0; x < MAXQ; ++x) {
+            const float4 a = 4 * x < nbp ? __ldg(zbr + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 b = 4 * x < nkp ? __ldg(zkr + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+            zb[4 * x] = a.x; zb[4 * x + 1] = a.y; zb[4 * x + 2] = a.z; zb[4 * x + 3] = a.w;
+            zk[4 * x] = b.x; zk[4 * x + 1] = b.y; zk[4 * x + 2] = b.z; zk[4 * x + 3] = b.w;
+        }
+        float Uj[MP], Wi[MP];
+#pragma unroll
+        for (int k = 0; k < MP; ++k) { Uj[k] = 0.f; Wi[k] = 0.f; }
+#pragma unroll
+        for (int I = 0; I < MP; ++I) {
+            if (I >= nbp) break;
+#pragma unroll
+            for (int x = 0; x < MAXQ; ++x) {
+                if (4 * x >= nkp) break;
+                const float4 gv = *reinterpret_cast<const float4*>(&g[I][4 * x]);
+                Uj[4 * x] = fmaf(zb[I], gv.x, Uj[4 * x]);
+                Uj[4 * x + 1] = fmaf(zb[I], gv.y, Uj[4 * x + 1]);
+                Uj[4 * x + 2] = fmaf(zb[I], gv.z, Uj[4 * x + 2]);
+                Uj[4 * x + 3] = fmaf(zb[I], gv.w, Uj[4 * x + 3]);
+                float w = Wi[I];
+                w = fmaf(gv.x, zk[4 * x], w);
+                w = fmaf(gv.y, zk[4 * x + 1], w);
+                w = fmaf(gv.z, zk[4 * x + 2], w);
+                w = fmaf(gv.w, zk[4 * x + 3], w);
+                Wi[I] = w;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < MP; ++k) { Uj[k] *= s; Wi[k] *= s; }
+        atomic_add_row(T.gzk + (int64_t)q * nk, Uj, nk);
+        atomic_add_row(T.gzb + (int64_t)p * nb, Wi, nb);
+    }
+}
 }  // namespace
 
 extern "C" int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_dev, int n_tasks, int64_t total_ctas,
@@ -335,6 +437,27 @@ extern "C" int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_de
                              (int)smem);
     density_adjoint_f32_grouped_kernel<<<(unsigned)total_ctas, kAdjThreads, smem, (cudaStream_t)stream>>>(tasks_dev,
                                                                                                          n_tasks);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_density_adjoint_f32_units(const xrh_dens_adj_task* tasks_dev, int n_tasks,
+                                             const xrh_dens_unit* units_dev, int64_t n_units, int max_n,
+                                             int g_layout, void* stream) {
+    if (n_tasks < 0 || n_units < 0 || max_n <= 0 || (g_layout != 0 && g_layout != 1)) return XRH_ERR_ARG;
+    if (n_tasks == 0 || n_units == 0) return XRH_OK;
+    if (!tasks_dev || !units_dev) return XRH_ERR_ARG;
+    const int64_t ctas = (n_units + 7) / 8;
+    if (ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (max_n <= 8)
+        density_adjoint_units_kernel<2><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units, g_layout);
+    else if (max_n <= 12)
+        density_adjoint_units_kernel<3><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units, g_layout);
+    else if (max_n <= 16)
+        density_adjoint_units_kernel<4><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units, g_layout);
+    else
+        return XRH_ERR_CAPACITY;
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -25,6 +25,8 @@ from .gemm import GroupedGemm, SplitRegistry, TCGroupedGemm
 from .hamiltonian import _Arena, _splitk
 
 
+ADJ_UNIT_MAX = 16     # blocks with at most this many states per side use the lane-per-coupling adjoint
+
 class XRDimerAdjoint:
     def __init__(self, plan, density_adjoint="simt"):
         """density_adjoint: 'simt' (the grouped CUDA-core kernel) or 'tc' (tensor cores, split-
@@ -332,11 +334,35 @@ class XRDimerAdjoint:
                     begin += cp.K
                 self.dens_adj_tc.append((torch.from_numpy(tasks.view(np.uint8).copy()).to(dev), len(entries), begin))
         elif self.prec32:
+            from .densities import _coupling_units
+            self.dens_adj_units = []
             for m in (0, 1):
+                bld = plan.builders[m]
+                # blocks of at most 16 states per side: lane per coupling, dE/drho read in place
+                small = [e for e in self.dens_adj
+                         if e[0] == m and e[5].shape[0] <= ADJ_UNIT_MAX and e[5].shape[1] <= ADJ_UNIT_MAX]
+                if small:
+                    tasks = np.zeros(len(small), dtype=_lib.DENS_ADJ_TASK_DTYPE)
+                    ulist = []
+                    for i, (_m, op, bc, kc, cp, rt, grho, gT) in enumerate(small):
+                        t = tasks[i]
+                        t["idx_ptr"], t["P"], t["Q"], t["sign"] = (cp.idx_ptr.data_ptr(), cp.P.data_ptr(),
+                                                                   cp.Q.data_ptr(), cp.sign.data_ptr())
+                        t["zb32"], t["zk32"] = bld.zbT32[bc].data_ptr(), bld.zT32[kc].data_ptr()
+                        t["gT"] = grho.data_ptr()
+                        t["gzb"], t["gzk"] = self.gz32[m][bc].data_ptr(), self.gz32[m][kc].data_ptr()
+                        t["K"], t["nb"], t["nk"] = cp.K, rt.shape[0], rt.shape[1]
+                        un = _coupling_units(cp)[0]
+                        un["task"] = i
+                        ulist.append(un)
+                    units = np.concatenate(ulist)
+                    self.dens_adj_units.append((torch.from_numpy(tasks.view(np.uint8).copy()).to(dev), len(small),
+                                                torch.from_numpy(units.view(np.uint8).copy()).to(dev), len(units),
+                                                max(max(e[5].shape[0], e[5].shape[1]) for e in small)))
+                    self.dens_adj = [e for e in self.dens_adj if not any(e is x for x in small)]
                 entries = [e for e in self.dens_adj if e[0] == m]
                 if not entries:
                     continue
-                bld = plan.builders[m]
                 tasks = np.zeros(len(entries), dtype=_lib.DENS_ADJ_TASK_DTYPE)
                 begin = 0
                 for i, (_m, op, bc, kc, cp, rt, grho, gT) in enumerate(entries):
@@ -381,6 +407,8 @@ class XRDimerAdjoint:
                  ptr(self.G[("gzT", m, bc)]), ptr(self.G[("gzT", m, kc)]), s)
         for (tasks, n_t, ctas, mnb, mnk) in self.dens_adj_groups:
             call("xrh_density_adjoint_f32_grouped", ptr(tasks), n_t, ctas, mnb, mnk, s)
+        for (tasks, n_t, units, n_u, mx) in getattr(self, "dens_adj_units", ()):
+            call("xrh_density_adjoint_f32_units", ptr(tasks), n_t, ptr(units), n_u, mx, 1, s)
         if self.dens_adj_tc:
             for (bld, zs) in self.z_split:
                 for c, (zh, zl) in zs.items():

@@ -200,3 +200,36 @@ def test_tensor_core_density_adjoint_matches_fp64_over_many_coupling_tiles():
         out[p] = torch.cat([tangent_project(g[m][c], coeffs[m][c]).reshape(-1) for m in range(2) for c in CHG])
     rel = float((out["tf32x3"] - out["fp64"]).norm() / out["fp64"].norm())
     assert rel < 1e-5, rel
+
+
+@pytest.mark.parametrize("path", ["units", "cta"])
+def test_fp32_density_adjoint_paths_match_fp64(path, monkeypatch):
+    """The FP32 density adjoint, lane per coupling on unit tables (dE/drho read in place) or
+    one CTA per operator index (transposed dE/drho), against the FP64 adjoint on a system with
+    hundreds of couplings per operator index: tangent state gradient within 1e-5 relative."""
+    from qodeapplications_gb300 import densities as D
+    from qodeapplications_gb300 import gradients as Gm
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
+    if path == "cta":
+        monkeypatch.setattr(Gm, "ADJ_UNIT_MAX", 0)
+        monkeypatch.setattr(D, "UNIT_MAX_PAIRS", 0)
+    n_orb, n_st = 6, 8
+    sysd = S.make_system(n_frag=2, n_orb=n_orb, n_states=n_st, charges=CHG, seed=43)
+    spaces = [D.FragmentSpace({c: sysd["states"][m][c][1] for c in CHG}, n_orb, 0, 4) for m in range(2)]
+    ns = [{c: n_st for c in CHG}] * 2
+    coeffs = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in CHG} for m in range(2)]
+    out = {}
+    for p in ("fp64", "tf32x3"):
+        plan = XRDimerPlan(spaces, ns, [list(CHG)] * 2, DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"]),
+                           precision=p)
+        adj = Gm.XRDimerAdjoint(plan)
+        if p == "tf32x3":
+            assert bool(adj.dens_adj_units) == (path == "units")
+        E, d, _ = _gpu_energy_and_grad(plan, adj, coeffs)
+        torch.cuda.synchronize()
+        plan.check_status()
+        adj.check_status()
+        g = adj.state_gradient()
+        out[p] = torch.cat([Gm.tangent_project(g[m][c], coeffs[m][c]).reshape(-1) for m in range(2) for c in CHG])
+    rel = float((out["tf32x3"] - out["fp64"]).norm() / out["fp64"].norm())
+    assert rel < 1e-5, rel
