@@ -230,6 +230,19 @@ int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, 
 int xrh_gemv_cols(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* c_dev,
                   double scale, double* y_dev, void* stream);
 int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double* beta_dev, void* stream);
+/* xrh_gemv_rows for a table of GEMVs in one launch: task t computes rows [0, rows) of
+ * y = alpha A x + beta y and owns the launch's rows [row_begin, row_begin + round_up(rows, 8));
+ * tasks sorted by row_begin, total_rows8 = the sum of the rounded row counts.  With beta == 1
+ * the products are added with FP64 atomics (tasks may then share rows of y). */
+typedef struct {
+    const double* A;
+    const double* x;
+    double* y;
+    int64_t rows, cols, lda;
+    double alpha, beta;
+    int64_t row_begin;
+} xrh_gemv_task;   /* 72 bytes */
+int xrh_gemv_rows_grouped(const xrh_gemv_task* tasks_dev, int n_tasks, int64_t total_rows8, void* stream);
 /* The whole Krylov loop of a small sector (n <= 4096) in one launch (one CTA): V[0] = v0,
  * then for j < m: w = H V[j]; two classical Gram-Schmidt passes against V[0..j];
  * alpha[j] = the two passes' coefficients of V[j] summed; beta[j] = |w|;
@@ -290,6 +303,20 @@ int xrh_left_multiply(const xrh_state_task* tasks_dev, int n_tasks, int64_t tota
  * (StateSpaceOptimizer/orb_grads.py, the two-electron term) is its main use. */
 int xrh_abt_small(int precision, int m, int n, int64_t K, const void* A_dev, int64_t lda,
                   const void* B_dev, int64_t ldb, double alpha, double* C_dev, void* stream);
+/* A table of such products in one launch: task t owns CTAs [cta_begin, cta_begin +
+ * xrh_state_ctas(K)) (tasks sorted by cta_begin, total_ctas the sum), m, n <= 64, C row
+ * stride n.  Used for E2 = Zb sigma^T, the monomer two-electron blocks
+ * (general-XRCC/build_density_tensors.py:122-133 folds them into ccaa numbers). */
+typedef struct {
+    const void* A;
+    const void* B;
+    double* C;
+    int64_t m, n, K, lda, ldb;
+    double alpha;
+    int64_t cta_begin;
+} xrh_abt_task;   /* 80 bytes */
+int xrh_abt_grouped(int precision, const xrh_abt_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                    void* stream);
 
 /* Adjoint of the density build (dE/dz from dE/drho), the reverse of xrh_density_accumulate
  * over the same coupling lists; replaces the determinant-bra density rebuild plus second H
@@ -456,6 +483,20 @@ typedef struct {
 int xrh_tc_chunk_elems(int precision);
 int xrh_split_operand(int precision, const double* src_dev, int64_t rows, int64_t K, int64_t ld,
                       int64_t Kp, void* hi_dev, void* lo_dev, void* stream);
+/* xrh_split_operand for every operand of a task table in one launch.  Task t splits rows x Kp
+ * (src rows of ld doubles, K of them used, the rest of each row written as zeros) into hi/lo
+ * (16-byte aligned, Kp a multiple of xrh_tc_chunk_elems); its 4-element groups are
+ * [group_begin, group_begin + rows * Kp / 4) of the launch, tasks sorted by group_begin and
+ * total_groups the sum. */
+typedef struct {
+    const double* src;
+    void* hi;
+    void* lo;
+    int64_t rows, K, ld, Kp;
+    int64_t group_begin;
+} xrh_split_task;   /* 64 bytes */
+int xrh_split_grouped(int precision, const xrh_split_task* tasks_dev, int n_tasks, int64_t total_groups,
+                      void* stream);
 int xrh_tc_encode_map(int precision, const void* base_dev, int64_t rows, int64_t Kp, int box_rows,
                       void* map_out_host);
 int xrh_gemm_tc_grouped(int precision, const xrh_tc_task* tasks_dev, int n_tasks, int64_t total_tiles,

@@ -34,6 +34,9 @@ _SIGS = {
     "xrh_lanczos_coop_work": (_i64, [_i32]),
     "xrh_lanczos_coop": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "xrh_state_ctas": (_i32, [_i64]),
+    "xrh_split_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
+    "xrh_gemv_rows_grouped": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_abt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
     "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
     "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),
     "xrh_inv_sqrt_small": (_i32, [_vp, _i32, _i32, _vp]),
@@ -156,6 +159,17 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+ABT_TASK_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("C", np.uint64), ("m", np.int64), ("n", np.int64),
+                           ("K", np.int64), ("lda", np.int64), ("ldb", np.int64), ("alpha", np.float64),
+                           ("cta_begin", np.int64)])
+assert ABT_TASK_DTYPE.itemsize == 80
+GEMV_TASK_DTYPE = np.dtype([("A", np.uint64), ("x", np.uint64), ("y", np.uint64), ("rows", np.int64),
+                            ("cols", np.int64), ("lda", np.int64), ("alpha", np.float64), ("beta", np.float64),
+                            ("row_begin", np.int64)])
+assert GEMV_TASK_DTYPE.itemsize == 72
+SPLIT_TASK_DTYPE = np.dtype([("src", np.uint64), ("hi", np.uint64), ("lo", np.uint64), ("rows", np.int64),
+                             ("K", np.int64), ("ld", np.int64), ("Kp", np.int64), ("group_begin", np.int64)])
+assert SPLIT_TASK_DTYPE.itemsize == 64
 DENS_UNIT_DTYPE = np.dtype([("task", np.int32), ("idx", np.int32), ("c_lo", np.int32), ("c_hi", np.int32)])
 assert DENS_UNIT_DTYPE.itemsize == 16
 STATE_TASK_DTYPE = np.dtype([("gT", np.uint64), ("gT32", np.uint64), ("z", np.uint64), ("zn", np.uint64), ("G", np.uint64),

@@ -366,40 +366,68 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // One thread per group of 4 consecutive K elements of a row (one division per group), one
 // 8- or 16-byte store per group and part.
 template <int KIND>
+__device__ __forceinline__ void split_group(const double* __restrict__ src, int64_t K, int64_t ld, int64_t Kp,
+                                            void* __restrict__ hi, void* __restrict__ lo, int64_t t) {
+    const int64_t groups = Kp >> 2;
+    const int64_t r = t / groups;
+    const int64_t k0 = (t - r * groups) * 4;
+    const double* srow = src + r * ld;
+    double x[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) x[e] = (k0 + e < K) ? __ldg(srow + k0 + e) : 0.0;
+    const int64_t o = r * Kp + k0;
+    if constexpr (KIND == 0) {
+        __nv_bfloat16 h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            h[e] = __float2bfloat16_rn((float)x[e]);
+            l[e] = __float2bfloat16_rn((float)(x[e] - (double)__bfloat162float(h[e])));
+        }
+        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(hi) + o) = *reinterpret_cast<uint2*>(h);
+        *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(lo) + o) = *reinterpret_cast<uint2*>(l);
+    } else {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h[e]) : "f"((float)x[e]));
+            const double rem = x[e] - (double)__uint_as_float(h[e]);
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l[e]) : "f"((float)rem));
+        }
+        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(hi) + o) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(lo) + o) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+template <int KIND>
 __global__ void split_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t ld, int64_t Kp,
                              void* __restrict__ hi, void* __restrict__ lo) {
-    const int64_t groups = Kp >> 2;
-    const int64_t total = rows * groups;
+    const int64_t total = rows * (Kp >> 2);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+        split_group<KIND>(src, K, ld, Kp, hi, lo, t);
+}
+
+// Every operand of a task table in one launch: global 4-element group g belongs to the task
+// with the last group_begin <= g (binary search over the group_begin values staged in shared
+// memory, SPLIT_SMEM_TASKS of them at most; larger tables search global memory).
+constexpr int SPLIT_SMEM_TASKS = 512;
+
+template <int KIND>
+__global__ void __launch_bounds__(256) split_grouped_kernel(const xrh_split_task* __restrict__ tasks, int n_tasks,
+                                                            int64_t total) {
+    __shared__ int64_t s_begin[SPLIT_SMEM_TASKS];
+    const bool in_smem = n_tasks <= SPLIT_SMEM_TASKS;
+    if (in_smem)
+        for (int i = threadIdx.x; i < n_tasks; i += blockDim.x) s_begin[i] = tasks[i].group_begin;
+    __syncthreads();
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / groups;
-        const int64_t k0 = (t - r * groups) * 4;
-        const double* srow = src + r * ld;
-        {
-            double x[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) x[t] = (k0 + t < K) ? __ldg(srow + k0 + t) : 0.0;
-            const int64_t o = r * Kp + k0;
-            if constexpr (KIND == 0) {
-                __nv_bfloat16 h[4], l[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    h[t] = __float2bfloat16_rn((float)x[t]);
-                    l[t] = __float2bfloat16_rn((float)(x[t] - (double)__bfloat162float(h[t])));
-                }
-                *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(hi) + o) = *reinterpret_cast<uint2*>(h);
-                *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(lo) + o) = *reinterpret_cast<uint2*>(l);
-            } else {
-                uint32_t h[4], l[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h[t]) : "f"((float)x[t]));
-                    const double rem = x[t] - (double)__uint_as_float(h[t]);
-                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l[t]) : "f"((float)rem));
-                }
-                *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(hi) + o) = make_uint4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(lo) + o) = make_uint4(l[0], l[1], l[2], l[3]);
-            }
+        int lo = 0, hi = n_tasks - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            const int64_t b = in_smem ? s_begin[mid] : tasks[mid].group_begin;
+            if (b <= t) lo = mid; else hi = mid - 1;
         }
+        const xrh_split_task& T = tasks[lo];
+        split_group<KIND>(T.src, T.K, T.ld, T.Kp, T.hi, T.lo, t - T.group_begin);
     }
 }
 
@@ -438,6 +466,22 @@ extern "C" int xrh_split_operand(int precision, const double* src_dev, int64_t r
         split_kernel<0><<<blocks, 256, 0, (cudaStream_t)stream>>>(src_dev, rows, K, ld, Kp, hi_dev, lo_dev);
     else
         split_kernel<1><<<blocks, 256, 0, (cudaStream_t)stream>>>(src_dev, rows, K, ld, Kp, hi_dev, lo_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_split_grouped(int precision, const xrh_split_task* tasks_dev, int n_tasks, int64_t total_groups,
+                                 void* stream) {
+    if (!xrh_tc_chunk_elems(precision)) return XRH_ERR_UNSUPPORTED;
+    if (n_tasks < 0 || total_groups < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_groups == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    const int64_t blocks64 = (total_groups + 255) / 256;
+    const unsigned blocks = (unsigned)(blocks64 < 152 * 32 ? blocks64 : 152 * 32);
+    if (precision == XRH_BF16X3)
+        split_grouped_kernel<0><<<blocks, 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, total_groups);
+    else
+        split_grouped_kernel<1><<<blocks, 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, total_groups);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

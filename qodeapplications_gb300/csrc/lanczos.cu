@@ -129,6 +129,32 @@ __global__ void __launch_bounds__(1024) lanczos_small_kernel(int n, int m, const
 }
 
 
+// Many row GEMVs in one launch: CTA b (8 warps, a row each) belongs to the task with the last
+// row_begin <= 8 b (task row ranges padded to multiples of 8).  With beta == 1 the result is
+// added atomically, so tasks may share output rows.
+__global__ void __launch_bounds__(256) gemv_rows_grouped_kernel(const xrh_gemv_task* __restrict__ tasks,
+                                                              int n_tasks) {
+    const int64_t row8 = (int64_t)blockIdx.x * 8;
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].row_begin <= row8) lo = mid; else hi = mid - 1;
+    }
+    const xrh_gemv_task& T = tasks[lo];
+    const int64_t row = row8 - T.row_begin + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= T.rows) return;
+    const double* a = T.A + row * T.lda;
+    double s = 0.0;
+    for (int64_t j = lane; j < T.cols; j += 32) s = fma(a[j], T.x[j], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        if (T.beta == 1.0) atomicAdd(T.y + row, T.alpha * s);
+        else T.y[row] = T.alpha * s + (T.beta == 0.0 ? 0.0 : T.beta * T.y[row]);
+    }
+}
+
 // ---- the Krylov loop over many CTAs (cooperative launch) ----------------------------------
 // The FP64 rate of one SM bounds the single-CTA loop; here the rows of H, V and w are split
 // over the CTAs of one cooperative launch and every step takes three grid barriers:
@@ -304,6 +330,17 @@ extern "C" int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, in
     if ((rows + 7) / 8 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     gemv_rows_kernel<<<(unsigned)((rows + 7) / 8), 256, 0, (cudaStream_t)stream>>>(rows, cols, A_dev, lda, x_dev, alpha,
                                                                                   beta, y_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_gemv_rows_grouped(const xrh_gemv_task* tasks_dev, int n_tasks, int64_t total_rows8,
+                                     void* stream) {
+    if (n_tasks < 0 || total_rows8 < 0 || (total_rows8 & 7)) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_rows8 == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_rows8 / 8 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    gemv_rows_grouped_kernel<<<(unsigned)(total_rows8 / 8), 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -111,6 +111,26 @@ __global__ void __launch_bounds__(SS_THREADS) abt_kernel(int m, int n, int64_t K
     abt_slice<T, ACC, false>(A, lda, nullptr, m, B, ldb, n, k_begin, k_end, alpha, C, sa, sb);
 }
 
+// Many small-output products in one launch: task t owns CTAs [cta_begin, cta_begin +
+// ceil(K / SS_KSLICE)) and adds alpha A B^T (m x n, row stride n) into C.
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(SS_THREADS) abt_grouped_kernel(const xrh_abt_task* __restrict__ tasks, int n_tasks) {
+    __shared__ T sa[64][GR_KCHUNK + 1], sb[64][GR_KCHUNK + 1];
+    int lo = 0, hi = n_tasks - 1;
+    const int64_t cta = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const xrh_abt_task& Tk = tasks[lo];
+    if (Tk.m <= 0 || Tk.m > 64 || Tk.n <= 0 || Tk.n > 64) return;   // checked by the host
+    const int64_t k_begin = (cta - Tk.cta_begin) * (int64_t)SS_KSLICE;
+    const int64_t k_end = k_begin + SS_KSLICE < Tk.K ? k_begin + SS_KSLICE : Tk.K;
+    abt_slice<T, ACC, false>(reinterpret_cast<const T*>(Tk.A), Tk.lda, nullptr, (int)Tk.m,
+                             reinterpret_cast<const T*>(Tk.B), Tk.ldb, (int)Tk.n, k_begin, k_end, Tk.alpha, Tk.C, sa,
+                             sb);
+}
+
 // out[i][k] = sum_j W[i][j] X[j][k] over this CTA's K slice, X (and g) staged TS_KCHUNK columns
 // at a time; thread (row group, column) = (t / TS_KCHUNK, t % TS_KCHUNK), rows i = row group +
 // (SS_THREADS / TS_KCHUNK) r.
@@ -287,6 +307,23 @@ extern "C" int xrh_abt_small(int precision, int m, int n, int64_t K, const void*
     else if (precision == XRH_FP32)
         abt_kernel<float, float><<<(unsigned)ctas, SS_THREADS, 0, s>>>(m, n, K, (const float*)A_dev, lda,
                                                                       (const float*)B_dev, ldb, alpha, C_dev);
+    else
+        return XRH_ERR_ARG;
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_abt_grouped(int precision, const xrh_abt_task* tasks_dev, int n_tasks, int64_t total_ctas,
+                               void* stream) {
+    if (n_tasks < 0 || total_ctas < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision == XRH_FP64)
+        abt_grouped_kernel<double, double><<<(unsigned)total_ctas, SS_THREADS, 0, s>>>(tasks_dev, n_tasks);
+    else if (precision == XRH_FP32)
+        abt_grouped_kernel<float, float><<<(unsigned)total_ctas, SS_THREADS, 0, s>>>(tasks_dev, n_tasks);
     else
         return XRH_ERR_ARG;
     XRH_CHECK_LAUNCH();

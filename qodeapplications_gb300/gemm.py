@@ -112,10 +112,12 @@ class SplitRegistry:
         self.maps = []       # host byte strings, 128 B each
         self.map_index = {}
         self.maps_dev = None
+        self._split_tables = {}
 
     def operand(self, t, rows, K, ld, group="in"):
         key = t.data_ptr()
         if key not in self.ops:
+            self._split_tables.pop(group, None)      # rebuilt at the group's next split
             Kp = ((K + self.kch - 1) // self.kch) * self.kch
             hi = torch.zeros((rows, Kp), dtype=self.dtype, device=self.device)
             lo = torch.zeros((rows, Kp), dtype=self.dtype, device=self.device)
@@ -142,11 +144,23 @@ class SplitRegistry:
         assert self.maps_dev.data_ptr() % 64 == 0
 
     def split(self, group, stream=None):
+        """Split every operand of `group` in one launch (task table built on first use and again
+        after an operand joins the group; not during a graph capture)."""
         s = stream_ptr(stream)
-        for op in self.ops.values():
-            if op["group"] == group:
-                call("xrh_split_operand", self.prec, ptr(op["src"]), op["rows"], op["K"], op["ld"], op["Kp"],
-                     ptr(op["hi"]), ptr(op["lo"]), s)
+        if group not in self._split_tables:
+            ops = [op for op in self.ops.values() if op["group"] == group]
+            tasks = np.zeros(len(ops), dtype=_lib.SPLIT_TASK_DTYPE)
+            begin = 0
+            for i, op in enumerate(ops):
+                t = tasks[i]
+                t["src"], t["hi"], t["lo"] = op["src"].data_ptr(), op["hi"].data_ptr(), op["lo"].data_ptr()
+                t["rows"], t["K"], t["ld"], t["Kp"], t["group_begin"] = op["rows"], op["K"], op["ld"], op["Kp"], begin
+                begin += op["rows"] * op["Kp"] // 4
+            dev = torch.from_numpy(tasks.view(np.uint8).copy()).to(self.device) if len(ops) else None
+            self._split_tables[group] = (dev, len(ops), begin)
+        dev, n, total = self._split_tables[group]
+        if n:
+            call("xrh_split_grouped", self.prec, ptr(dev), n, total, s)
 
 
 _TUNE_CACHE = {}

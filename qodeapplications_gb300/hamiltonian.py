@@ -247,6 +247,22 @@ def _splitk(K_total, target=384, cap=32):
     return int(max(1, min(cap, K_total // target)))
 
 
+
+def _abt_table(entries, device):
+    """Task table of xrh_abt_grouped (FP64) for [(m, n, (A, lda, B, ldb, K, alpha), C)], C with
+    row stride n; None when empty."""
+    if not entries:
+        return None
+    tab = np.zeros(len(entries), dtype=_lib.ABT_TASK_DTYPE)
+    cta = 0
+    for i, (m, n, (A, lda, B, ldb, K, alpha), C) in enumerate(entries):
+        t = tab[i]
+        t["A"], t["B"], t["C"] = A.data_ptr(), B.data_ptr(), C.data_ptr()
+        t["m"], t["n"], t["K"], t["lda"], t["ldb"], t["alpha"], t["cta_begin"] = m, n, K, lda, ldb, alpha, cta
+        cta += int(_lib.lib().xrh_state_ctas(K))
+    return torch.from_numpy(tab.view(np.uint8).copy()).to(device), len(entries), cta
+
+
 class XRDimerPlan:
     """Planned order-0 XR-H build of a dimer (fragments 0 and 1, S = 1 integrals).
 
@@ -395,6 +411,22 @@ class XRDimerPlan:
         self.mono_gemv = [(sg_[0][0], sg_[0][2], out_, M_, sg_[0][4]) for (M_, N_, sg_, out_, _l, _s) in mono if N_ == 1]
         mono = [t for t in mono if t[1] != 1]
         self.mono_flops = sum(2.0 * M_ * K_ for (_a, _w, _o, M_, K_) in self.mono_gemv)
+        self.mono_gemv_tasks = None
+        if self.mono_gemv:
+            gt = np.zeros(len(self.mono_gemv), dtype=_lib.GEMV_TASK_DTYPE)
+            rb = 0
+            for i, (A_, w_, out_, M_, K_) in enumerate(self.mono_gemv):
+                t = gt[i]
+                t["A"], t["x"], t["y"] = A_.data_ptr(), w_.data_ptr(), out_.data_ptr()
+                t["rows"], t["cols"], t["lda"], t["alpha"], t["beta"], t["row_begin"] = M_, K_, K_, 1.0, 1.0, rb
+                rb += (M_ + 7) // 8 * 8
+            self.mono_gemv_tasks = (torch.from_numpy(gt.view(np.uint8).copy()).to(self.device), len(gt), rb)
+        # small outputs over long K (E2 = Zb sigma^T, n x n over the determinants): split-K
+        # products in one launch instead of 64 x 64 tiles
+        abt = [t for t in mono if len(t[2]) == 1 and t[0] <= 64 and t[1] <= 64 and t[4] == t[1]]
+        mono = [t for t in mono if not any(t is a for a in abt)]
+        self.mono_abt = _abt_table([(M_, N_, segs_[0], out_) for (M_, N_, segs_, out_, _l, _s) in abt], dev)
+        self.mono_flops += sum(2.0 * M_ * N_ * segs_[0][4] for (M_, N_, segs_, _o, _l, _s) in abt)
         for (M_, N_, segs_, out_, ldc_, sk_) in mono:
             pre.add(M_, N_, segs_, out_, ldc_, mode=1, splitk=sk_)
         self.pre = pre.finalize()
@@ -575,8 +607,12 @@ class XRDimerPlan:
                 sg.run_sigma(self.builders[m].zT[c])
         self.arena.buf.zero_()
         s = stream_ptr()
-        for (A_, w_, out_, M_, K_) in self.mono_gemv:
-            call("xrh_gemv_rows", M_, K_, ptr(A_), K_, ptr(w_), 1.0, 1.0, ptr(out_), s)
+        if self.mono_gemv_tasks is not None:
+            gtd, n_g, rows8 = self.mono_gemv_tasks
+            call("xrh_gemv_rows_grouped", ptr(gtd), n_g, rows8, s)
+        if self.mono_abt is not None:
+            atd, n_a, ctas = self.mono_abt
+            call("xrh_abt_grouped", _lib.FP64, ptr(atd), n_a, ctas, s)
         if self.tc:
             self.reg.split("in")
             self.pre_tc.run()
