@@ -107,20 +107,35 @@ typedef struct {
 int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
                                        int max_nb, int max_nk, void* stream);
 
-/* Same product for blocks of few states (n_b * ceil(n_k / 4) <= max_pairs <= 128), one warp
- * per unit: unit u covers couplings [idx_ptr[idx] + c_lo, idx_ptr[idx] + c_hi) of operator
- * index idx of task `task` (cta_begin and splits of the tasks are not used).  A unit with
- * c_lo = 0 and c_hi = the index's coupling count stores rhoT[idx] (an index with no
- * couplings needs such a unit, it writes zeros); the units of an index split into several
- * ranges ADD atomically, so the rhoT of their tasks must be zeroed by the caller. */
+/* Same product for blocks of at most max_n <= 16 states per side, one warp per unit: unit u
+ * covers couplings [idx_ptr[idx] + c_lo, idx_ptr[idx] + c_hi) of operator index idx of task
+ * `task` (cta_begin and splits of the tasks are not used).  A unit with c_lo = 0 and c_hi =
+ * the index's coupling count stores rhoT[idx] (an index with no couplings needs such a unit,
+ * it writes zeros); the units of an index split into several ranges ADD atomically, so the
+ * rhoT of their tasks must be zeroed by the caller.  zb32 / zk32 rows as for
+ * xrh_density_accumulate_f32 (16-byte aligned, padded with zeros). */
 typedef struct {
     int32_t task;
     int32_t idx;
     int32_t c_lo, c_hi;
 } xrh_dens_unit;   /* 16 bytes */
 int xrh_density_accumulate_f32_units(const xrh_dens_task* tasks_dev, int n_tasks,
-                                     const xrh_dens_unit* units_dev, int64_t n_units, int max_pairs,
+                                     const xrh_dens_unit* units_dev, int64_t n_units, int max_n,
                                      void* stream);
+
+/* Coefficient staging of the builds in one launch: task t (a charge sector) writes
+ * zT[k*n + i] = src[i*K + k] (FP64; skipped when zT is NULL) and zT32[k*npad + i] =
+ * fl32(src[i*K + k]) (FP32 round to nearest; skipped when zT32 is NULL; columns n..npad
+ * untouched) for k < K, i < n; its rows are [row_begin, row_begin + K) of the launch (tasks
+ * sorted by row_begin, total_rows = the last row_begin + K). */
+typedef struct {
+    const double* src;
+    double* zT;
+    float* zT32;
+    int64_t n, K, npad;
+    int64_t row_begin;
+} xrh_coeff_task;   /* 56 bytes */
+int xrh_coeff_stage(const xrh_coeff_task* tasks_dev, int n_tasks, int64_t total_rows, void* stream);
 
 /* Allocation-free transition densities (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- for example code running
@@ -141,6 +156,16 @@ int xrh_density_build_noalloc(int precision, int64_t K, const int64_t* idx_ptr_d
 
 /* out[c, r] = in[r, c] for a row-major [rows, cols] FP64 matrix. */
 int xrh_transpose(const double* in_dev, int64_t rows, int64_t cols, double* out_dev, void* stream);
+/* Many transposes in one launch: task t transposes in [rows, cols] into out [cols, rows] and
+ * owns the launch's 32 x 32 tiles [tile_begin, tile_begin + ceil(rows/32) * ceil(cols/32))
+ * (tasks sorted by tile_begin, total_tiles the sum). */
+typedef struct {
+    const double* in;
+    double* out;
+    int64_t rows, cols;
+    int64_t tile_begin;
+} xrh_transpose_task;   /* 40 bytes */
+int xrh_transpose_grouped(const xrh_transpose_task* tasks_dev, int n_tasks, int64_t total_tiles, void* stream);
 
 /* Mirrored density blocks (no reference counterpart: the reference builds every block):
  * rho^cca(b, k)[I, J, p, q, r] = rho^caa(k, b)[J, I, r, q, p], and likewise cc / aa, c / a.

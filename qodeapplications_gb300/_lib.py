@@ -37,6 +37,8 @@ _SIGS = {
     "xrh_split_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
     "xrh_gemv_rows_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_abt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
+    "xrh_coeff_stage": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_transpose_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
     "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),
     "xrh_inv_sqrt_small": (_i32, [_vp, _i32, _i32, _vp]),
@@ -103,17 +105,16 @@ def register(name, restype, argtypes):
 
 
 class LaunchCounter:
-    """Counts library calls that launch one kernel each (the gpu_launches figure)."""
-    launching = {"xrh_density_accumulate", "xrh_density_accumulate_f32", "xrh_transpose", "xrh_sigma2e", "xrh_gemm_fp64_grouped", "xrh_gemm_simt_grouped",
-                 "xrh_couplings_count", "xrh_couplings_fill", "xrh_gemv_rows", "xrh_gemv_cols",
-                 "xrh_lanczos_normalize", "xrh_density_adjoint", "xrh_ccaa_weighted", "xrh_split_operand",
-                 "xrh_gemm_tc_grouped"}
+    """Counts library calls that launch a kernel (the gpu_launches figure): every entry point
+    except the host-only ones below launches exactly one kernel of this library."""
+    host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems",
+                 "xrh_tc_encode_map", "xrh_state_ctas", "xrh_lanczos_coop_work"}
     count = 0
 
 
 def call(name, *args):
     """Call one ABI function; raise XRHError on a non-zero status."""
-    if name in LaunchCounter.launching:
+    if name not in LaunchCounter.host_only:
         LaunchCounter.count += 1
     st = getattr(lib(), name)(*args)
     if st != XRH_OK:
@@ -159,6 +160,12 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+TRANSPOSE_TASK_DTYPE = np.dtype([("in", np.uint64), ("out", np.uint64), ("rows", np.int64), ("cols", np.int64),
+                                 ("tile_begin", np.int64)])
+assert TRANSPOSE_TASK_DTYPE.itemsize == 40
+COEFF_TASK_DTYPE = np.dtype([("src", np.uint64), ("zT", np.uint64), ("zT32", np.uint64), ("n", np.int64),
+                             ("K", np.int64), ("npad", np.int64), ("row_begin", np.int64)])
+assert COEFF_TASK_DTYPE.itemsize == 56
 ABT_TASK_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("C", np.uint64), ("m", np.int64), ("n", np.int64),
                            ("K", np.int64), ("lda", np.int64), ("ldb", np.int64), ("alpha", np.float64),
                            ("cta_begin", np.int64)])
@@ -183,3 +190,27 @@ TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64)
                        ("diagB", np.uint64), ("batch", np.int64), ("sC", np.int64)])
 assert SEGMENT_DTYPE.itemsize == 72 and TASK_DTYPE.itemsize == 152
 
+
+class Transposes:
+    """A fixed list of transposes (out = in^T for contiguous FP64 [rows, cols] inputs) run as
+    one xrh_transpose_grouped launch."""
+
+    def __init__(self, pairs, device):
+        import torch
+        tab = np.zeros(len(pairs), dtype=TRANSPOSE_TASK_DTYPE)
+        tiles = 0
+        for i, (src, dst, rows, cols) in enumerate(pairs):
+            if src.dtype != torch.float64 or not src.is_contiguous() or not dst.is_contiguous():
+                raise ValueError("grouped transposes need contiguous FP64 tensors")
+            if src.numel() < rows * cols or dst.numel() < rows * cols:
+                raise ValueError("transpose shape larger than its tensors")
+            t = tab[i]
+            t["in"], t["out"], t["rows"], t["cols"], t["tile_begin"] = src.data_ptr(), dst.data_ptr(), rows, cols, tiles
+            tiles += ((rows + 31) // 32) * ((cols + 31) // 32)
+        self.n, self.tiles = len(pairs), tiles
+        self.keep = pairs
+        self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(pairs) else None
+
+    def run(self, stream=None):
+        if self.n:
+            call("xrh_transpose_grouped", ptr(self.dev), self.n, self.tiles, stream_ptr(stream))

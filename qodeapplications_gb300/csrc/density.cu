@@ -107,6 +107,30 @@ __global__ void transpose_kernel(const double* __restrict__ in, int64_t rows, in
     }
 }
 
+// Many transposes in one launch: 32 x 32 tiles, CTA -> task by binary search on tile_begin.
+__global__ void transpose_grouped_kernel(const xrh_transpose_task* __restrict__ tasks, int n_tasks) {
+    __shared__ double tile[32][33];
+    const int64_t bt = blockIdx.x;
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].tile_begin <= bt) lo = mid; else hi = mid - 1;
+    }
+    const xrh_transpose_task& T = tasks[lo];
+    const int64_t local = bt - T.tile_begin;
+    const int64_t tiles_c = (T.cols + 31) / 32;
+    const int64_t c0 = (local % tiles_c) * 32, r0 = (local / tiles_c) * 32;
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int64_t r = r0 + dy, c = c0 + threadIdx.x;
+        if (r < T.rows && c < T.cols) tile[dy][threadIdx.x] = T.in[r * T.cols + c];
+    }
+    __syncthreads();
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int64_t c = c0 + dy, r = r0 + threadIdx.x;
+        if (r < T.rows && c < T.cols) T.out[c * T.rows + r] = tile[threadIdx.x][dy];
+    }
+}
+
 // ---- sigma vector of the two-electron operator ------------------------------------------
 constexpr int kSigThreads = 128;
 constexpr int kSigMaxNk = 256;
@@ -375,7 +399,9 @@ namespace {
 constexpr int kF32Chunk = 64;
 
 // One operator index (and one split of its couplings) per CTA: a 4 x 4 register tile of the
-// n_b x n_k block per thread over a double-buffered ring of gathered coefficient rows.
+// n_b x n_k block per thread over a double-buffered ring of gathered coefficient rows.  FP32
+// chunk sums are folded into FP32 (hi, lo) pairs by TwoSum and fl32(hi + lo) is written: the
+// FP64 pipe, a small fraction of the FP32 rate on this part, stays idle.
 __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const int64_t* __restrict__ idx_ptr,
                                                  const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
                                                  const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb,
@@ -432,11 +458,14 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
         const int t = t0 + threadIdx.x;
         const bool active = t < n_tiles;
         const int i0 = active ? (t / tiles_j) * 4 : 0, j0 = active ? (t % tiles_j) * 4 : 0;
-        double acc[4][4];
+        float acc[4][4], acc_lo[4][4];          // running sums as FP32 (hi, lo) pairs (TwoSum)
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+            for (int b = 0; b < 4; ++b) {
+                acc[a][b] = 0.f;
+                acc_lo[a][b] = 0.f;
+            }
         __syncthreads();
         load_idx(0, 0);
         __syncthreads();
@@ -472,7 +501,12 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
+                    for (int b = 0; b < 4; ++b) {
+                        float sum, err;
+                        xrh_two_sum(acc[a][b], part[a][b], sum, err);
+                        acc[a][b] = sum;
+                        acc_lo[a][b] += err;
+                    }
             }
         }
         if (active) {
@@ -482,8 +516,9 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
                 for (int b = 0; b < 4; ++b) {
                     if (i0 + a >= nb || j0 + b >= nk) continue;
                     double* o = out + (int64_t)(i0 + a) * nk + j0 + b;
-                    if (splits == 1) *o = acc[a][b];
-                    else atomicAdd(o, acc[a][b]);
+                    const double v = xrh_f32_to_f64(__fadd_rn(acc[a][b], acc_lo[a][b]));
+                    if (splits == 1) *o = v;
+                    else atomicAdd(o, v);
                 }
         }
     }
@@ -514,29 +549,71 @@ __global__ void __launch_bounds__(kAccThreads) density_acc_f32_grouped_kernel(co
 }
 
 
+// Coefficient staging for the builds: for every task (one charge sector), zT[k][i] = src[i][k]
+// (FP64, K x n) and zT32[k][i] = fl32(src[i][k]) (FP32, K x npad, columns n.. npad left as
+// they are: zero from allocation).  Thread per row k of the launch (rows of a task start at
+// row_begin; CTAs of 256 rows find their task by binary search).
+__global__ void __launch_bounds__(256) coeff_stage_kernel(const xrh_coeff_task* __restrict__ tasks, int n_tasks,
+                                                          int64_t total_rows) {
+    const int64_t row = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t row0 = (int64_t)blockIdx.x * 256;
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].row_begin <= row0) lo = mid; else hi = mid - 1;
+    }
+    // a CTA's rows may run into the next task: step forward per thread
+    int t = lo;
+    while (t + 1 < n_tasks && tasks[t + 1].row_begin <= row) ++t;
+    if (row >= total_rows) return;
+    const xrh_coeff_task& T = tasks[t];
+    const int64_t k = row - T.row_begin;
+    if (k >= T.K) return;
+    for (int i = 0; i < T.n; ++i) {
+        const double x = T.src[(int64_t)i * T.K + k];
+        if (T.zT) T.zT[k * T.n + i] = x;
+        if (T.zT32) T.zT32[k * T.npad + i] = xrh_f64_to_f32(x);
+    }
+}
+
 // ---- small blocks: one warp per coupling range ----------------------------------------------
-// For blocks with n_b * ceil(n_k / 4) <= 32 R output quads, a CTA per operator index leaves
-// most threads idle and pays three barriers per chunk.  Here a warp owns one unit (an
-// operator index, or a range of at most a few hundred of its couplings): lane l holds the
-// quads (I, 4 jq .. 4 jq + 3) with I * ceil(n_k/4) + jq = l + 32 r, r < R.  The warp reads 32
-// couplings at a time (one per lane, coalesced), then broadcasts each (P with the sign packed
-// in, Q) by shuffle; every lane loads zb[P][I] and the float4 zk[Q][4 jq..] (L1/L2 gathers)
-// and does four FMAs.  FP32 partial sums over each 32 couplings, FP64 running sums.  Units
-// covering a whole index store rhoT[idx] directly; units of a split index add atomically
-// (rhoT zeroed by the caller).
+// For blocks of at most 16 states per side a CTA per operator index leaves most threads idle
+// and pays three barriers per chunk.  Here a warp owns one unit (an operator index, or a range
+// of at most a few hundred of its couplings) and walks its couplings 32 at a time:
+//   * staging: lane l copies the padded FP32 rows zb[P_c] and zk[Q_c] of coupling c = c0 + l
+//     into the warp's shared-memory buffer with cp.async (one instruction gathers 32 rows),
+//     one chunk ahead of the compute, double buffered;
+//   * compute: lane l holds the output quads (I, 4 jq .. 4 jq + 3), I * ceil(n_k/4) + jq =
+//     l + 32 r (r < R); per staged coupling it reads zb[I] and the float4 zk[4 jq..] from
+//     shared memory and the sign by shuffle, and does four FMAs.
+// Accumulation stays off the FP64 pipe (a small fraction of the FP32 rate on this part): FP32
+// partial sums per chunk are folded into FP32 (hi, lo) pairs by TwoSum and fl32(hi + lo) is
+// written to the FP64 rhoT.  Units covering a whole index store rhoT[idx]; units of a split
+// index add atomically (rhoT zeroed by the caller).
+// Staged row: [zb (nbp floats) | zk (nkp floats)], stride = an odd number of float4s.
+constexpr int UNIT_WARPS = 4;
+
+__host__ __device__ __forceinline__ int unit_stride(int nbp, int nkp) {
+    const int q = (nbp + nkp) / 4;
+    return 4 * (q | 1);
+}
+
 template <int R>
-__global__ void __launch_bounds__(256) density_f32_units_kernel(const xrh_dens_task* __restrict__ tasks,
-                                                               const xrh_dens_unit* __restrict__ units,
-                                                               int64_t n_units) {
-    const int lane = threadIdx.x & 31;
-    const int64_t u = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(UNIT_WARPS * 32) density_f32_units_kernel(const xrh_dens_task* __restrict__ tasks,
+                                                                           const xrh_dens_unit* __restrict__ units,
+                                                                           int64_t n_units, int max_stride) {
+    extern __shared__ __align__(16) float usm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t u = (int64_t)blockIdx.x * UNIT_WARPS + warp;
     if (u >= n_units) return;
     const xrh_dens_unit U = units[u];
     const xrh_dens_task& T = tasks[U.task];
     const int nb = T.nb, nk = T.nk;
-    const int nkq = (nk + 3) >> 2, nkp = nkq * 4, nbp = (nb + 3) & ~3;
+    const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3, nbq = nbp >> 2, nkq = nkp >> 2;
+    const int stride = unit_stride(nbp, nkp);
     const int pairs = nb * nkq;
-    if (pairs > 32 * R) return;                      // the host never builds such a unit
+    if (pairs > 32 * R || stride > max_stride) return;      // the host never builds such a unit
+    float* buf0 = usm + (int64_t)warp * 2 * 32 * max_stride;
     const int64_t base = T.idx_ptr[U.idx];
     const int64_t len = T.idx_ptr[U.idx + 1] - base;
     const int64_t c_lo = base + U.c_lo, c_hi = base + U.c_hi;
@@ -550,57 +627,78 @@ __global__ void __launch_bounds__(256) density_f32_units_kernel(const xrh_dens_t
         Iu[r] = act[r] ? pr / nkq : 0;
         jq[r] = act[r] ? pr - (pr / nkq) * nkq : 0;
     }
-    double acc[R][4];
+    float hi[R][4], lo[R][4];
 #pragma unroll
     for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int k = 0; k < 4; ++k) acc[r][k] = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            hi[r][k] = 0.f;
+            lo[r][k] = 0.f;
+        }
     const float* __restrict__ zb = T.zb32;
     const float* __restrict__ zk = T.zk32;
-    for (int64_t c0 = c_lo; c0 < c_hi; c0 += 32) {
+    // stage the chunk starting at c0 into buffer b; returns this lane's sign (0 beyond c_hi)
+    auto stage = [&](int64_t c0, int b) -> float {
         const int64_t c = c0 + lane;
-        int ps = 0, q = 0;                           // padding couplings: row 0 times a zero sign
-        float pad = 0.f;
+        float sg = 0.f;
         if (c < c_hi) {
-            const int p = T.P[c];
-            q = T.Q[c];
-            ps = T.sign[c] < 0 ? ~p : p;
-            pad = 1.f;
+            const int p = T.P[c], q = T.Q[c];
+            sg = T.sign[c] < 0 ? -1.f : 1.f;
+            float* row = buf0 + (b * 32 + lane) * max_stride;
+            const float* zbr = zb + (int64_t)p * nbp;
+            const float* zkr = zk + (int64_t)q * nkp;
+            for (int x = 0; x < nbq; ++x) cp_async16_ca(row + 4 * x, zbr + 4 * x);
+            for (int x = 0; x < nkq; ++x) cp_async16_ca(row + nbp + 4 * x, zkr + 4 * x);
         }
+        cp_async_commit();
+        return sg;
+    };
+    float s_cur = stage(c_lo, 0);
+    int b = 0;
+    for (int64_t c0 = c_lo; c0 < c_hi; c0 += 32) {
+        float s_next = 0.f;
+        if (c0 + 32 < c_hi) {
+            s_next = stage(c0 + 32, b ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const float* rows = buf0 + b * 32 * max_stride;
         const int cnt = (int)((c_hi - c0) < 32 ? (c_hi - c0) : 32);
-        const int cnt4 = (cnt + 3) & ~3;
         float part[R][4];
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int k = 0; k < 4; ++k) part[r][k] = 0.f;
-        for (int t = 0; t < cnt4; t += 4) {
+#pragma unroll 4
+        for (int t = 0; t < cnt; ++t) {
+            const float st = __shfl_sync(0xffffffffu, s_cur, t);
+            const float* row = rows + t * max_stride;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int pst = __shfl_sync(0xffffffffu, ps, t + e);
-                const int qt = __shfl_sync(0xffffffffu, q, t + e);
-                const float live = __shfl_sync(0xffffffffu, pad, t + e);
-                const int pt = pst < 0 ? ~pst : pst;
-                const float st = pst < 0 ? -live : live;
-                const float* zbr = zb + (int64_t)pt * nbp;
-                const float4* zkr = reinterpret_cast<const float4*>(zk + (int64_t)qt * nkp);
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    if (act[r]) {
-                        const float a = st * __ldg(zbr + Iu[r]);
-                        const float4 b4 = __ldg(zkr + jq[r]);
-                        part[r][0] = fmaf(a, b4.x, part[r][0]);
-                        part[r][1] = fmaf(a, b4.y, part[r][1]);
-                        part[r][2] = fmaf(a, b4.z, part[r][2]);
-                        part[r][3] = fmaf(a, b4.w, part[r][3]);
-                    }
+            for (int r = 0; r < R; ++r) {
+                if (act[r]) {
+                    const float a = st * row[Iu[r]];
+                    const float4 b4 = *reinterpret_cast<const float4*>(row + nbp + 4 * jq[r]);
+                    part[r][0] = fmaf(a, b4.x, part[r][0]);
+                    part[r][1] = fmaf(a, b4.y, part[r][1]);
+                    part[r][2] = fmaf(a, b4.z, part[r][2]);
+                    part[r][3] = fmaf(a, b4.w, part[r][3]);
                 }
             }
         }
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int k = 0; k < 4; ++k) acc[r][k] += (double)part[r][k];
+            for (int k = 0; k < 4; ++k) {
+                float sum, err;
+                xrh_two_sum(hi[r][k], part[r][k], sum, err);
+                hi[r][k] = sum;
+                lo[r][k] += err;
+            }
+        __syncwarp();                                  // buffer b is restaged two chunks on
+        s_cur = s_next;
+        b ^= 1;
     }
     double* out = T.rhoT + (int64_t)U.idx * nb * nk;
 #pragma unroll
@@ -610,12 +708,14 @@ __global__ void __launch_bounds__(256) density_f32_units_kernel(const xrh_dens_t
         for (int k = 0; k < 4; ++k) {
             const int J = 4 * jq[r] + k;
             if (J >= nk) continue;
+            const double v = xrh_f32_to_f64(__fadd_rn(hi[r][k], lo[r][k]));
             double* o = out + (int64_t)Iu[r] * nk + J;
-            if (whole) *o = acc[r][k];
-            else atomicAdd(o, acc[r][k]);
+            if (whole) *o = v;
+            else atomicAdd(o, v);
         }
     }
 }
+
 }  // namespace
 
 extern "C" int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev, int n_tasks, int64_t total_ctas,
@@ -655,22 +755,47 @@ extern "C" int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* 
 }
 
 extern "C" int xrh_density_accumulate_f32_units(const xrh_dens_task* tasks_dev, int n_tasks,
-                                                const xrh_dens_unit* units_dev, int64_t n_units, int max_pairs,
+                                                const xrh_dens_unit* units_dev, int64_t n_units, int max_n,
                                                 void* stream) {
-    if (n_tasks < 0 || n_units < 0 || max_pairs <= 0) return XRH_ERR_ARG;
+    if (n_tasks < 0 || n_units < 0 || max_n <= 0) return XRH_ERR_ARG;
+    if (max_n > 16) return XRH_ERR_CAPACITY;
     if (n_tasks == 0 || n_units == 0) return XRH_OK;
     if (!tasks_dev || !units_dev) return XRH_ERR_ARG;
-    const int64_t ctas = (n_units + 7) / 8;
+    const int64_t ctas = (n_units + UNIT_WARPS - 1) / UNIT_WARPS;
     if (ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    const int np = (max_n + 3) & ~3;
+    const int max_stride = unit_stride(np, np);     // 4 (q | 1) grows with q: the largest stride
+    const size_t smem = sizeof(float) * (size_t)UNIT_WARPS * 2 * 32 * (size_t)max_stride;
     cudaStream_t s = (cudaStream_t)stream;
-    if (max_pairs <= 32)
-        density_f32_units_kernel<1><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
-    else if (max_pairs <= 64)
-        density_f32_units_kernel<2><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
-    else if (max_pairs <= 128)
-        density_f32_units_kernel<4><<<(unsigned)ctas, 256, 0, s>>>(tasks_dev, units_dev, n_units);
+    // output quads per warp: max_n * ceil(max_n / 4) <= 64
+    if (max_n * ((max_n + 3) / 4) <= 32)
+        density_f32_units_kernel<1><<<(unsigned)ctas, UNIT_WARPS * 32, smem, s>>>(tasks_dev, units_dev, n_units,
+                                                                                  max_stride);
     else
-        return XRH_ERR_CAPACITY;
+        density_f32_units_kernel<2><<<(unsigned)ctas, UNIT_WARPS * 32, smem, s>>>(tasks_dev, units_dev, n_units,
+                                                                                  max_stride);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_coeff_stage(const xrh_coeff_task* tasks_dev, int n_tasks, int64_t total_rows, void* stream) {
+    if (n_tasks < 0 || total_rows < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_rows == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    const int64_t ctas = (total_rows + 255) / 256;
+    if (ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    coeff_stage_kernel<<<(unsigned)ctas, 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks, total_rows);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_transpose_grouped(const xrh_transpose_task* tasks_dev, int n_tasks, int64_t total_tiles,
+                                     void* stream) {
+    if (n_tasks < 0 || total_tiles < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_tiles == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_tiles > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    transpose_grouped_kernel<<<(unsigned)total_tiles, dim3(32, 8), 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -25,9 +25,11 @@ __device__ __forceinline__ int find_task(const xrh_gemm_task* __restrict__ tasks
     return lo;
 }
 
-// T = double: the plain FP64 path.  T = float: operands rounded to FP32 in shared memory,
-// products and the partial sum of each 16-wide K step in FP32, running sums in FP64 (used
-// for the adjoint on the split-precision paths).
+// T = double: the plain FP64 path.  T = float (the adjoint on the split-precision paths):
+// operands rounded to FP32 (by integer operations) into shared memory, products and partial
+// sums of each 32 K in FP32, running sums as FP32 (hi, lo) pairs by TwoSum, results written
+// as fl32(hi + lo).  Nothing of the float variant runs on the FP64 pipe, a small fraction of
+// the FP32 rate on this part.
 template <typename T_>
 __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __restrict__ tasks, int n_tasks,
                                                       const xrh_gemm_segment* __restrict__ segs) {
@@ -45,17 +47,27 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
     local -= split * tiles_m * tiles_n;
     const int64_t m0 = (local / tiles_n) * BM, n0 = (local % tiles_n) * BN;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4];
+    constexpr bool F32 = sizeof(T_) == 4;
+    double acc[4][4];                  // FP64 variant
+    float hi[4][4], lo[4][4];          // FP32 variant
+    T_ part[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < 4; ++j) {
+            acc[i][j] = 0.0;
+            hi[i][j] = 0.f;
+            lo[i][j] = 0.f;
+            part[i][j] = (T_)0;
+        }
+    int pending = 0;                   // K steps summed in part since the last fold
 
     for (int64_t s = Tk.seg_begin; s < Tk.seg_begin + Tk.seg_count; ++s) {
         const xrh_gemm_segment S = segs[s];
         const double* __restrict__ Ap = S.A + bidx * S.sA;
         const double* __restrict__ Bp = S.B + bidx * S.sB;
         const bool at = (S.flags & 1) != 0, bt = (S.flags & 2) != 0;
+        const float alpha32 = F32 ? xrh_f64_to_f32(S.alpha) : 0.f;
         int64_t kb = 0, ke = S.K;
         if (Tk.splitk > 1) {
             const int64_t per = (S.K + Tk.splitk - 1) / Tk.splitk;
@@ -73,20 +85,19 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
                 {
                     const int rr = at ? r2 : r, cc = at ? c2 : c;
                     const int64_t gm = m0 + rr, gk = k0 + cc;
-                    As[cc][rr] = (T_)((gm < Tk.M && gk < ke) ? S.alpha * (at ? Ap[gk * S.lda + gm] : Ap[gm * S.lda + gk]) : 0.0);
+                    const double x = (gm < Tk.M && gk < ke) ? (at ? Ap[gk * S.lda + gm] : Ap[gm * S.lda + gk]) : 0.0;
+                    if constexpr (F32) As[cc][rr] = alpha32 * xrh_f64_to_f32(x);
+                    else As[cc][rr] = S.alpha * x;
                 }
                 {
                     const int rr = bt ? r2 : r, cc = bt ? c2 : c;
                     const int64_t gn = n0 + rr, gk = k0 + cc;
-                    Bs[cc][rr] = (T_)((gn < Tk.N && gk < ke) ? (bt ? Bp[gk * S.ldb + gn] : Bp[gn * S.ldb + gk]) : 0.0);
+                    const double x = (gn < Tk.N && gk < ke) ? (bt ? Bp[gk * S.ldb + gn] : Bp[gn * S.ldb + gk]) : 0.0;
+                    if constexpr (F32) Bs[cc][rr] = xrh_f64_to_f32(x);
+                    else Bs[cc][rr] = x;
                 }
             }
             __syncthreads();
-            T_ part[4][4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) part[i][j] = (T_)0;
 #pragma unroll
             for (int kk = 0; kk < BK; ++kk) {
                 T_ a[4], b[4];
@@ -99,11 +110,40 @@ __global__ void __launch_bounds__(NT) gemm_fp64_kernel(const xrh_gemm_task* __re
 #pragma unroll
                     for (int j = 0; j < 4; ++j) part[i][j] = fma(a[i], b[j], part[i][j]);
             }
+            if constexpr (F32) {
+                if (++pending == 2) {          // fold every 32 products
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+                    for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] += (double)part[i][j];
+                        for (int j = 0; j < 4; ++j) {
+                            float sum, err;
+                            xrh_two_sum(hi[i][j], (float)part[i][j], sum, err);
+                            hi[i][j] = sum;
+                            lo[i][j] += err;
+                            part[i][j] = (T_)0;
+                        }
+                    pending = 0;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        acc[i][j] += (double)part[i][j];
+                        part[i][j] = (T_)0;
+                    }
+            }
         }
+    }
+    if constexpr (F32) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float sum, err;
+                xrh_two_sum(hi[i][j], (float)part[i][j], sum, err);
+                acc[i][j] = xrh_f32_to_f64(__fadd_rn(sum, lo[i][j] + err));
+            }
     }
 
 #pragma unroll

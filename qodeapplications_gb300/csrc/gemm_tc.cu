@@ -372,16 +372,19 @@ __device__ __forceinline__ void split_group(const double* __restrict__ src, int6
     const int64_t r = t / groups;
     const int64_t k0 = (t - r * groups) * 4;
     const double* srow = src + r * ld;
-    double x[4];
+    // x rounded to FP32 by integer operations; hi from it and lo = x32 - hi, exact in FP32 (it
+    // keeps the low mantissa bits of x32); the part of x below FP32 (2^-24 |x|) lies under
+    // lo's own resolution.  No FP64 arithmetic: the FP64 pipe is slow on this part.
+    float x[4];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) x[e] = (k0 + e < K) ? __ldg(srow + k0 + e) : 0.0;
+    for (int e = 0; e < 4; ++e) x[e] = (k0 + e < K) ? xrh_f64_to_f32(__ldg(srow + k0 + e)) : 0.f;
     const int64_t o = r * Kp + k0;
     if constexpr (KIND == 0) {
         __nv_bfloat16 h[4], l[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            h[e] = __float2bfloat16_rn((float)x[e]);
-            l[e] = __float2bfloat16_rn((float)(x[e] - (double)__bfloat162float(h[e])));
+            h[e] = __float2bfloat16_rn(x[e]);
+            l[e] = __float2bfloat16_rn(__fsub_rn(x[e], __bfloat162float(h[e])));
         }
         *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(hi) + o) = *reinterpret_cast<uint2*>(h);
         *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(lo) + o) = *reinterpret_cast<uint2*>(l);
@@ -389,9 +392,9 @@ __device__ __forceinline__ void split_group(const double* __restrict__ src, int6
         uint32_t h[4], l[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h[e]) : "f"((float)x[e]));
-            const double rem = x[e] - (double)__uint_as_float(h[e]);
-            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l[e]) : "f"((float)rem));
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h[e]) : "f"(x[e]));
+            const float rem = __fsub_rn(x[e], __uint_as_float(h[e]));
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l[e]) : "f"(rem));
         }
         *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(hi) + o) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(lo) + o) = make_uint4(l[0], l[1], l[2], l[3]);

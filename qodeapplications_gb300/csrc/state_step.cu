@@ -33,8 +33,8 @@ __device__ __forceinline__ int find_task(const xrh_state_task* __restrict__ t, i
 }
 
 // One CTA: C (m x n) += alpha * A[:, k_begin:k_end] B[:, k_begin:k_end]^T, m, n <= 64.
-// ACC is the type of the per-chunk sums (FP32 for float inputs: at most GR_KCHUNK products
-// are summed in FP32 before each FP64 fold).
+// ACC is the type of the per-chunk sums; with FP32 inputs the chunk sums (GR_KCHUNK products)
+// are folded into FP32 (hi, lo) pairs by TwoSum, keeping the FP64 pipe out of the loop.
 // With AT, A is given transposed (K x m, row stride m) as AT_main + AT_add (AT_add may be null),
 // staged with loads that run along the contiguous chunk.
 template <typename T, typename ACC, bool AT>
@@ -43,9 +43,15 @@ __device__ __forceinline__ void abt_slice(const T* __restrict__ A, int64_t lda, 
                                           int64_t k_end, double alpha, double* __restrict__ C,
                                           T (*sa)[GR_KCHUNK + 1], T (*sb)[GR_KCHUNK + 1]) {
     const int mn = m * n;
-    double acc[16];
+    constexpr bool F32 = sizeof(ACC) == 4;
+    double acc[16];                    // FP64 sums (FP64 inputs)
+    float hi[16], lo[16];              // FP32 (hi, lo) TwoSum pairs (FP32 inputs)
 #pragma unroll
-    for (int u = 0; u < 16; ++u) acc[u] = 0.0;
+    for (int u = 0; u < 16; ++u) {
+        acc[u] = 0.0;
+        hi[u] = 0.f;
+        lo[u] = 0.f;
+    }
     for (int64_t k0 = k_begin; k0 < k_end; k0 += GR_KCHUNK) {
         __syncthreads();
         for (int e = threadIdx.x; e < 64 * GR_KCHUNK; e += SS_THREADS) {
@@ -76,14 +82,23 @@ __device__ __forceinline__ void abt_slice(const T* __restrict__ A, int64_t lda, 
                 ACC s = ACC(0);
 #pragma unroll 8
                 for (int kk = 0; kk < GR_KCHUNK; ++kk) s = fma((ACC)sa[i][kk], (ACC)sb[j][kk], s);
-                acc[u] += (double)s;
+                if constexpr (F32) {
+                    float sum, err;
+                    xrh_two_sum(hi[u], (float)s, sum, err);
+                    hi[u] = sum;
+                    lo[u] += err;
+                } else {
+                    acc[u] += (double)s;
+                }
             }
         }
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
         const int o = threadIdx.x + u * SS_THREADS;
-        if (o < mn) atomicAdd(C + o, alpha * acc[u]);
+        if (o >= mn) continue;
+        if constexpr (F32) atomicAdd(C + o, alpha * xrh_f32_to_f64(__fadd_rn(hi[u], lo[u])));
+        else atomicAdd(C + o, alpha * acc[u]);
     }
 }
 

@@ -69,6 +69,51 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
                  "l"(gmem_src)
                  : "memory");
 }
+// Error-free FP32 sum (Knuth's TwoSum): s + e == a + b exactly, s = fl(a + b).
+__device__ __forceinline__ void xrh_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Exact FP32 -> FP64 by integer operations (keeps conversions off the FP64 pipe, which is a
+// small fraction of the FP32 rate on this part).  Zero, subnormal, infinite and NaN inputs
+// take the hardware conversion.
+__device__ __forceinline__ double xrh_f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    const uint64_t bits = ((uint64_t)(u >> 31) << 63) | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// FP64 -> FP32 round-to-nearest-even by integer operations (same result as __double2float_rn;
+// zero takes a shortcut, values outside the normal FP32 range the hardware conversion).
+__device__ __forceinline__ float xrh_f64_to_f32(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    if ((b << 1) == 0) return __uint_as_float((uint32_t)(b >> 32) & 0x80000000u);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+    if (e < 897u || e > 1150u) return __double2float_rn(x);
+    uint32_t m = (uint32_t)(b >> 29) & 0x7fffffu;
+    const uint32_t rem = (uint32_t)b & 0x1fffffffu;
+    uint32_t fe = e - 896u;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) {
+        m += 1u;
+        if (m == 0x800000u) {
+            m = 0u;
+            fe += 1u;
+        }
+    }
+    if (fe >= 255u) return __double2float_rn(x);
+    return __uint_as_float(((uint32_t)(b >> 63) << 31) | (fe << 23) | m);
+}
+
+// Same through L1 (gathers with reuse across warps of an SM).
+__device__ __forceinline__ void cp_async16_ca(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem_dst)),
+                 "l"(gmem_src)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }

@@ -231,7 +231,7 @@ def mirror_pairs(space):
     return out
 
 
-UNIT_MAX_PAIRS = 128     # n_b * ceil(n_k / 4) up to which a block takes the warp-per-unit kernel
+UNIT_MAX_STATES = 16     # blocks with at most this many states per side take the warp-per-unit kernel
 UNIT_COUPLINGS = 256     # couplings per unit at most
 
 
@@ -273,13 +273,13 @@ class DensityBuilder:
         dev = space.device
         self.rho = {}
         self._tmp = {}
-        # FP32 path: blocks with few states (nb * ceil(nk / 4) <= 128) go to the warp-per-unit
+        # FP32 path: blocks with few states (<= UNIT_MAX_STATES per side) go to the warp-per-unit
         # kernel; units of split operator indices add atomically into a zeroed arena
         self.f32 = self.precision == _lib.FP32
         self._unit_keys = set()
         if self.f32:
             self._unit_keys = {key for key in space.couplings if key not in self.mirror and
-                               self.n_states_bra[key[1]] * ((self.n_states[key[2]] + 3) // 4) <= UNIT_MAX_PAIRS}
+                               max(self.n_states_bra[key[1]], self.n_states[key[2]]) <= UNIT_MAX_STATES}
         unit_units, split_keys = {}, []
         for key in sorted(self._unit_keys, key=str):
             cp = space.couplings[key]
@@ -300,15 +300,21 @@ class DensityBuilder:
                 self._tmp[(op, bc, kc)] = torch.empty(cp.K * nb * nk, dtype=torch.float64, device=dev)
         self.zT = {c: torch.empty((space.n_conf[c], self.n_states[c]), dtype=torch.float64, device=dev)
                    for c in space.charges}
-        self.zbT = {c: torch.empty((space.n_conf[c], self.n_states_bra[c]), dtype=torch.float64, device=dev)
-                    for c in space.charges}
+        # the bra side is the ket side unless separate bra states are built (mirror off)
+        self.same_bra = bool(mirror) and self.n_states_bra == self.n_states
+        self.zbT = self.zT if self.same_bra else {
+            c: torch.empty((space.n_conf[c], self.n_states_bra[c]), dtype=torch.float64, device=dev)
+            for c in space.charges}
+        self._stage = None
+        self._tr_direct = self._tr_derived = None
         # FP32 path: coefficients converted once per build, rows padded to 16 bytes
         if self.f32:
             pad = lambda n: (n + 3) // 4 * 4
             self.zT32 = {c: torch.zeros((space.n_conf[c], pad(self.n_states[c])), dtype=torch.float32, device=dev)
                          for c in space.charges}
-            self.zbT32 = {c: torch.zeros((space.n_conf[c], pad(self.n_states_bra[c])), dtype=torch.float32, device=dev)
-                          for c in space.charges}
+            self.zbT32 = self.zT32 if self.same_bra else {
+                c: torch.zeros((space.n_conf[c], pad(self.n_states_bra[c])), dtype=torch.float32, device=dev)
+                for c in space.charges}
             # operator strings with few indices (K < 1024, e.g. K = N for a/c) spread the couplings
             # of every index over several CTAs, about 256 couplings each
             self.splits = {}
@@ -339,7 +345,7 @@ class DensityBuilder:
             # the warp-per-unit blocks: tasks (cta_begin unused) and their unit table
             ukeys = sorted(self._unit_keys, key=str)
             utasks = np.zeros(len(ukeys), dtype=_lib.DENS_TASK_DTYPE)
-            ulist, self._max_pairs = [], 1
+            ulist, self._max_n = [], 1
             for i, (op, bc, kc) in enumerate(ukeys):
                 cp = space.couplings[(op, bc, kc)]
                 t = utasks[i]
@@ -349,7 +355,7 @@ class DensityBuilder:
                 t["rhoT"] = self._tmp[(op, bc, kc)].data_ptr()
                 nb, nk = self.n_states_bra[bc], self.n_states[kc]
                 t["K"], t["nb"], t["nk"], t["splits"] = cp.K, nb, nk, 1
-                self._max_pairs = max(self._max_pairs, nb * ((nk + 3) // 4))
+                self._max_n = max(self._max_n, nb, nk)
                 un = unit_units[(op, bc, kc)][0].copy()
                 un["task"] = i
                 ulist.append(un)
@@ -361,18 +367,40 @@ class DensityBuilder:
             self._max_nb = max(self.n_states_bra.values()) if self.n_states_bra else 1
             self._max_nk = max(self.n_states.values()) if self.n_states else 1
 
+    def _stage_coefficients(self, coeffs, bra_coeffs, s):
+        """zT (and zbT) = coefficients transposed, plus their padded FP32 copies on the FP32
+        path, in one launch (task table rebuilt when other coefficient tensors come in)."""
+        sides = [(coeffs, self.zT, self.zT32 if self.f32 else None, self.n_states)]
+        if not self.same_bra:
+            sides.append((coeffs if bra_coeffs is None else bra_coeffs, self.zbT,
+                          self.zbT32 if self.f32 else None, self.n_states_bra))
+        key = tuple(src[c].data_ptr() for src, _, _, _ in sides for c in self.space.charges)
+        if self._stage is None or self._stage[0] != key:
+            tab = np.zeros(len(sides) * len(self.space.charges), dtype=_lib.COEFF_TASK_DTYPE)
+            row, i = 0, 0
+            for src, zt, z32, ns in sides:
+                for c in self.space.charges:
+                    x = src[c]
+                    if x.dtype != torch.float64 or not x.is_contiguous() or x.shape != (ns[c], self.space.n_conf[c]):
+                        raise ValueError("coefficients must be contiguous FP64 (n_states, n_conf) tensors")
+                    t = tab[i]
+                    t["src"], t["zT"] = x.data_ptr(), zt[c].data_ptr()
+                    t["zT32"] = z32[c].data_ptr() if z32 is not None else 0
+                    t["n"], t["K"], t["row_begin"] = ns[c], self.space.n_conf[c], row
+                    t["npad"] = z32[c].shape[1] if z32 is not None else ns[c]
+                    row += self.space.n_conf[c]
+                    i += 1
+            self._stage = (key, torch.from_numpy(tab.view(np.uint8).copy()).to(self.space.device), len(tab), row,
+                           [src for src, _, _, _ in sides])
+        _, tab_dev, n_t, rows, _keep = self._stage
+        call("xrh_coeff_stage", ptr(tab_dev), n_t, rows, s)
+
     def build(self, coeffs, bra_coeffs=None):
         """coeffs: {charge: CUDA float64 tensor (n_states, n_conf)}."""
         s = stream_ptr()
-        if bra_coeffs is not None and self.mirror:
+        if bra_coeffs is not None and (self.mirror or self.same_bra):
             raise ValueError("separate bra coefficients need DensityBuilder(..., mirror=False)")
-        for c in self.space.charges:
-            self.zT[c].copy_(coeffs[c].t())
-            self.zbT[c].copy_((coeffs if bra_coeffs is None else bra_coeffs)[c].t())
-        if self.f32:
-            for c in self.space.charges:
-                self.zT32[c][:, :self.n_states[c]].copy_(self.zT[c])
-                self.zbT32[c][:, :self.n_states_bra[c]].copy_(self.zbT[c])
+        self._stage_coefficients(coeffs, bra_coeffs, s)
         if self.f32:
             for t in self._zero_first:
                 t.zero_()
@@ -383,22 +411,33 @@ class DensityBuilder:
                 if self._unit_zero is not None:
                     self._unit_zero.zero_()
                 call("xrh_density_accumulate_f32_units", ptr(self._unit_tasks), self._n_unit_tasks, ptr(self._units),
-                     self._n_units, self._max_pairs, s)
-        for (op, bc, kc), cp in self.space.couplings.items():
-            if (op, bc, kc) in self.mirror:
-                continue
-            nb, nk = self.n_states_bra[bc], self.n_states[kc]
-            tmp = self._tmp[(op, bc, kc)]
-            if not self.f32:
+                     self._n_units, self._max_n, s)
+        if not self.f32:
+            for (op, bc, kc), cp in self.space.couplings.items():
+                if (op, bc, kc) in self.mirror:
+                    continue
+                nb, nk = self.n_states_bra[bc], self.n_states[kc]
                 call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
-                     ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(tmp), s)
-            call("xrh_transpose", ptr(tmp), cp.K, nb * nk, ptr(self.rho[op][(bc, kc)]), s)
+                     ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(self._tmp[(op, bc, kc)]), s)
+        if self._tr_direct is None:
+            # rho^T [K, nb nk] -> rho [nb nk, K] for the accumulated blocks; the mirrored blocks go
+            # the other way after the mirror kernels (their rho^T feeds the reverse pass)
+            direct, derived = [], []
+            for (op, bc, kc), cp in self.space.couplings.items():
+                nbnk = self.n_states_bra[bc] * self.n_states[kc]
+                tmp, rho = self._tmp[(op, bc, kc)], self.rho[op][(bc, kc)]
+                if (op, bc, kc) in self.mirror:
+                    derived.append((rho, tmp, nbnk, cp.K))
+                else:
+                    direct.append((tmp, rho, cp.K, nbnk))
+            self._tr_direct = _lib.Transposes(direct, self.space.device)
+            self._tr_derived = _lib.Transposes(derived, self.space.device)
+        self._tr_direct.run()
         for (op, bc, kc), (pop, pbc, pkc) in self.mirror.items():
             nb, nk = self.n_states_bra[bc], self.n_states[kc]
-            K = self.space.couplings[(op, bc, kc)].K
             call("xrh_mirror_density", nb, nk, self.space.N, len(op), ptr(self.rho[pop][(pbc, pkc)]),
                  ptr(self.rho[op][(bc, kc)]), 0, s)
-            call("xrh_transpose", ptr(self.rho[op][(bc, kc)]), nb * nk, K, ptr(self._tmp[(op, bc, kc)]), s)
+        self._tr_derived.run()
         return self.rho
 
 

@@ -169,6 +169,7 @@ class XRDimerAdjoint:
                 writers[rho_t.data_ptr()] = writers.get(rho_t.data_ptr(), 0) + 1
         self.l3_tc = plan.tc
         self.l3_T = []
+        self._l3_tr = None
         if plan.tc:
             # tensor cores (split precision, FP32 chunk sums): d rho = dP W on K-major W^T; dW = dP^T rho
             # on rho^T, which the density build leaves in its pre-transpose buffer
@@ -382,7 +383,12 @@ class XRDimerAdjoint:
     def launch_L3(self):
         """The precontraction adjoint (after launches 1 and 2)."""
         if self.l3_tc:
-            for src, dst in self.l3_T:
+            if self._l3_tr is None:
+                flat = [(a, b) for a, b in self.l3_T if a.is_contiguous() and a.dtype == torch.float64]
+                self._l3_tr = _lib.Transposes([(a, b, a.shape[0], a.shape[1]) for a, b in flat], self.plan.device)
+                self._l3_rest = [(a, b) for a, b in self.l3_T if not any(a is x for x, _ in flat)]
+            self._l3_tr.run()
+            for src, dst in self._l3_rest:
                 dst.copy_(src.t())
             self.reg3.split("g")
             self.reg3.split("rhoT")

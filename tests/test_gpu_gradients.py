@@ -212,7 +212,7 @@ def test_fp32_density_adjoint_paths_match_fp64(path, monkeypatch):
     from qodeapplications_gb300.hamiltonian import DeviceIntegrals, XRDimerPlan
     if path == "cta":
         monkeypatch.setattr(Gm, "ADJ_UNIT_MAX", 0)
-        monkeypatch.setattr(D, "UNIT_MAX_PAIRS", 0)
+        monkeypatch.setattr(D, "UNIT_MAX_STATES", 0)
     n_orb, n_st = 6, 8
     sysd = S.make_system(n_frag=2, n_orb=n_orb, n_states=n_st, charges=CHG, seed=43)
     spaces = [D.FragmentSpace({c: sysd["states"][m][c][1] for c in CHG}, n_orb, 0, 4) for m in range(2)]

@@ -76,7 +76,7 @@ def test_density_fp32_paths_match_fp64(path, n_states, monkeypatch):
     the block's largest element (64 couplings or fewer per FP32 partial sum)."""
     from qodeapplications_gb300 import densities as D
     if path == "cta":
-        monkeypatch.setattr(D, "UNIT_MAX_PAIRS", 0)
+        monkeypatch.setattr(D, "UNIT_MAX_STATES", 0)
     sysd = S.make_system(n_frag=2, n_orb=9, n_states=n_states, charges=(+1, 0, -1), seed=5)
     st = sysd["states"][0]
     charges = (+1, 0, -1)
@@ -98,6 +98,29 @@ def test_density_fp32_paths_match_fp64(path, n_states, monkeypatch):
     for op, blocks in again.items():
         for key, t in blocks.items():
             assert torch.equal(t, r32[op][key]) or (t - r32[op][key]).abs().max().item() < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_densities_with_separate_bra_states_match_oracle(precision):
+    """Transition densities between different bra and ket state sets (the determinant-bra
+    densities of the reference's state gradient) through DensityBuilder(mirror=False)."""
+    from qodeapplications_gb300.densities import DensityBuilder, FragmentSpace
+    sysd = _system(n_states=3)
+    charges = (+1, 0, -1)
+    st = sysd["states"][0]
+    rng = np.random.default_rng(8)
+    bra = {c: rng.standard_normal((5, st[c][0].shape[1])) for c in charges}
+    space = FragmentSpace({c: st[c][1] for c in charges}, sysd["n_orb"], 0, 4)
+    b = DensityBuilder(space, {c: 3 for c in charges}, precision=precision, n_states_bra={c: 5 for c in charges},
+                       mirror=False)
+    rho = b.build({c: torch.as_tensor(st[c][0], device="cuda") for c in charges},
+                  bra_coeffs={c: torch.as_tensor(bra[c], device="cuda") for c in charges})
+    N = 2 * sysd["n_orb"]
+    tol = 1e-13 if precision == "fp64" else 2e-6
+    for op, blocks in rho.items():
+        for (bc, kc), t in blocks.items():
+            ref = O.transition_density(op, bra[bc], st[bc][1], st[kc][0], st[kc][1], N, sysd["n_orb"], 0)
+            np.testing.assert_allclose(t.cpu().numpy(), ref, rtol=0, atol=tol * max(1.0, np.abs(ref).max()))
 
 
 def test_monomer_two_electron_matches_oracle():
