@@ -189,62 +189,71 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
     return sum(ms) / 1e3 / steps, Es, it
 
 
-# DRAM bytes (read + write) per launch of the grouped FP32 density build, from one ncu
-# capture of the bench command (profiles/density_acc_f32_grouped_dimer2x9.md); None where
-# no capture exists for the workload
-DENSITY_TRAFFIC_BYTES = {1: 26_977_664}
+# DRAM bytes (read + write) per launch of the dominant kernel (the FP32 density adjoint of
+# one fragment), from one ncu capture of the bench command (profiles/); None where no capture
+# exists for the workload
+DENSITY_ADJ_TRAFFIC_BYTES = {1: None}
 
 
-def density_kernel_work(builder):
-    """Algorithmic bytes and FLOPs of one grouped density launch of a fragment: coupling lists
-    read once (idx_ptr 8 B per index; P, Q 4 B and sign 1 B per coupling), the FP32 coefficient
-    rows read once, rho^T written once (8 B per element); 2 n_b n_k FLOPs per coupling."""
-    sp = builder.space
+def density_adjoint_work(adj, m):
+    """Algorithmic bytes and FLOPs of one FP32 density-adjoint launch of fragment m (all its
+    accumulated blocks): coupling lists read once (P, Q 4 B and sign 1 B per coupling, idx_ptr
+    8 B per index), dE/drho read once (8 B per element), the FP32 coefficient rows read once and
+    the FP32 gradient rows read and written once; 4 n_b n_k FLOPs per coupling (U = zb^T G and
+    W = G zk)."""
+    plan = adj.plan
+    sp = plan.spaces[m]
+    bld = plan.builders[m]
     by, fl = 0.0, 0.0
-    for (op, bc, kc), cp in sp.couplings.items():
-        nb, nk = builder.n_states_bra[bc], builder.n_states[kc]
+    for (mm, op, bc, kc, cp, rt, grho, gT) in adj.dens_adj_all:
+        if mm != m:
+            continue
+        nb, nk = rt.shape[0], rt.shape[1]
         by += 8.0 * (cp.K + 1) + 9.0 * cp.count + 8.0 * cp.K * nb * nk
-        fl += 2.0 * nb * nk * cp.count
+        fl += 4.0 * nb * nk * cp.count
     for c in sp.charges:
-        by += 4.0 * sp.n_conf[c] * (builder.zT32[c].shape[1] + builder.zbT32[c].shape[1])
+        by += 4.0 * sp.n_conf[c] * bld.zT32[c].shape[1] + 8.0 * sp.n_conf[c] * plan.n_states[m][c]
     return by, fl
 
 
 def dominant_kernel_roofline(it, config, reps=20):
     """Live CUDA-event timing, on the launching stream, of the dominant kernel of the step in
-    the ncu launch list (the grouped FP32 density build: one launch per fragment), with the
-    buffers as the last iteration left them."""
+    the ncu launch list: the FP32 density adjoint (dE/dz from dE/drho), one launch per
+    fragment (lane per coupling on unit tables for blocks of at most 16 states, one CTA per
+    operator index above).  Timed with the buffers the last iteration left (the launches add
+    into the gradient buffers, which the next iteration zeroes)."""
     import torch
     from qodeapplications_gb300 import _lib
-    plan = it.opt.plan
-    builders = [b for b in plan.builders if getattr(b, "f32", False)]
-    if not builders:
+    adj = it.opt.adj
+    launches = []
+    for m, (tasks, n_t, units, n_u, mx) in enumerate(getattr(adj, "dens_adj_units", ())):
+        launches.append(("xrh_density_adjoint_f32_units", (_lib.ptr(tasks), n_t, _lib.ptr(units), n_u, mx, 1)))
+    for (tasks, n_t, ctas, mnb, mnk) in adj.dens_adj_groups:
+        launches.append(("xrh_density_adjoint_f32_grouped", (_lib.ptr(tasks), n_t, ctas, mnb, mnk)))
+    if not launches:
         return None
-    work = [density_kernel_work(b) for b in builders]
+    name = launches[0][0]
+    launches = [l for l in launches if l[0] == name]
+    work = [density_adjoint_work(adj, m) for m in (0, 1)]
     stream = torch.cuda.current_stream()
     s = _lib.stream_ptr(stream)
-
-    def launch(b):
-        for t in b._zero_first:
-            t.zero_()
-        _lib.call("xrh_density_accumulate_f32_grouped", _lib.ptr(b._dens_tasks), b._n_dens_tasks, b._dens_ctas,
-                  b._max_nb, b._max_nk, s)
     for _ in range(3):
-        for b in builders:
-            launch(b)
+        for fn, a in launches:
+            _lib.call(fn, *a, s)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(reps):
-        for b in builders:
-            launch(b)
+        for fn, a in launches:
+            _lib.call(fn, *a, s)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / (reps * len(builders))
+    ms = e0.elapsed_time(e1) / (reps * len(launches))
     by = sum(w[0] for w in work) / len(work)
     fl = sum(w[1] for w in work) / len(work)
-    return dict(name="density_acc_f32_grouped_kernel (FP32 density build, one launch per fragment)",
-                ms=ms, bytes=by, flops=fl, traffic=DENSITY_TRAFFIC_BYTES.get(config))
+    kname = ("density_adjoint_units_kernel" if name.endswith("units") else "density_adjoint_f32_grouped_kernel")
+    return dict(name=f"{kname} (FP32 density adjoint, one launch per fragment)", ms=ms, bytes=by, flops=fl,
+                traffic=DENSITY_ADJ_TRAFFIC_BYTES.get(config))
 
 
 def run_ours(args):

@@ -283,6 +283,14 @@ int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const doubl
  * sums and the barrier words, reset by this call).  A barrier wait that exceeds its poll
  * limit sets *status_dev = XRH_ERR_TIMEOUT and the kernel returns early; *status_dev must be
  * XRH_OK on entry. */
+/* The same loop inside one thread-block cluster (8 or 16 CTAs, one per SM; hardware cluster
+ * barriers, partial sums and V[j+1] exchanged through distributed shared memory, H rows kept
+ * in shared memory when they fit).  XRH_ERR_CAPACITY when the sector does not fit the
+ * cluster's shared memory (then use xrh_lanczos_coop). */
+int xrh_lanczos_cluster(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
+                        double* alpha_dev, double* beta_dev, void* stream);
+/* 1 when xrh_lanczos_cluster can take an n x n sector and m steps on the current device. */
+int xrh_lanczos_cluster_fits(int n, int m);
 int64_t xrh_lanczos_coop_work(int m);
 int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
                      double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
@@ -329,7 +337,7 @@ int xrh_left_multiply(const xrh_state_task* tasks_dev, int n_tasks, int64_t tota
 int xrh_abt_small(int precision, int m, int n, int64_t K, const void* A_dev, int64_t lda,
                   const void* B_dev, int64_t ldb, double alpha, double* C_dev, void* stream);
 /* A table of such products in one launch: task t owns CTAs [cta_begin, cta_begin +
- * xrh_state_ctas(K)) (tasks sorted by cta_begin, total_ctas the sum), m, n <= 64, C row
+ * xrh_abt_ctas(K)) (tasks sorted by cta_begin, total_ctas the sum), m, n <= 64, C row
  * stride n.  Used for E2 = Zb sigma^T, the monomer two-electron blocks
  * (general-XRCC/build_density_tensors.py:122-133 folds them into ccaa numbers). */
 typedef struct {
@@ -339,7 +347,9 @@ typedef struct {
     int64_t m, n, K, lda, ldb;
     double alpha;
     int64_t cta_begin;
-} xrh_abt_task;   /* 80 bytes */
+    int64_t flags;    /* bit 0: A stored K-major (A[i][k] = A[k*lda + i]); bit 1: B likewise */
+} xrh_abt_task;   /* 88 bytes */
+int xrh_abt_ctas(int64_t K);
 int xrh_abt_grouped(int precision, const xrh_abt_task* tasks_dev, int n_tasks, int64_t total_ctas,
                     void* stream);
 

@@ -32,8 +32,11 @@ _SIGS = {
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xrh_lanczos_coop_work": (_i64, [_i32]),
+    "xrh_lanczos_cluster": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "xrh_lanczos_cluster_fits": (_i32, [_i32, _i32]),
     "xrh_lanczos_coop": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "xrh_state_ctas": (_i32, [_i64]),
+    "xrh_abt_ctas": (_i32, [_i64]),
     "xrh_split_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
     "xrh_gemv_rows_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_abt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
@@ -108,7 +111,8 @@ class LaunchCounter:
     """Counts library calls that launch a kernel (the gpu_launches figure): every entry point
     except the host-only ones below launches exactly one kernel of this library."""
     host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems",
-                 "xrh_tc_encode_map", "xrh_state_ctas", "xrh_lanczos_coop_work"}
+                 "xrh_tc_encode_map", "xrh_state_ctas", "xrh_abt_ctas", "xrh_lanczos_coop_work",
+                 "xrh_lanczos_cluster_fits"}
     count = 0
 
 
@@ -168,8 +172,8 @@ COEFF_TASK_DTYPE = np.dtype([("src", np.uint64), ("zT", np.uint64), ("zT32", np.
 assert COEFF_TASK_DTYPE.itemsize == 56
 ABT_TASK_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("C", np.uint64), ("m", np.int64), ("n", np.int64),
                            ("K", np.int64), ("lda", np.int64), ("ldb", np.int64), ("alpha", np.float64),
-                           ("cta_begin", np.int64)])
-assert ABT_TASK_DTYPE.itemsize == 80
+                           ("cta_begin", np.int64), ("flags", np.int64)])
+assert ABT_TASK_DTYPE.itemsize == 88
 GEMV_TASK_DTYPE = np.dtype([("A", np.uint64), ("x", np.uint64), ("y", np.uint64), ("rows", np.int64),
                             ("cols", np.int64), ("lda", np.int64), ("alpha", np.float64), ("beta", np.float64),
                             ("row_begin", np.int64)])

@@ -33,7 +33,7 @@ static_assert(sizeof(xrh_dens_adj_task) == 96, "xrh_dens_adj_task layout is part
 static_assert(sizeof(xrh_dens_adj_tc_task) == 112, "xrh_dens_adj_tc_task layout is part of the ABI");
 static_assert(sizeof(xrh_transpose_task) == 40, "xrh_transpose_task layout is part of the ABI");
 static_assert(sizeof(xrh_coeff_task) == 56, "xrh_coeff_task layout is part of the ABI");
-static_assert(sizeof(xrh_abt_task) == 80, "xrh_abt_task layout is part of the ABI");
+static_assert(sizeof(xrh_abt_task) == 88, "xrh_abt_task layout is part of the ABI");
 static_assert(sizeof(xrh_gemv_task) == 72, "xrh_gemv_task layout is part of the ABI");
 static_assert(sizeof(xrh_split_task) == 64, "xrh_split_task layout is part of the ABI");
 static_assert(sizeof(xrh_dens_unit) == 16, "xrh_dens_unit layout is part of the ABI");

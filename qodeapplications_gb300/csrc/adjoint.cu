@@ -373,8 +373,8 @@ __global__ void __launch_bounds__(256) density_adjoint_units_kernel(const xrh_de
         const int I = e / MP, J = e - I * MP;
         float v = 0.f;
         if (I < nb && J < nk)
-            v = (float)(g_layout == 0 ? T.gT[((int64_t)U.idx * nb + I) * nk + J]
-                                      : T.gT[((int64_t)I * nk + J) * T.K + U.idx]);
+            v = xrh_f64_to_f32(g_layout == 0 ? T.gT[((int64_t)U.idx * nb + I) * nk + J]
+                                             : T.gT[((int64_t)I * nk + J) * T.K + U.idx]);
         g[I][J] = v;
     }
     __syncwarp();

@@ -8,6 +8,8 @@
 //   xrh_lanczos_normalize: beta[k] = ||w||, v = w / beta[k]  (one CTA; the norm stays on the
 //       device so the whole Krylov loop can be replayed as one CUDA graph)
 // All FP64: the eigensolve is kept in double precision on every precision path.
+#include <cooperative_groups.h>
+
 #include "xrh_common.cuh"
 
 namespace {
@@ -251,11 +253,27 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
         }
         for (int r = warp; r < nr; r += LC_WARPS) {
             const double* h = H + (r0 + r) * ld;
-            double s = 0.0;
-            if (stage_v)
-                for (int64_t k = lane; k < n; k += 32) s = fma(h[k], vst[k], s);
-            else
-                for (int64_t k = lane; k < n; k += 32) s = fma(h[k], __ldcg(vj + k), s);
+            // four independent chains: the FP64 latency, not its rate, bounds a single chain
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int64_t k = lane;
+            if (stage_v) {
+                for (; k + 96 < n; k += 128) {
+                    s0 = fma(h[k], vst[k], s0);
+                    s1 = fma(h[k + 32], vst[k + 32], s1);
+                    s2 = fma(h[k + 64], vst[k + 64], s2);
+                    s3 = fma(h[k + 96], vst[k + 96], s3);
+                }
+                for (; k < n; k += 32) s0 = fma(h[k], vst[k], s0);
+            } else {
+                for (; k + 96 < n; k += 128) {
+                    s0 = fma(h[k], __ldcg(vj + k), s0);
+                    s1 = fma(h[k + 32], __ldcg(vj + k + 32), s1);
+                    s2 = fma(h[k + 64], __ldcg(vj + k + 64), s2);
+                    s3 = fma(h[k + 96], __ldcg(vj + k + 96), s3);
+                }
+                for (; k < n; k += 32) s0 = fma(h[k], __ldcg(vj + k), s0);
+            }
+            double s = (s0 + s1) + (s2 + s3);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) w[r] = s;
@@ -283,9 +301,16 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
             __syncthreads();
             a += c[j];
             for (int r = tid; r < nr; r += LC_THREADS) {
-                double s = 0.0;
-                for (int i = 0; i <= j; ++i) s = fma(c[i], Vs[(int64_t)i * rows_max + r], s);
-                w[r] -= s;
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                int i = 0;
+                for (; i + 3 <= j; i += 4) {
+                    s0 = fma(c[i], Vs[(int64_t)i * rows_max + r], s0);
+                    s1 = fma(c[i + 1], Vs[(int64_t)(i + 1) * rows_max + r], s1);
+                    s2 = fma(c[i + 2], Vs[(int64_t)(i + 2) * rows_max + r], s2);
+                    s3 = fma(c[i + 3], Vs[(int64_t)(i + 3) * rows_max + r], s3);
+                }
+                for (; i <= j; ++i) s0 = fma(c[i], Vs[(int64_t)i * rows_max + r], s0);
+                w[r] -= (s0 + s1) + (s2 + s3);
             }
             if (pass == 1) {
                 for (int i = 0; i <= j; ++i) cc2 = fma(c[i], c[i], cc2);
@@ -309,6 +334,143 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
     }
 }
 
+
+// ---- the Krylov loop in one thread-block cluster ----------------------------------------
+// For sectors whose rows of H fit in the shared memory of a cluster (up to 16 CTAs, one per
+// SM), the loop runs inside one cluster: CTA b owns rows [r0, r1) of H (kept in its shared
+// memory for the whole loop when they fit), of V and of w, and a full copy of V[j].  Partial
+// dot products and the slices of V[j+1] are exchanged through distributed shared memory at
+// hardware cluster barriers (three per step: after each Gram-Schmidt pass's partial dots and
+// after V[j+1]); every CTA sums the partials in the same CTA order, so all hold identical
+// coefficients.  Same recurrence as lanczos_coop_kernel (beta^2 = |w|^2 - |c'|^2 after the
+// second pass).
+namespace cg = cooperative_groups;
+constexpr int LK_THREADS = 512;
+constexpr int LK_WARPS = LK_THREADS / 32;
+
+__global__ void __launch_bounds__(LK_THREADS, 1) lanczos_cluster_kernel(int n, int m, const double* __restrict__ H,
+                                                                   int64_t ld, const double* __restrict__ v0,
+                                                                   double* __restrict__ V, double* __restrict__ alpha,
+                                                                   double* __restrict__ beta, int rows_max, int h_smem) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned int nb = cluster.num_blocks(), b = cluster.block_rank();
+    extern __shared__ __align__(16) double lsm[];
+    const int r0 = (int)((int64_t)b * n / nb), r1 = (int)((int64_t)(b + 1) * n / nb);
+    const int nr = r1 - r0;
+    const int ms = m + 2;
+    double* vfull = lsm;                              // [n]      V[j] whole
+    double* Vs = vfull + n;                           // [m+1][rows_max] own rows of V
+    double* w = Vs + (int64_t)(m + 1) * rows_max;     // [rows_max]
+    double* vslice = w + rows_max;                    // [rows_max] own rows of V[j+1] for the peers
+    double* pa = vslice + rows_max;                   // [ms]     pass-1 partial dots of this CTA
+    double* pb = pa + ms;                             // [ms]     pass-2 partial dots (+ |w|^2)
+    double* c = pb + ms;                              // [ms]     summed coefficients
+    double* Hs = c + ms;                              // [nr][n]  own rows of H (when h_smem)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (h_smem)
+        for (int64_t e = tid; e < (int64_t)nr * n; e += LK_THREADS) {
+            const int r = (int)(e / n), k = (int)(e - (int64_t)r * n);
+            Hs[e] = H[(int64_t)(r0 + r) * ld + k];
+        }
+    for (int k = tid; k < n; k += LK_THREADS) vfull[k] = v0[k];
+    for (int r = tid; r < nr; r += LK_THREADS) {
+        Vs[r] = v0[r0 + r];
+        V[r0 + r] = v0[r0 + r];
+    }
+    __syncthreads();
+    for (int j = 0; j < m; ++j) {
+        for (int r = warp; r < nr; r += LK_WARPS) {
+            const double* h = h_smem ? Hs + (int64_t)r * n : H + (int64_t)(r0 + r) * ld;
+            // four independent chains (the FP64 latency, not its rate, bounds this loop)
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int k = lane;
+            for (; k + 96 < n; k += 128) {
+                s0 = fma(h[k], vfull[k], s0);
+                s1 = fma(h[k + 32], vfull[k + 32], s1);
+                s2 = fma(h[k + 64], vfull[k + 64], s2);
+                s3 = fma(h[k + 96], vfull[k + 96], s3);
+            }
+            for (; k < n; k += 32) s0 = fma(h[k], vfull[k], s0);
+            double s = (s0 + s1) + (s2 + s3);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) w[r] = s;
+        }
+        double a = 0.0, cc2 = 0.0;
+        for (int pass = 0; pass < 2; ++pass) {
+            double* pp = pass == 0 ? pa : pb;
+            const int cnt = j + 1 + pass;
+            __syncthreads();
+            for (int i = warp; i < cnt; i += LK_WARPS) {
+                double s = 0.0;
+                if (i <= j)
+                    for (int r = lane; r < nr; r += 32) s = fma(Vs[(int64_t)i * rows_max + r], w[r], s);
+                else
+                    for (int r = lane; r < nr; r += 32) s = fma(w[r], w[r], s);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) pp[i] = s;
+            }
+            cluster.sync();
+            // c[i] = sum over the CTAs: warp per i, lane q reads CTA q's partial (one
+            // distributed-shared-memory round trip), fixed shuffle tree (same order everywhere)
+            for (int i = warp; i < cnt; i += LK_WARPS) {
+                double s = lane < (int)nb ? cluster.map_shared_rank(pp, (unsigned int)lane)[i] : 0.0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) c[i] = s;
+            }
+            __syncthreads();
+            if (pass == 1 && warp == LK_WARPS - 1) {
+                // |c'|^2 by one warp (lanes over i, fixed shuffle tree) into c[m + 1], read after
+                // the barrier below the pass loop
+                double q = 0.0;
+                for (int i = lane; i <= j; i += 32) q = fma(c[i], c[i], q);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+                if (lane == 0) c[m + 1] = c[j + 1] - q;
+            }
+            a += c[j];
+            for (int r = tid; r < nr; r += LK_THREADS) {
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                int i = 0;
+                for (; i + 3 <= j; i += 4) {
+                    s0 = fma(c[i], Vs[(int64_t)i * rows_max + r], s0);
+                    s1 = fma(c[i + 1], Vs[(int64_t)(i + 1) * rows_max + r], s1);
+                    s2 = fma(c[i + 2], Vs[(int64_t)(i + 2) * rows_max + r], s2);
+                    s3 = fma(c[i + 3], Vs[(int64_t)(i + 3) * rows_max + r], s3);
+                }
+                for (; i <= j; ++i) s0 = fma(c[i], Vs[(int64_t)i * rows_max + r], s0);
+                w[r] -= (s0 + s1) + (s2 + s3);
+            }
+        }
+        __syncthreads();
+        cc2 = c[m + 1];
+        const double bj = sqrt(cc2 > 0.0 ? cc2 : 0.0);
+        const double inv = bj > 0.0 ? 1.0 / bj : 0.0;
+        for (int r = tid; r < nr; r += LK_THREADS) {
+            const double x = w[r] * inv;
+            Vs[(int64_t)(j + 1) * rows_max + r] = x;
+            vslice[r] = x;
+            V[(int64_t)(j + 1) * n + r0 + r] = x;
+        }
+        if (b == 0 && tid == 0) {
+            alpha[j] = a;
+            beta[j] = bj;
+        }
+        cluster.sync();
+        for (int k = tid; k < n; k += LK_THREADS) {
+            // owner of row k: the largest q with q n / nb <= k
+            unsigned int q = (unsigned int)(((int64_t)k * nb) / n);
+            while (q + 1 < nb && (int)((int64_t)(q + 1) * n / nb) <= k) ++q;
+            while (q > 0 && (int)((int64_t)q * n / nb) > k) --q;
+            vfull[k] = cluster.map_shared_rank(vslice, q)[k - (int)((int64_t)q * n / nb)];
+        }
+        // vslice is rewritten at the end of the next step, two cluster barriers later
+        __syncthreads();
+    }
+    cluster.sync();                                   // peers may still read this CTA's smem
+}
 }  // namespace
 
 extern "C" int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
@@ -411,6 +573,113 @@ extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t l
                     (void*)&beta_dev, (void*)&part, (void*)&count, (void*)&status_dev, &rows_arg, &stage_arg};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_coop_kernel, dim3((unsigned)nb),
                                                       dim3(LC_THREADS), args, smem, s);
+    if (e != cudaSuccess) {
+        xrh_set_last_cuda_error((int)e);
+        return XRH_ERR_CUDA;
+    }
+    return XRH_OK;
+}
+
+// Shared memory (bytes) of the cluster loop for a given split; 0 when it does not fit.
+static size_t lanczos_cluster_smem(int n, int m, int nb, int h_smem, int smem_optin) {
+    const int rows_max = (n + nb - 1) / nb;
+    size_t d = (size_t)n + (size_t)(m + 1) * rows_max + 2 * (size_t)rows_max + 3 * (size_t)(m + 2);
+    if (h_smem) d += (size_t)rows_max * n;
+    const size_t bytes = d * sizeof(double);
+    return bytes <= (size_t)smem_optin ? bytes : 0;
+}
+
+// Cluster size (16 CTAs when the part schedules such clusters with the needed shared memory,
+// else 8), H in shared memory or not, and the shared memory per CTA for an n x n sector and m
+// steps.  Decided once per shape (on the first, eager call) and cached, so no occupancy query
+// runs inside a stream capture.  Returns false when no cluster takes the sector.
+static bool lanczos_cluster_choice(int n, int m, int& nb, int& h_smem, size_t& smem) {
+    struct Choice { int n, m, nb, h_smem; size_t smem; bool ok; };
+    static Choice cache[32];
+    static int n_cache = 0;
+    for (int i = 0; i < n_cache; ++i)
+        if (cache[i].n == n && cache[i].m == m) {
+            nb = cache[i].nb;
+            h_smem = cache[i].h_smem;
+            smem = cache[i].smem;
+            return cache[i].ok;
+        }
+    int dev = 0, smem_optin = 0;
+    bool ok = false;
+    nb = 0;
+    h_smem = 0;
+    smem = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
+        static int nonportable = -1;
+        if (nonportable < 0)
+            nonportable = cudaFuncSetAttribute(lanczos_cluster_kernel,
+                                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess ? 1 : 0;
+        static size_t smem_set = 48 * 1024;
+        for (int want = nonportable ? 16 : 8; !ok && want >= 8; want -= 8) {
+            nb = want < n ? want : n;
+            h_smem = 1;
+            smem = lanczos_cluster_smem(n, m, nb, 1, smem_optin);
+            if (!smem) {
+                h_smem = 0;
+                smem = lanczos_cluster_smem(n, m, nb, 0, smem_optin);
+            }
+            if (!smem) continue;
+            if (smem > smem_set) {
+                if (cudaFuncSetAttribute(lanczos_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem) != cudaSuccess)
+                    continue;
+                smem_set = smem;
+            }
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)nb;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3((unsigned)nb);
+            cfg.blockDim = dim3(LK_THREADS);
+            cfg.dynamicSmemBytes = smem;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            ok = cudaOccupancyMaxActiveClusters(&clusters, lanczos_cluster_kernel, &cfg) == cudaSuccess && clusters > 0;
+        }
+        cudaGetLastError();
+    }
+    if (n_cache < 32) cache[n_cache++] = Choice{n, m, nb, h_smem, smem, ok};
+    return ok;
+}
+
+extern "C" int xrh_lanczos_cluster_fits(int n, int m) {
+    if (n <= 0 || m <= 0) return 0;
+    int nb, h_smem;
+    size_t smem;
+    return lanczos_cluster_choice(n, m, nb, h_smem, smem) ? 1 : 0;
+}
+
+extern "C" int xrh_lanczos_cluster(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
+                                   double* alpha_dev, double* beta_dev, void* stream) {
+    if (n <= 0 || m <= 0 || ld < n) return XRH_ERR_ARG;
+    if (!H_dev || !v0_dev || !V_dev || !alpha_dev || !beta_dev) return XRH_ERR_ARG;
+    int nb = 0, h_smem = 0;
+    size_t smem = 0;
+    if (!lanczos_cluster_choice(n, m, nb, h_smem, smem)) return XRH_ERR_CAPACITY;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)nb;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)nb);
+    cfg.blockDim = dim3(LK_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.stream = (cudaStream_t)stream;
+    const int rows_max = (n + nb - 1) / nb;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, lanczos_cluster_kernel, n, m, H_dev, ld, v0_dev, V_dev, alpha_dev,
+                                             beta_dev, rows_max, h_smem);
     if (e != cudaSuccess) {
         xrh_set_last_cuda_error((int)e);
         return XRH_ERR_CUDA;

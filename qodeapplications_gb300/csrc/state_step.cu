@@ -18,9 +18,9 @@
 namespace {
 
 constexpr int SS_THREADS = 256;
-constexpr int SS_KSLICE = 256;     // K columns per CTA (matches the host's CTA count)
+constexpr int SS_KSLICE = 64;      // K columns per CTA of the state update (xrh_state_ctas)
+constexpr int ABT_KSLICE = 256;    // K columns per CTA of the A B^T products (xrh_abt_ctas)
 constexpr int GR_KCHUNK = 32;      // columns staged per step in the Gram kernel
-constexpr int TS_KCHUNK = 8;       // columns staged per step in the tangent / left kernels
 constexpr int NS_MAX = 32;
 
 __device__ __forceinline__ int find_task(const xrh_state_task* __restrict__ t, int n_tasks, int64_t cta) {
@@ -33,14 +33,38 @@ __device__ __forceinline__ int find_task(const xrh_state_task* __restrict__ t, i
 }
 
 // One CTA: C (m x n) += alpha * A[:, k_begin:k_end] B[:, k_begin:k_end]^T, m, n <= 64.
+// A is m x K: A[i][k] = A[i*lda + k], or with at A[k*lda + i] (then plus A_add[k*lda + i] when
+// A_add is given); B likewise with bt.  Operands are staged GR_KCHUNK columns at a time with
+// loads that run along the contiguous dimension.
 // ACC is the type of the per-chunk sums; with FP32 inputs the chunk sums (GR_KCHUNK products)
 // are folded into FP32 (hi, lo) pairs by TwoSum, keeping the FP64 pipe out of the loop.
-// With AT, A is given transposed (K x m, row stride m) as AT_main + AT_add (AT_add may be null),
-// staged with loads that run along the contiguous chunk.
-template <typename T, typename ACC, bool AT>
-__device__ __forceinline__ void abt_slice(const T* __restrict__ A, int64_t lda, const float* __restrict__ A_add,
-                                          int m, const T* __restrict__ B, int64_t ldb, int n, int64_t k_begin,
-                                          int64_t k_end, double alpha, double* __restrict__ C,
+template <typename T>
+__device__ __forceinline__ void abt_stage(const T* __restrict__ X, int64_t ld, bool xt, const float* __restrict__ X_add,
+                                          int rows, int64_t k0, int64_t k_end, T (*sx)[GR_KCHUNK + 1]) {
+    if (!xt) {
+        for (int e = threadIdx.x; e < rows * GR_KCHUNK; e += SS_THREADS) {
+            const int i = e / GR_KCHUNK, kk = e - i * GR_KCHUNK;
+            const int64_t k = k0 + kk;
+            sx[i][kk] = k < k_end ? X[(int64_t)i * ld + k] : T(0);
+        }
+    } else {
+        for (int e = threadIdx.x; e < rows * GR_KCHUNK; e += SS_THREADS) {
+            const int kk = e / rows, i = e - kk * rows;
+            const int64_t k = k0 + kk;
+            T v = T(0);
+            if (k < k_end) {
+                v = X[k * ld + i];
+                if (X_add) v += (T)X_add[k * ld + i];
+            }
+            sx[i][kk] = v;
+        }
+    }
+}
+
+template <typename T, typename ACC>
+__device__ __forceinline__ void abt_slice(const T* __restrict__ A, int64_t lda, bool at, const float* __restrict__ A_add,
+                                          int m, const T* __restrict__ B, int64_t ldb, bool bt, int n,
+                                          int64_t k_begin, int64_t k_end, double alpha, double* __restrict__ C,
                                           T (*sa)[GR_KCHUNK + 1], T (*sb)[GR_KCHUNK + 1]) {
     const int mn = m * n;
     constexpr bool F32 = sizeof(ACC) == 4;
@@ -54,25 +78,8 @@ __device__ __forceinline__ void abt_slice(const T* __restrict__ A, int64_t lda, 
     }
     for (int64_t k0 = k_begin; k0 < k_end; k0 += GR_KCHUNK) {
         __syncthreads();
-        for (int e = threadIdx.x; e < 64 * GR_KCHUNK; e += SS_THREADS) {
-            const int i = e / GR_KCHUNK, kk = e - i * GR_KCHUNK;
-            const int64_t k = k0 + kk;
-            const bool kin = k < k_end;
-            if (!AT && i < m) sa[i][kk] = kin ? A[(int64_t)i * lda + k] : T(0);
-            if (i < n) sb[i][kk] = kin ? B[(int64_t)i * ldb + k] : T(0);
-        }
-        if (AT) {
-            for (int e = threadIdx.x; e < m * GR_KCHUNK; e += SS_THREADS) {
-                const int kk = e / m, i = e - kk * m;
-                const int64_t k = k0 + kk;
-                T v = T(0);
-                if (k < k_end) {
-                    v = A[k * m + i];
-                    if (A_add) v += (T)A_add[k * m + i];
-                }
-                sa[i][kk] = v;
-            }
-        }
+        abt_stage<T>(A, lda, at, A_add, m, k0, k_end, sa);
+        abt_stage<T>(B, ldb, bt, nullptr, n, k0, k_end, sb);
         __syncthreads();
 #pragma unroll
         for (int u = 0; u < 16; ++u) {
@@ -111,9 +118,9 @@ __global__ void __launch_bounds__(SS_THREADS) gram_kernel(const xrh_state_task* 
     const int64_t k_begin = (blockIdx.x - T.cta_begin) * (int64_t)SS_KSLICE;
     const int64_t k_end = k_begin + SS_KSLICE < K ? k_begin + SS_KSLICE : K;
     if (which == 0)
-        abt_slice<double, double, true>(T.gT, T.n, T.gT32, T.n, T.z, K, T.n, k_begin, k_end, 1.0, T.G, sa, sb);
+        abt_slice<double, double>(T.gT, T.n, true, T.gT32, T.n, T.z, K, false, T.n, k_begin, k_end, 1.0, T.G, sa, sb);
     else
-        abt_slice<double, double, false>(T.zn, K, nullptr, T.n, T.zn, K, T.n, k_begin, k_end, 1.0, T.S, sa, sb);
+        abt_slice<double, double>(T.zn, K, false, nullptr, T.n, T.zn, K, false, T.n, k_begin, k_end, 1.0, T.S, sa, sb);
 }
 
 template <typename T, typename ACC>
@@ -121,9 +128,9 @@ __global__ void __launch_bounds__(SS_THREADS) abt_kernel(int m, int n, int64_t K
                                                          int64_t lda, const T* __restrict__ B, int64_t ldb,
                                                          double alpha, double* __restrict__ C) {
     __shared__ T sa[64][GR_KCHUNK + 1], sb[64][GR_KCHUNK + 1];
-    const int64_t k_begin = (int64_t)blockIdx.x * SS_KSLICE;
-    const int64_t k_end = k_begin + SS_KSLICE < K ? k_begin + SS_KSLICE : K;
-    abt_slice<T, ACC, false>(A, lda, nullptr, m, B, ldb, n, k_begin, k_end, alpha, C, sa, sb);
+    const int64_t k_begin = (int64_t)blockIdx.x * ABT_KSLICE;
+    const int64_t k_end = k_begin + ABT_KSLICE < K ? k_begin + ABT_KSLICE : K;
+    abt_slice<T, ACC>(A, lda, false, nullptr, m, B, ldb, false, n, k_begin, k_end, alpha, C, sa, sb);
 }
 
 // Many small-output products in one launch: task t owns CTAs [cta_begin, cta_begin +
@@ -139,24 +146,22 @@ __global__ void __launch_bounds__(SS_THREADS) abt_grouped_kernel(const xrh_abt_t
     }
     const xrh_abt_task& Tk = tasks[lo];
     if (Tk.m <= 0 || Tk.m > 64 || Tk.n <= 0 || Tk.n > 64) return;   // checked by the host
-    const int64_t k_begin = (cta - Tk.cta_begin) * (int64_t)SS_KSLICE;
-    const int64_t k_end = k_begin + SS_KSLICE < Tk.K ? k_begin + SS_KSLICE : Tk.K;
-    abt_slice<T, ACC, false>(reinterpret_cast<const T*>(Tk.A), Tk.lda, nullptr, (int)Tk.m,
-                             reinterpret_cast<const T*>(Tk.B), Tk.ldb, (int)Tk.n, k_begin, k_end, Tk.alpha, Tk.C, sa,
-                             sb);
+    const int64_t k_begin = (cta - Tk.cta_begin) * (int64_t)ABT_KSLICE;
+    const int64_t k_end = k_begin + ABT_KSLICE < Tk.K ? k_begin + ABT_KSLICE : Tk.K;
+    abt_slice<T, ACC>(reinterpret_cast<const T*>(Tk.A), Tk.lda, (Tk.flags & 1) != 0, nullptr, (int)Tk.m,
+                      reinterpret_cast<const T*>(Tk.B), Tk.ldb, (Tk.flags & 2) != 0, (int)Tk.n, k_begin, k_end,
+                      Tk.alpha, Tk.C, sa, sb);
 }
 
-// out[i][k] = sum_j W[i][j] X[j][k] over this CTA's K slice, X (and g) staged TS_KCHUNK columns
-// at a time; thread (row group, column) = (t / TS_KCHUNK, t % TS_KCHUNK), rows i = row group +
-// (SS_THREADS / TS_KCHUNK) r.
+// out[i][k] = sum_j W[i][j] X[j][k] over this CTA's K slice: thread per column k (the column
+// of X read through L1 n times, W by broadcast from shared memory), n independent FP64 chains.
 // mode 0 (tangent): W = sym(G), X = z; t = g - W z; zn = z - eps t; sq += t^2.
 // mode 1 (left):    W = M, X = zn; z = W zn.
 template <int MODE>
 __global__ void __launch_bounds__(SS_THREADS) rowmix_kernel(const xrh_state_task* __restrict__ tasks, int n_tasks,
                                                             double eps, double* __restrict__ sq) {
     __shared__ double w[64 * 64];
-    __shared__ double xs[64][TS_KCHUNK];
-    __shared__ double gs[TS_KCHUNK][65];
+    __shared__ double red[SS_THREADS / 32];
     const xrh_state_task& T = tasks[find_task(tasks, n_tasks, blockIdx.x)];
     const int n = T.n;
     if (n <= 0 || n > 64) return;
@@ -165,51 +170,46 @@ __global__ void __launch_bounds__(SS_THREADS) rowmix_kernel(const xrh_state_task
         const int i = e / n, j = e - i * n;
         w[e] = MODE == 0 ? 0.5 * (T.G[i * n + j] + T.G[j * n + i]) : T.M[e];
     }
+    __syncthreads();
     const double* X = MODE == 0 ? T.z : T.zn;
     const int64_t k_begin = (blockIdx.x - T.cta_begin) * (int64_t)SS_KSLICE;
     const int64_t k_end = k_begin + SS_KSLICE < K ? k_begin + SS_KSLICE : K;
-    const int kk = threadIdx.x & (TS_KCHUNK - 1);
-    const int r0 = threadIdx.x / TS_KCHUNK;
     double part = 0.0;
-    for (int64_t k0 = k_begin; k0 < k_end; k0 += TS_KCHUNK) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * TS_KCHUNK; e += SS_THREADS) {
-            const int j = e / TS_KCHUNK, c = e - j * TS_KCHUNK;
-            const int64_t k = k0 + c;
-            xs[j][c] = k < k_end ? X[(int64_t)j * K + k] : 0.0;
-        }
-        if (MODE == 0) {
-            for (int e = threadIdx.x; e < n * TS_KCHUNK; e += SS_THREADS) {
-                const int c = e / n, i = e - c * n;
-                const int64_t k = k0 + c;
-                double v = 0.0;
-                if (k < k_end) {
-                    v = T.gT[k * n + i];
-                    if (T.gT32) v += (double)T.gT32[k * n + i];
-                }
-                gs[c][i] = v;
+    // SS_THREADS / SS_KSLICE threads per column split the rows
+    constexpr int RG = SS_THREADS / SS_KSLICE;
+    const int64_t k = k_begin + (threadIdx.x % SS_KSLICE);
+    const int r0 = threadIdx.x / SS_KSLICE;
+    if (k < k_end) {
+        for (int i = r0; i < n; i += RG) {
+            double s0 = 0.0, s1 = 0.0;
+            int j = 0;
+            for (; j + 1 < n; j += 2) {
+                s0 = fma(w[i * n + j], X[(int64_t)j * K + k], s0);
+                s1 = fma(w[i * n + j + 1], X[(int64_t)(j + 1) * K + k], s1);
             }
-        }
-        __syncthreads();
-        const int64_t k = k0 + kk;
-        if (k < k_end) {
-            for (int i = r0; i < n; i += SS_THREADS / TS_KCHUNK) {
-                double s = 0.0;
-                for (int j = 0; j < n; ++j) s = fma(w[i * n + j], xs[j][kk], s);
-                if (MODE == 0) {
-                    const double t = gs[kk][i] - s;
-                    part = fma(t, t, part);
-                    T.zn[(int64_t)i * K + k] = xs[i][kk] - eps * t;
-                } else {
-                    T.z[(int64_t)i * K + k] = s;
-                }
+            if (j < n) s0 = fma(w[i * n + j], X[(int64_t)j * K + k], s0);
+            const double s = s0 + s1;
+            if (MODE == 0) {
+                double g = T.gT[k * n + i];
+                if (T.gT32) g += (double)T.gT32[k * n + i];
+                const double t = g - s;
+                part = fma(t, t, part);
+                T.zn[(int64_t)i * K + k] = X[(int64_t)i * K + k] - eps * t;
+            } else {
+                T.z[(int64_t)i * K + k] = s;
             }
         }
     }
     if (MODE == 0) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        if ((threadIdx.x & 31) == 0 && part != 0.0) atomicAdd(sq, part);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int q = 0; q < SS_THREADS / 32; ++q) t += red[q];
+            if (t != 0.0) atomicAdd(sq, t);
+        }
     }
 }
 
@@ -266,6 +266,7 @@ int check(const xrh_state_task* tasks, int n_tasks, int64_t total_ctas) {
 }  // namespace
 
 extern "C" int xrh_state_ctas(int64_t K) { return (int)((K + SS_KSLICE - 1) / SS_KSLICE); }
+extern "C" int xrh_abt_ctas(int64_t K) { return (int)((K + ABT_KSLICE - 1) / ABT_KSLICE); }
 
 extern "C" int xrh_gram_grouped(const xrh_state_task* tasks_dev, int n_tasks, int64_t total_ctas, int which,
                                 void* stream) {
@@ -313,7 +314,7 @@ extern "C" int xrh_abt_small(int precision, int m, int n, int64_t K, const void*
     if (m < 0 || n < 0 || K < 0 || m > 64 || n > 64) return XRH_ERR_ARG;
     if (m == 0 || n == 0 || K == 0) return XRH_OK;
     if (!A_dev || !B_dev || !C_dev || lda < K || ldb < K) return XRH_ERR_ARG;
-    const int64_t ctas = (K + SS_KSLICE - 1) / SS_KSLICE;
+    const int64_t ctas = (K + ABT_KSLICE - 1) / ABT_KSLICE;
     if (ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     cudaStream_t s = (cudaStream_t)stream;
     if (precision == XRH_FP64)

@@ -7,9 +7,11 @@ classical Gram-Schmidt against all previous vectors, normalisation) runs entirel
 device with fixed shapes, so it can be captured in a CUDA graph; only the small tridiagonal
 eigenproblem (m x m) is solved on the host.
 
-The default loop ("coop") is one cooperative launch whose CTAs split the rows of H and meet at
-four grid barriers per step (the FP64 rate of one SM would otherwise bound it); "small" is
-the one-CTA loop and "steps" six launches per step, kept as cross-checks.
+The default loop is "cluster" (one thread-block cluster of 8-16 CTAs, hardware cluster
+barriers, distributed shared memory; for sectors whose rows fit the cluster's shared memory)
+or else "coop" (one cooperative launch whose CTAs split the rows of H and meet at three grid
+barriers per step): the FP64 rate of one SM would otherwise bound the loop.  "small" is the
+one-CTA loop and "steps" six launches per step, kept as cross-checks.
 """
 import numpy as np
 import torch
@@ -17,11 +19,11 @@ import torch
 from ._lib import call, ptr, stream_ptr
 
 SMALL_SECTOR = 2048
-MODES = ("coop", "small", "steps")
+MODES = ("auto", "cluster", "coop", "small", "steps")
 
 
 class Lanczos:
-    def __init__(self, n, m=96, device="cuda", seed=7, mode="coop"):
+    def __init__(self, n, m=96, device="cuda", seed=7, mode="auto"):
         self.n = int(n)
         self.m = int(min(m, n))
         dev = torch.device(device)
@@ -42,6 +44,12 @@ class Lanczos:
             raise ValueError(f"mode must be one of {MODES}")
         if mode == "small" and self.n > SMALL_SECTOR:
             mode = "steps"
+        if mode in ("auto", "cluster"):
+            from ._lib import lib
+            fits = bool(lib().xrh_lanczos_cluster_fits(self.n, self.m))
+            if mode == "cluster" and not fits:
+                raise ValueError("sector too large for the cluster Lanczos loop")
+            mode = "cluster" if fits else "coop"
         self.mode = mode
         self.small = mode != "steps"      # alpha/beta written straight into self.ab
         if mode == "coop":
@@ -55,6 +63,10 @@ class Lanczos:
         s = stream_ptr()
         n, m = self.n, self.m
         ld = n if ld is None else ld
+        if self.mode == "cluster":
+            call("xrh_lanczos_cluster", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab), ptr(self.ab[m:]),
+                 s)
+            return
         if self.mode == "coop":
             call("xrh_lanczos_coop", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab), ptr(self.ab[m:]),
                  ptr(self.work), self.work.numel(), ptr(self.status), s)

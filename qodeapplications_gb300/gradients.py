@@ -301,6 +301,7 @@ class XRDimerAdjoint:
                     continue
                 gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
+        self.dens_adj_all = list(self.dens_adj)
         # FP32 path: every block of a fragment in one grouped launch, on the tensor cores when
         # every block has at most 64 states per side (else the CUDA-core kernel)
         self.dens_adj_groups = []
@@ -493,15 +494,19 @@ class XRDimerAdjoint:
         return out
 
     def integral_gradients(self):
-        """dE/dT, dE/dU, dE/dV as supersystem spin-orbital tensors (device)."""
-        plan = self.plan
-        Ns = plan.N
-        off = [0, Ns[0], Ns[0] + Ns[1]]
-        tot = off[-1]
-        dev = plan.device
+        """dE/dT, dE/dU, dE/dV as supersystem spin-orbital tensors (device, new tensors)."""
+        tot = sum(self.plan.N)
+        dev = self.plan.device
         dT = torch.zeros((tot, tot), dtype=torch.float64, device=dev)
         dU = torch.zeros((2, tot, tot), dtype=torch.float64, device=dev)
         dV = torch.zeros((tot,) * 4, dtype=torch.float64, device=dev)
+        return self._integral_gradients_into(dT, dU, dV)
+
+    def _integral_gradients_into(self, dT, dU, dV):
+        """Add dE/dT, dE/dU, dE/dV into zeroed (tot, tot), (2, tot, tot), (tot,)*4 tensors."""
+        plan = self.plan
+        Ns = plan.N
+        off = [0, Ns[0], Ns[0] + Ns[1]]
         sl = [slice(off[m], off[m + 1]) for m in (0, 1)]
         G = self.G
         gw = G[("gW", "v0101")].view(Ns[1], Ns[1], Ns[0], Ns[0])
@@ -524,35 +529,74 @@ class XRDimerAdjoint:
             dV[sl[m], sl[m], sl[m], sl[m]] += Gf
         return dT, dU, dV
 
+    def _orbital_buffers(self, T, U, V):
+        """Persistent buffers and the one-body task table of orbital_gradient for these
+        integral tensors (None when t > 64 or the tensors are not contiguous FP64)."""
+        t = V.shape[0]
+        ok = (t <= 64 and all(x.dtype == torch.float64 and x.is_contiguous() for x in (T, U, V)) and
+              tuple(T.shape) == (t, t) and tuple(U.shape[1:]) == (t, t))
+        if not ok:
+            return None
+        key = (T.data_ptr(), U.data_ptr(), V.data_ptr(), t, U.shape[0])
+        b = getattr(self, "_orb", None)
+        if b is not None and b["key"] == key:
+            return b
+        dev = V.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        b = dict(key=key, keep=(T, U, V))
+        b["dT"] = torch.zeros((t, t), **f64)
+        b["dU"] = torch.zeros((U.shape[0], t, t), **f64)
+        b["dV"] = torch.zeros((t,) * 4, **f64)
+        b["Gso"] = torch.zeros((t, t), **f64)
+        if self.prec32:
+            b["A"] = torch.empty((t,) * 4, dtype=torch.float32, device=dev)
+            b["B"] = torch.empty((t,) * 4, dtype=torch.float32, device=dev)
+        else:
+            b["A"] = V
+            b["B"] = torch.empty((t,) * 4, **f64)
+        pairs = [(T, b["dT"], b["Gso"])] + [(U[k], b["dU"][k], b["Gso"]) for k in range(U.shape[0])]
+        b["one_body"] = _one_body_table(pairs, dev)
+        self._orb = b
+        return b
+
     def orbital_gradient(self, T, U, V, spatial_index):
         """dE/dkappa (antisymmetric, spatial orbitals) for X' = R^T X R with R = exp(kappa)
         applied to every integral at kappa = 0.  T (tot x tot), U (n_frag x tot x tot),
         V (tot^4) are the current spin-orbital integrals on the device; spatial_index[i]
         is the spatial orbital of spin orbital i."""
-        dT, dU, dV = self.integral_gradients()
-        Gso = T @ dT.t() + T.t() @ dT
-        for k in range(U.shape[0]):
-            Gso += U[k] @ dU[k].t() + U[k].t() @ dU[k]
         t = V.shape[0]
+        b = self._orbital_buffers(T, U, V)
+        if b is None:
+            dT, dU, dV = self.integral_gradients()
+            Gso = T @ dT.t() + T.t() @ dT
+            for k in range(U.shape[0]):
+                Gso += U[k] @ dU[k].t() + U[k].t() @ dU[k]
+        else:
+            dT, dU, dV, Gso = b["dT"], b["dU"], b["dV"], b["Gso"]
+            dT.zero_()
+            dU.zero_()
+            dV.zero_()
+            self._integral_gradients_into(dT, dU, dV)
+            Gso.zero_()
+            # the one-body terms T dT^T + T^T dT + sum_k U_k dU_k^T + U_k^T dU_k in one launch
+            tab, n_tab, ctas = b["one_body"]
+            call("xrh_abt_grouped", _lib.FP64, ptr(tab), n_tab, ctas, stream_ptr())
         # E sees V only through its symmetric part (V_pqrs = -V_qprs = -V_pqsr = V_rspq for real
         # orbitals), so dE/dV may be replaced by its projection on that symmetry; then the four
         # index positions of V' = R^T..R contribute equally: dE/dR = 4 V_(1) Gbar_(1)^T
         Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
-        # 4 V_(1) Gbar_(1)^T with Gbar = (Ga + Ga^(rs,pq)) / 8: a t x t result over t^3 terms,
-        # split over CTAs by xrh_abt_small (FP32 products on the split-precision paths)
-        if t <= 64:
-            Gso = Gso.contiguous()
+        if b is not None:
+            # 4 V_(1) Gbar_(1)^T with Gbar = (Ga + Ga^(rs,pq)) / 8: a t x t result over t^3 terms,
+            # split over CTAs by xrh_abt_small (FP32 products on the split-precision paths)
             K3 = t ** 3
             if self.prec32:
-                B = torch.empty(V.shape, dtype=torch.float32, device=V.device)
-                torch.add(Ga, Ga.permute(2, 3, 0, 1), out=B)
-                A = V.to(torch.float32).contiguous()
+                torch.add(Ga, Ga.permute(2, 3, 0, 1), out=b["B"])
+                b["A"].copy_(V)
                 prec = _lib.FP32
             else:
-                B = Ga + Ga.permute(2, 3, 0, 1)
-                A = V.contiguous()
+                torch.add(Ga, Ga.permute(2, 3, 0, 1), out=b["B"])
                 prec = _lib.FP64
-            call("xrh_abt_small", prec, t, t, K3, ptr(A), K3, ptr(B), K3, 0.5, ptr(Gso), stream_ptr())
+            call("xrh_abt_small", prec, t, t, K3, ptr(b["A"]), K3, ptr(b["B"]), K3, 0.5, ptr(Gso), stream_ptr())
         else:
             Gbar = 0.125 * (Ga + Ga.permute(2, 3, 0, 1))
             Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
@@ -566,6 +610,22 @@ class XRDimerAdjoint:
         # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs
         Gsp = Pm.t() @ (Gso * same) @ Pm
         return Gsp - Gsp.t()
+
+
+def _one_body_table(pairs, device):
+    """xrh_abt_grouped (FP64) tasks C += X dX^T and C += X^T dX for each (X, dX, C), all t x t
+    row-major."""
+    tab = np.zeros(2 * len(pairs), dtype=_lib.ABT_TASK_DTYPE)
+    cta = 0
+    for i, (X, dX, C) in enumerate(pairs):
+        t = X.shape[0]
+        for h, flags in enumerate((0, 3)):
+            e = tab[2 * i + h]
+            e["A"], e["B"], e["C"] = X.data_ptr(), dX.data_ptr(), C.data_ptr()
+            e["m"], e["n"], e["K"], e["lda"], e["ldb"], e["alpha"] = t, t, t, t, t, 1.0
+            e["cta_begin"], e["flags"] = cta, flags
+            cta += int(_lib.lib().xrh_abt_ctas(t))
+    return torch.from_numpy(tab.view(np.uint8).copy()).to(device), len(tab), cta
 
 
 def _same_spin(t, spatial_index, device):

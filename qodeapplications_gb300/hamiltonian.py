@@ -259,7 +259,7 @@ def _abt_table(entries, device):
         t = tab[i]
         t["A"], t["B"], t["C"] = A.data_ptr(), B.data_ptr(), C.data_ptr()
         t["m"], t["n"], t["K"], t["lda"], t["ldb"], t["alpha"], t["cta_begin"] = m, n, K, lda, ldb, alpha, cta
-        cta += int(_lib.lib().xrh_state_ctas(K))
+        cta += int(_lib.lib().xrh_abt_ctas(K))
     return torch.from_numpy(tab.view(np.uint8).copy()).to(device), len(entries), cta
 
 

@@ -21,9 +21,12 @@ def _matrix(n, seed):
 
 
 @pytest.mark.parametrize("n,m", [(300, 24), (2, 2), (1, 1), (1000, 60), (5003, 40)])
-@pytest.mark.parametrize("mode", ["coop", "small", "steps"])
+@pytest.mark.parametrize("mode", ["cluster", "coop", "small", "steps"])
 def test_lanczos_modes(n, m, mode):
+    from qodeapplications_gb300 import _lib
     from qodeapplications_gb300.eigen import Lanczos
+    if mode == "cluster" and not _lib.lib().xrh_lanczos_cluster_fits(n, m):
+        pytest.skip("sector larger than the cluster loop takes")
     A, w0 = _matrix(n, n + m)
     Ad = A.cuda()
     lz = Lanczos(n, m=m, mode=mode)
@@ -39,28 +42,32 @@ def test_lanczos_modes(n, m, mode):
         assert r.norm().item() < 1e-7
 
 
-@pytest.mark.parametrize("n,m", [(300, 24), (4099, 30)])
+@pytest.mark.parametrize("n,m", [(300, 24), (4099, 30), (1000, 48)])
 def test_lanczos_coop_matches_steps(n, m):
+    from qodeapplications_gb300 import _lib
     from qodeapplications_gb300.eigen import Lanczos
     A, _ = _matrix(n, 5)
     Ad = A.cuda()
     out = {}
-    for mode in ("coop", "steps"):
+    modes = ["coop", "steps"] + (["cluster"] if _lib.lib().xrh_lanczos_cluster_fits(n, m) else [])
+    for mode in modes:
         lz = Lanczos(n, m=m, mode=mode)
         lz.krylov(Ad)
         lz.stage_to_host()
         torch.cuda.synchronize()
         out[mode] = lz._host[:2 * m].numpy().copy()
-    a, b = out["coop"], out["steps"]
-    assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+    b = out["steps"]
+    for mode in modes[:1] + modes[2:]:
+        assert np.abs(out[mode] - b).max() <= 1e-11 * np.abs(b).max(), mode
 
 
-def test_lanczos_coop_in_graph():
-    """The cooperative launch is captured and replayed as part of a CUDA graph."""
+@pytest.mark.parametrize("mode", ["coop", "cluster"])
+def test_lanczos_in_graph(mode):
+    """The cooperative and the cluster launches are captured and replayed in a CUDA graph."""
     from qodeapplications_gb300.eigen import Lanczos
     A, w0 = _matrix(300, 9)
     Ad = A.cuda()
-    lz = Lanczos(300, m=24, mode="coop")
+    lz = Lanczos(300, m=24, mode=mode)
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
