@@ -192,7 +192,7 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
 # DRAM bytes (read + write) per launch of the dominant kernel (the FP32 density adjoint of
 # one fragment), from one ncu capture of the bench command (profiles/); None where no capture
 # exists for the workload
-DENSITY_ADJ_TRAFFIC_BYTES = {1: None}
+DENSITY_ADJ_TRAFFIC_BYTES = {1: 26_176_896}
 
 
 def density_adjoint_work(adj, m):

@@ -84,9 +84,9 @@ __global__ void __launch_bounds__(kAdjThreads) density_adjoint_kernel(
 // into FP32 gradient rows with 16-byte vector atomics.
 __device__ __forceinline__ void atomic_add4(float* dst, const float (&v)[4], int valid) {
     if (valid == 4 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
-        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(v[0], v[1], v[2], v[3]));
+        xrh_red_add_v4(dst, v[0], v[1], v[2], v[3]);
     } else {
-        for (int k = 0; k < valid; ++k) atomicAdd(dst + k, v[k]);
+        for (int k = 0; k < valid; ++k) xrh_red_add(dst + k, v[k]);
     }
 }
 
@@ -337,7 +337,7 @@ __device__ __forceinline__ void atomic_add_row(float* dst, const float (&v)[MP],
     for (int k = 0; k < MP; k += 4) {
         if (k >= n) break;
         if (a16 && k + 3 < n) {
-            atomicAdd(reinterpret_cast<float4*>(dst + k), make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]));
+            xrh_red_add_v4(dst + k, v[k], v[k + 1], v[k + 2], v[k + 3]);
             continue;
         }
 #pragma unroll
@@ -345,10 +345,10 @@ __device__ __forceinline__ void atomic_add_row(float* dst, const float (&v)[MP],
             const int kk = k + h;
             if (kk >= n) break;
             if (kk + 1 < n && a8) {
-                atomicAdd(reinterpret_cast<float2*>(dst + kk), make_float2(v[kk], v[kk + 1]));
+                xrh_red_add_v2(dst + kk, v[kk], v[kk + 1]);
             } else {
-                atomicAdd(dst + kk, v[kk]);
-                if (kk + 1 < n) atomicAdd(dst + kk + 1, v[kk + 1]);
+                xrh_red_add(dst + kk, v[kk]);
+                if (kk + 1 < n) xrh_red_add(dst + kk + 1, v[kk + 1]);
             }
         }
     }

@@ -48,9 +48,9 @@ __device__ __forceinline__ void atomic_row4(float* dst, const float* v, float s,
     for (int j = 0; j < n; j += 4) {
         const int valid = n - j < 4 ? n - j : 4;
         if (valid == 4 && (reinterpret_cast<uintptr_t>(dst + j) & 15) == 0) {
-            atomicAdd(reinterpret_cast<float4*>(dst + j), make_float4(s * v[j], s * v[j + 1], s * v[j + 2], s * v[j + 3]));
+            xrh_red_add_v4(dst + j, s * v[j], s * v[j + 1], s * v[j + 2], s * v[j + 3]);
         } else {
-            for (int t = 0; t < valid; ++t) atomicAdd(dst + j + t, s * v[j + t]);
+            for (int t = 0; t < valid; ++t) xrh_red_add(dst + j + t, s * v[j + t]);
         }
     }
 }

@@ -108,6 +108,20 @@ __device__ __forceinline__ float xrh_f64_to_f32(double x) {
     return __uint_as_float(((uint32_t)(b >> 63) << 31) | (fe << 23) | m);
 }
 
+// Fire-and-forget vector additions to global memory (red: no value comes back, so nothing
+// waits on the L2 round trip; the vector atomicAdd overloads return the old value).
+// Addresses 16- (v4) or 8-byte (v2) aligned.
+__device__ __forceinline__ void xrh_red_add_v4(float* addr, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+__device__ __forceinline__ void xrh_red_add_v2(float* addr, float a, float b) {
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(a), "f"(b) : "memory");
+}
+__device__ __forceinline__ void xrh_red_add(float* addr, float a) {
+    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(a) : "memory");
+}
+
 // Same through L1 (gathers with reuse across warps of an SM).
 __device__ __forceinline__ void cp_async16_ca(void* smem_dst, const void* gmem_src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem_dst)),
