@@ -174,6 +174,17 @@ int xrh_transpose_grouped(const xrh_transpose_task* tasks_dev, int n_tasks, int6
  * reverse order).  The adjoint uses the same map with accumulate = 1. */
 int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev,
                        int accumulate, void* stream);
+/* Many mirrors in one launch: task t is one xrh_mirror_density call and owns the launch's CTAs
+ * [cta_begin, cta_begin + na * nb * (L == 3 ? N : 1)) (tasks sorted by cta_begin, total_ctas
+ * the sum).  The tasks' dst blocks must not overlap. */
+typedef struct {
+    const double* src;
+    double* dst;
+    int32_t na, nb, N, L;
+    int32_t accumulate, reserved;
+    int64_t cta_begin;
+} xrh_mirror_task;   /* 48 bytes */
+int xrh_mirror_grouped(const xrh_mirror_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
 
 /* Monomer two-electron term without the N^4 density (replaces building rho^ccaa and
  * contracting it, general-XRCC/build_density_tensors.py:122-133 + H_contractions.c:61-78):
@@ -328,6 +339,29 @@ int xrh_tangent_step(const xrh_state_task* tasks_dev, int n_tasks, int64_t total
                      double* sq_dev, void* stream);
 int xrh_inv_sqrt_small(const xrh_state_task* tasks_dev, int n_tasks, int iters, void* stream);
 int xrh_left_multiply(const xrh_state_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
+
+/* Integral derivatives for the orbital gradient from the reverse pass's pieces (replaces the
+ * integral-derivative assembly feeding StateSpaceOptimizer/orb_grads.py): pointers to the
+ * contiguous FP64 pieces of a dimer (fragment 0 = spin orbitals [0, N0), fragment 1 = [N0,
+ * N0 + N1), N0 + N1 <= 64; gw (N1, N1, N0, N0); per fragment m with o the other: h1 (No, Nm),
+ * cca and caa (No, Nm, Nm, Nm), cc (No, No, Nm, Nm), mono1 (Nm, Nm), gamma64 (Nm^4) plus an
+ * optional FP32 part gamma32).  xrh_orbital_terms writes dT (t x t, t = N0 + N1; also the
+ * derivative of every fragment potential) and B[p,q,r,s] = Ga[pqrs] + Ga[rspq] with Ga the
+ * (pq)- and (rs)-antisymmetrised dE/dV (t^4; FP32 with FP32 arithmetic for XRH_FP32, FP64 for
+ * XRH_FP64).  dE/dkappa's two-electron part is then 1/2 V_(1) B_(1)^T (xrh_abt_small).
+ * in_host is a host pointer; two kernel launches. */
+typedef struct {
+    const double* gw;
+    const double* h1[2];
+    const double* cca[2];
+    const double* caa[2];
+    const double* cc[2];
+    const double* mono1[2];
+    const double* gamma64[2];
+    const float* gamma32[2];
+    int32_t N0, N1;
+} xrh_orbital_inputs;   /* 128 bytes */
+int xrh_orbital_terms(const xrh_orbital_inputs* in_host, double* dT_dev, void* B_dev, int precision, void* stream);
 
 /* C (m x n, FP64, row-major, ld n) += alpha * A B^T for m, n <= 64 and long K: A (m x K, ld
  * lda) and B (n x K, ld ldb) are double (XRH_FP64) or float (XRH_FP32: FP32 products summed in

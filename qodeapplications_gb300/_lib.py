@@ -42,6 +42,8 @@ _SIGS = {
     "xrh_abt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
     "xrh_coeff_stage": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_transpose_grouped": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_mirror_grouped": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_orbital_terms": (_i32, [_vp, _vp, _vp, _i32, _vp]),
     "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
     "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),
     "xrh_inv_sqrt_small": (_i32, [_vp, _i32, _i32, _vp]),
@@ -109,7 +111,9 @@ def register(name, restype, argtypes):
 
 class LaunchCounter:
     """Counts library calls that launch a kernel (the gpu_launches figure): every entry point
-    except the host-only ones below launches exactly one kernel of this library."""
+    except the host-only ones below launches one kernel of this library (those in `multi` the
+    number given)."""
+    multi = {"xrh_orbital_terms": 2}
     host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems",
                  "xrh_tc_encode_map", "xrh_state_ctas", "xrh_abt_ctas", "xrh_lanczos_coop_work",
                  "xrh_lanczos_cluster_fits"}
@@ -119,7 +123,7 @@ class LaunchCounter:
 def call(name, *args):
     """Call one ABI function; raise XRHError on a non-zero status."""
     if name not in LaunchCounter.host_only:
-        LaunchCounter.count += 1
+        LaunchCounter.count += LaunchCounter.multi.get(name, 1)
     st = getattr(lib(), name)(*args)
     if st != XRH_OK:
         msg = lib().xrh_status_string(st).decode()
@@ -164,6 +168,15 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+ORBITAL_INPUTS_DTYPE = np.dtype([("gw", np.uint64), ("h1", np.uint64, 2), ("cca", np.uint64, 2),
+                                 ("caa", np.uint64, 2), ("cc", np.uint64, 2), ("mono1", np.uint64, 2),
+                                 ("gamma64", np.uint64, 2), ("gamma32", np.uint64, 2), ("N0", np.int32),
+                                 ("N1", np.int32)])
+assert ORBITAL_INPUTS_DTYPE.itemsize == 128
+MIRROR_TASK_DTYPE = np.dtype([("src", np.uint64), ("dst", np.uint64), ("na", np.int32), ("nb", np.int32),
+                              ("N", np.int32), ("L", np.int32), ("accumulate", np.int32), ("reserved", np.int32),
+                              ("cta_begin", np.int64)])
+assert MIRROR_TASK_DTYPE.itemsize == 48
 TRANSPOSE_TASK_DTYPE = np.dtype([("in", np.uint64), ("out", np.uint64), ("rows", np.int64), ("cols", np.int64),
                                  ("tile_begin", np.int64)])
 assert TRANSPOSE_TASK_DTYPE.itemsize == 40
@@ -218,3 +231,29 @@ class Transposes:
     def run(self, stream=None):
         if self.n:
             call("xrh_transpose_grouped", ptr(self.dev), self.n, self.tiles, stream_ptr(stream))
+
+
+class Mirrors:
+    """A fixed list of xrh_mirror_density calls [(src, dst, na, nb, N, L, accumulate)] run as
+    one xrh_mirror_grouped launch (dst blocks distinct)."""
+
+    def __init__(self, items, device):
+        import torch
+        dsts = [it[1].data_ptr() for it in items]
+        if len(set(dsts)) != len(dsts):
+            raise ValueError("grouped mirrors need distinct destination blocks")
+        tab = np.zeros(len(items), dtype=MIRROR_TASK_DTYPE)
+        cta = 0
+        for i, (src, dst, na, nb, N, L, acc) in enumerate(items):
+            if N > 64 or not 1 <= L <= 3:
+                raise ValueError("mirror needs N <= 64 and 1 <= L <= 3")
+            t = tab[i]
+            t["src"], t["dst"], t["na"], t["nb"], t["N"], t["L"] = src.data_ptr(), dst.data_ptr(), na, nb, N, L
+            t["accumulate"], t["cta_begin"] = int(acc), cta
+            cta += na * nb * (N if L == 3 else 1)
+        self.n, self.ctas, self.keep = len(items), cta, items
+        self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(items) else None
+
+    def run(self, stream=None):
+        if self.n:
+            call("xrh_mirror_grouped", ptr(self.dev), self.n, self.ctas, stream_ptr(stream))

@@ -331,6 +331,49 @@ __global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int 
     }
 }
 
+// Many mirrors in one launch: CTA -> task by binary search on cta_begin; the tasks' dst
+// blocks are distinct (the host checks), so accumulating tasks do not race.
+__device__ __forceinline__ void mirror_plane(int na, int nb, int N, int L, const double* __restrict__ src,
+                                             double* __restrict__ dst, int accumulate, int64_t blk,
+                                             double (*tile)[65]) {
+    int64_t F = 1;
+    for (int l = 0; l < L; ++l) F *= N;
+    const int q = (L == 3) ? (int)(blk % N) : 0;
+    const int64_t ab = (L == 3) ? blk / N : blk;
+    const int a = (int)(ab / nb), b = (int)(ab - (int64_t)(ab / nb) * nb);
+    const double* sp = src + ((int64_t)b * na + a) * F;
+    double* dp = dst + ((int64_t)a * nb + b) * F;
+    if (L == 1) {
+        for (int p = threadIdx.x; p < N; p += blockDim.x) dp[p] = (accumulate ? dp[p] : 0.0) + sp[p];
+        return;
+    }
+    const int NN = N * N;
+    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+        const int p = i / N, r = i - p * N;
+        tile[p][r] = sp[L == 2 ? i : ((int64_t)p * N + q) * N + r];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+        const int r = i / N, p = i - r * N;
+        const int64_t pos = L == 2 ? i : ((int64_t)r * N + q) * N + p;
+        const double v = tile[p][r];
+        dp[pos] = accumulate ? dp[pos] + v : v;
+    }
+}
+
+__global__ void __launch_bounds__(256) mirror_grouped_kernel(const xrh_mirror_task* __restrict__ tasks, int n_tasks) {
+    __shared__ double tile[64][65];
+    const int64_t cta = blockIdx.x;
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const xrh_mirror_task& T = tasks[lo];
+    if (T.N <= 0 || T.N > 64 || T.L < 1 || T.L > 3) return;   // checked by the host
+    mirror_plane(T.na, T.nb, T.N, T.L, T.src, T.dst, T.accumulate, cta - T.cta_begin, tile);
+}
+
 extern "C" int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev, int accumulate,
                                   void* stream) {
     if (na <= 0 || nb <= 0 || N <= 0 || L < 1 || L > 3 || !src_dev || !dst_dev || src_dev == dst_dev)
@@ -796,6 +839,16 @@ extern "C" int xrh_transpose_grouped(const xrh_transpose_task* tasks_dev, int n_
     if (!tasks_dev) return XRH_ERR_ARG;
     if (total_tiles > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     transpose_grouped_kernel<<<(unsigned)total_tiles, dim3(32, 8), 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_mirror_grouped(const xrh_mirror_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream) {
+    if (n_tasks < 0 || total_ctas < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    mirror_grouped_kernel<<<(unsigned)total_ctas, 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -307,6 +307,7 @@ class DensityBuilder:
             for c in space.charges}
         self._stage = None
         self._tr_direct = self._tr_derived = None
+        self._mirrors = None
         # FP32 path: coefficients converted once per build, rows padded to 16 bytes
         if self.f32:
             pad = lambda n: (n + 3) // 4 * 4
@@ -433,10 +434,12 @@ class DensityBuilder:
             self._tr_direct = _lib.Transposes(direct, self.space.device)
             self._tr_derived = _lib.Transposes(derived, self.space.device)
         self._tr_direct.run()
-        for (op, bc, kc), (pop, pbc, pkc) in self.mirror.items():
-            nb, nk = self.n_states_bra[bc], self.n_states[kc]
-            call("xrh_mirror_density", nb, nk, self.space.N, len(op), ptr(self.rho[pop][(pbc, pkc)]),
-                 ptr(self.rho[op][(bc, kc)]), 0, s)
+        if self._mirrors is None:
+            self._mirrors = _lib.Mirrors(
+                [(self.rho[pop][(pbc, pkc)], self.rho[op][(bc, kc)], self.n_states_bra[bc], self.n_states[kc],
+                  self.space.N, len(op), 0) for (op, bc, kc), (pop, pbc, pkc) in self.mirror.items()],
+                self.space.device)
+        self._mirrors.run()
         self._tr_derived.run()
         return self.rho
 

@@ -26,6 +26,7 @@ from .hamiltonian import _Arena, _splitk
 
 
 ADJ_UNIT_MAX = 16     # blocks with at most this many states per side use the lane-per-coupling adjoint
+ORBITAL_FUSED = True  # integral derivatives of the orbital gradient by xrh_orbital_terms
 
 class XRDimerAdjoint:
     def __init__(self, plan, density_adjoint="simt"):
@@ -170,6 +171,7 @@ class XRDimerAdjoint:
         self.l3_tc = plan.tc
         self.l3_T = []
         self._l3_tr = None
+        self._mirror_adj_launch = None
         if plan.tc:
             # tensor cores (split precision, FP32 chunk sums): d rho = dP W on K-major W^T; dW = dP^T rho
             # on rho^T, which the density build leaves in its pre-transpose buffer
@@ -401,8 +403,12 @@ class XRDimerAdjoint:
         s = stream_ptr()
         for (b, grads, gz) in self.im_adj:
             b.adjoint(grads, gz)
-        for (gsrc, gdst, na, nb, Nm, L) in self.mirror_adj:
-            call("xrh_mirror_density", na, nb, Nm, L, ptr(gsrc), ptr(gdst), 1, s)
+        if self.mirror_adj:
+            if self._mirror_adj_launch is None:
+                self._mirror_adj_launch = _lib.Mirrors(
+                    [(gsrc, gdst, na, nb, Nm, L, 1) for (gsrc, gdst, na, nb, Nm, L) in self.mirror_adj],
+                    self.plan.device)
+            self._mirror_adj_launch.run()
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
@@ -554,10 +560,35 @@ class XRDimerAdjoint:
         else:
             b["A"] = V
             b["B"] = torch.empty((t,) * 4, **f64)
-        pairs = [(T, b["dT"], b["Gso"])] + [(U[k], b["dU"][k], b["Gso"]) for k in range(U.shape[0])]
+        # the derivative of every fragment potential U_k equals dT (both receive the same
+        # one-electron pieces)
+        pairs = [(T, b["dT"], b["Gso"])] + [(U[k], b["dT"], b["Gso"]) for k in range(U.shape[0])]
         b["one_body"] = _one_body_table(pairs, dev)
+        b["inputs"] = self._orbital_inputs()
         self._orb = b
         return b
+
+    def _orbital_inputs(self):
+        """Host struct of xrh_orbital_terms: the reverse pass's pieces of dE/dT and dE/dV."""
+        plan, G = self.plan, self.G
+        inp = np.zeros(1, dtype=_lib.ORBITAL_INPUTS_DTYPE)
+
+        def ptr_of(x):
+            if not x.is_contiguous() or x.dtype != torch.float64:
+                raise ValueError("orbital-gradient pieces must be contiguous FP64 tensors")
+            return x.data_ptr()
+
+        inp["gw"] = ptr_of(G[("gW", "v0101")])
+        for m in (0, 1):
+            inp["h1"][0, m] = ptr_of(G[("gW", ("h1", m))])
+            inp["cca"][0, m] = ptr_of(G[("gW", ("cca", m))])
+            inp["caa"][0, m] = ptr_of(G[("gW", ("caa", m))])
+            inp["cc"][0, m] = ptr_of(G[("gW", ("cc", m))])
+            inp["mono1"][0, m] = ptr_of(G[("gmono1", m)])
+            inp["gamma64"][0, m] = ptr_of(G[("Gamma", m)])
+            inp["gamma32"][0, m] = self.Gamma32[m].data_ptr() if self.prec32 else 0
+        inp["N0"], inp["N1"] = plan.N[0], plan.N[1]
+        return inp
 
     def orbital_gradient(self, T, U, V, spatial_index):
         """dE/dkappa (antisymmetric, spatial orbitals) for X' = R^T X R with R = exp(kappa)
@@ -572,32 +603,36 @@ class XRDimerAdjoint:
             for k in range(U.shape[0]):
                 Gso += U[k] @ dU[k].t() + U[k].t() @ dU[k]
         else:
-            dT, dU, dV, Gso = b["dT"], b["dU"], b["dV"], b["Gso"]
-            dT.zero_()
-            dU.zero_()
-            dV.zero_()
-            self._integral_gradients_into(dT, dU, dV)
-            Gso.zero_()
-            # the one-body terms T dT^T + T^T dT + sum_k U_k dU_k^T + U_k^T dU_k in one launch
-            tab, n_tab, ctas = b["one_body"]
-            call("xrh_abt_grouped", _lib.FP64, ptr(tab), n_tab, ctas, stream_ptr())
-        # E sees V only through its symmetric part (V_pqrs = -V_qprs = -V_pqsr = V_rspq for real
-        # orbitals), so dE/dV may be replaced by its projection on that symmetry; then the four
-        # index positions of V' = R^T..R contribute equally: dE/dR = 4 V_(1) Gbar_(1)^T
-        Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
-        if b is not None:
-            # 4 V_(1) Gbar_(1)^T with Gbar = (Ga + Ga^(rs,pq)) / 8: a t x t result over t^3 terms,
-            # split over CTAs by xrh_abt_small (FP32 products on the split-precision paths)
-            K3 = t ** 3
-            if self.prec32:
-                torch.add(Ga, Ga.permute(2, 3, 0, 1), out=b["B"])
-                b["A"].copy_(V)
-                prec = _lib.FP32
+            dT, Gso = b["dT"], b["Gso"]
+            prec = _lib.FP32 if self.prec32 else _lib.FP64
+            s = stream_ptr()
+            if ORBITAL_FUSED:
+                # dT and B = Ga + Ga^(rs,pq) element-wise from the reverse pass's pieces
+                call("xrh_orbital_terms", b["inputs"].ctypes.data, ptr(dT), ptr(b["B"]), prec, s)
             else:
+                dU, dV = b["dU"], b["dV"]
+                dT.zero_()
+                dU.zero_()
+                dV.zero_()
+                self._integral_gradients_into(dT, dU, dV)
+                Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
                 torch.add(Ga, Ga.permute(2, 3, 0, 1), out=b["B"])
-                prec = _lib.FP64
-            call("xrh_abt_small", prec, t, t, K3, ptr(b["A"]), K3, ptr(b["B"]), K3, 0.5, ptr(Gso), stream_ptr())
-        else:
+            Gso.zero_()
+            # the one-body terms T dT^T + T^T dT + sum_k U_k dU_k^T + U_k^T dU_k (dU_k = dT) in
+            # one launch
+            tab, n_tab, ctas = b["one_body"]
+            call("xrh_abt_grouped", _lib.FP64, ptr(tab), n_tab, ctas, s)
+            # E sees V only through its symmetric part (V_pqrs = -V_qprs = -V_pqsr = V_rspq for
+            # real orbitals), so dE/dV may be replaced by its projection on that symmetry; then
+            # the four index positions of V' = R^T..R contribute equally: dE/dR = 4 V_(1) Gbar_(1)^T
+            # with Gbar = B / 8: a t x t result over t^3 terms, split over CTAs by xrh_abt_small
+            # (FP32 products on the split-precision paths)
+            if self.prec32:
+                b["A"].copy_(V)
+            K3 = t ** 3
+            call("xrh_abt_small", prec, t, t, K3, ptr(b["A"]), K3, ptr(b["B"]), K3, 0.5, ptr(Gso), s)
+        if b is None:
+            Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
             Gbar = 0.125 * (Ga + Ga.permute(2, 3, 0, 1))
             Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
         key = (tuple(spatial_index), T.device)
