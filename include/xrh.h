@@ -471,6 +471,22 @@ int xrh_pair_scatter(int64_t n_entries, const int32_t* X_dev, const int64_t* off
 int xrh_pair_gather(int n_X, const int64_t* xptr_dev, const int64_t* off_dev,
                     const int8_t* sign_dev, const double* E_dev, int n, const int64_t* stride_dev,
                     double* sigmaT_dev, void* stream);
+/* Many xrh_pair_scatter (gather = 0) or xrh_pair_gather (gather = 1) calls in one launch.
+ * Scatter task: dst = D, src = zT, count = n_entries (X, off, sign, stride per entry).
+ * Gather task: dst = sigmaT, src = E, count = n_X (xptr, off, sign, stride per entry).
+ * max_total = the largest count * n over the tasks (it sizes the grid). */
+typedef struct {
+    const int32_t* X;
+    const int64_t* xptr;
+    const int64_t* off;
+    const int8_t* sign;
+    const int64_t* stride;
+    const double* src;
+    double* dst;
+    int64_t count;
+    int64_t n;
+} xrh_pair_task;   /* 72 bytes */
+int xrh_pair_grouped(int gather, const xrh_pair_task* tasks_dev, int n_tasks, int64_t max_total, void* stream);
 
 /* Transition densities through intermediate determinants K (no reference counterpart; they
  * replace the per-coupling outer products of density_tensors.c:142-556 on the split-precision

@@ -44,6 +44,7 @@ _SIGS = {
     "xrh_transpose_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_mirror_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_orbital_terms": (_i32, [_vp, _vp, _vp, _i32, _vp]),
+    "xrh_pair_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
     "xrh_gram_grouped": (_i32, [_vp, _i32, _i64, _i32, _vp]),
     "xrh_tangent_step": (_i32, [_vp, _i32, _i64, _dbl, _vp, _vp]),
     "xrh_inv_sqrt_small": (_i32, [_vp, _i32, _i32, _vp]),
@@ -168,6 +169,10 @@ DENS_TASK_DTYPE = np.dtype([("idx_ptr", np.uint64), ("P", np.uint64), ("Q", np.u
                             ("nb", np.int32), ("nk", np.int32), ("splits", np.int32), ("reserved", np.int32),
                             ("cta_begin", np.int64)])
 assert DENS_TASK_DTYPE.itemsize == 88
+PAIR_TASK_DTYPE = np.dtype([("X", np.uint64), ("xptr", np.uint64), ("off", np.uint64), ("sign", np.uint64),
+                            ("stride", np.uint64), ("src", np.uint64), ("dst", np.uint64), ("count", np.int64),
+                            ("n", np.int64)])
+assert PAIR_TASK_DTYPE.itemsize == 72
 ORBITAL_INPUTS_DTYPE = np.dtype([("gw", np.uint64), ("h1", np.uint64, 2), ("cca", np.uint64, 2),
                                  ("caa", np.uint64, 2), ("cc", np.uint64, 2), ("mono1", np.uint64, 2),
                                  ("gamma64", np.uint64, 2), ("gamma32", np.uint64, 2), ("N0", np.int32),
@@ -257,3 +262,26 @@ class Mirrors:
     def run(self, stream=None):
         if self.n:
             call("xrh_mirror_grouped", ptr(self.dev), self.n, self.ctas, stream_ptr(stream))
+
+
+class PairLaunch:
+    """A fixed list of pair scatters (gather=False: (pl, off, stride, zT, D, n)) or gathers
+    (gather=True: (pl, off, stride, E, sigmaT, n)) run as one xrh_pair_grouped launch."""
+
+    def __init__(self, items, gather, device):
+        import torch
+        tab = np.zeros(len(items), dtype=PAIR_TASK_DTYPE)
+        mx = 0
+        for i, (pl, off, stride, src, dst, n) in enumerate(items):
+            t = tab[i]
+            t["X"], t["xptr"] = pl["X_dev"].data_ptr(), pl["xptr_dev"].data_ptr()
+            t["off"], t["sign"], t["stride"] = off.data_ptr(), pl["sign_dev"].data_ptr(), stride.data_ptr()
+            t["src"], t["dst"], t["n"] = src.data_ptr(), dst.data_ptr(), n
+            t["count"] = (pl["xptr_dev"].numel() - 1) if gather else len(pl["X"])
+            mx = max(mx, int(t["count"]) * n)
+        self.gather, self.n, self.max_total, self.keep = int(gather), len(items), mx, items
+        self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(items) else None
+
+    def run(self, stream=None):
+        if self.n:
+            call("xrh_pair_grouped", self.gather, ptr(self.dev), self.n, self.max_total, stream_ptr(stream))

@@ -31,6 +31,7 @@ static_assert(sizeof(xrh_tc_segment) == 32, "xrh_tc_segment layout is part of th
 static_assert(sizeof(xrh_dens_task) == 88, "xrh_dens_task layout is part of the ABI");
 static_assert(sizeof(xrh_dens_adj_task) == 96, "xrh_dens_adj_task layout is part of the ABI");
 static_assert(sizeof(xrh_dens_adj_tc_task) == 112, "xrh_dens_adj_tc_task layout is part of the ABI");
+static_assert(sizeof(xrh_pair_task) == 72, "xrh_pair_task layout is part of the ABI");
 static_assert(sizeof(xrh_orbital_inputs) == 128, "xrh_orbital_inputs layout is part of the ABI");
 static_assert(sizeof(xrh_mirror_task) == 48, "xrh_mirror_task layout is part of the ABI");
 static_assert(sizeof(xrh_transpose_task) == 40, "xrh_transpose_task layout is part of the ABI");

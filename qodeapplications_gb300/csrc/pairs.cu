@@ -45,6 +45,36 @@ __global__ void pair_gather_kernel(int n_X, const int64_t* __restrict__ xptr, co
     }
 }
 
+// Many scatters / gathers in one launch: blockIdx.y is the task, blocks stride over its entries.
+__global__ void pair_scatter_grouped_kernel(const xrh_pair_task* __restrict__ tasks) {
+    const xrh_pair_task& T = tasks[blockIdx.y];
+    const int n = T.n;
+    const int64_t total = T.count * n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / n;
+        const int s = (int)(t - e * n);
+        const double v = __ldg(T.src + (int64_t)__ldg(T.X + e) * n + s);
+        T.dst[__ldg(T.off + e) + (int64_t)s * __ldg(T.stride + e)] = __ldg(T.sign + e) < 0 ? -v : v;
+    }
+}
+
+__global__ void pair_gather_grouped_kernel(const xrh_pair_task* __restrict__ tasks) {
+    const xrh_pair_task& T = tasks[blockIdx.y];
+    const int n = T.n;
+    const int64_t n_X = T.count;
+    const int64_t total = n_X * n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(t / n_X);
+        const int64_t x = t - (int64_t)s * n_X;
+        double acc = 0.0;
+        for (int64_t e = __ldg(T.xptr + x); e < __ldg(T.xptr + x + 1); ++e) {
+            const double v = __ldg(T.src + __ldg(T.off + e) + (int64_t)s * __ldg(T.stride + e));
+            acc += __ldg(T.sign + e) < 0 ? -v : v;
+        }
+        T.dst[(int64_t)s * n_X + x] = acc;
+    }
+}
+
 unsigned grid_for(int64_t total) {
     const int64_t b = (total + 255) / 256;
     return (unsigned)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
@@ -71,6 +101,20 @@ extern "C" int xrh_pair_gather(int n_X, const int64_t* xptr_dev, const int64_t* 
     if (!xptr_dev || !off_dev || !sign_dev || !E_dev || !stride_dev || !sigmaT_dev) return XRH_ERR_ARG;
     pair_gather_kernel<<<grid_for((int64_t)n_X * n), 256, 0, (cudaStream_t)stream>>>(n_X, xptr_dev, off_dev, sign_dev,
                                                                                     E_dev, n, stride_dev, sigmaT_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_pair_grouped(int gather, const xrh_pair_task* tasks_dev, int n_tasks, int64_t max_total,
+                                void* stream) {
+    if (n_tasks < 0 || max_total < 0 || n_tasks > 65535) return XRH_ERR_ARG;
+    if (n_tasks == 0 || max_total == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    const dim3 grid(grid_for(max_total), (unsigned)n_tasks);
+    if (gather)
+        pair_gather_grouped_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(tasks_dev);
+    else
+        pair_scatter_grouped_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(tasks_dev);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -172,6 +172,7 @@ class XRDimerAdjoint:
         self.l3_T = []
         self._l3_tr = None
         self._mirror_adj_launch = None
+        self._gamma_scatter = None
         if plan.tc:
             # tensor cores (split precision, FP32 chunk sums): d rho = dP W on K-major W^T; dW = dP^T rho
             # on rho^T, which the density build leaves in its pre-transpose buffer
@@ -434,8 +435,12 @@ class XRDimerAdjoint:
         """Two-particle densities of the monomer two-electron terms (after launch 2)."""
         plan = self.plan
         s = stream_ptr()
-        for (m, c, sg, Dy) in self.gamma_ri:
-            sg.scatter(self.G[("YT", m, c)], Dy)
+        if self.gamma_ri:
+            if self._gamma_scatter is None:
+                self._gamma_scatter = _lib.PairLaunch(
+                    [(sg.pl, sg.off_dev, sg.stride_dev, self.G[("YT", m, c)], Dy, sg.n) for (m, c, sg, Dy) in self.gamma_ri],
+                    False, self.plan.device)
+            self._gamma_scatter.run()
         for src, dst in self.gam_T:
             dst.copy_(src.t())
         if self.gam_T:

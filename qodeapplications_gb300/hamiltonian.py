@@ -104,7 +104,7 @@ class SigmaTwoElectron:
     density then holds the same-class blocks only: the entries between pairs of different
     spin classes multiply integrals that vanish by spin symmetry."""
 
-    def __init__(self, space, charge, n_states, V_block, precision=_lib.FP64):
+    def __init__(self, space, charge, n_states, V_block, precision=_lib.FP64, own_gemm=True):
         self.space, self.c, self.n = space, charge, n_states
         self.V = V_block.contiguous()
         self.precision = precision if precision in (_lib.FP64, _lib.FP32) else _lib.FP32
@@ -130,10 +130,11 @@ class SigmaTwoElectron:
             # split-precision plans: 3 x TF32 on the tensor cores (sigma feeds the monomer
             # energies, the largest entries of H); FP64 plans: the FP64 grouped GEMM
             self.tc = self.precision == _lib.FP32
-            if self.tc:
+            self.reg, self.gemm, g = None, None, None
+            if own_gemm and self.tc:
                 self.reg = SplitRegistry("tf32x3", dev)
                 g = TCGroupedGemm(self.reg)
-            else:
+            elif own_gemm:
                 g = GroupedGemm(dev, precision="fp64")
             for cl in pl["classes"]:
                 u = torch.as_tensor(cl["u"], device=dev)
@@ -146,17 +147,25 @@ class SigmaTwoElectron:
                 Ec = self.E[b:b + n * nK * npr].view(n * nK, npr)
                 self.Dc.append(Dc)
                 self.Ec.append(Ec)
-                # E[c][(s, K)][pq] = sum_rs D[c][(s, K)][rs] W_c[pq, rs]
-                if self.tc:
-                    g.add(n * nK, npr, [(Dc, npr, W, npr, npr, 1.0)], Ec, npr, mode=0, groups=[("sig", "sigW")])
-                else:
-                    g.add(n * nK, npr, [(Dc, npr, W, npr, npr, 1.0)], Ec, npr, mode=0)
-            if self.tc:
+                if g is not None:
+                    self.add_gemm_tasks(g, len(self.Dc) - 1)
+            if g is not None and self.tc:
                 self.reg.upload()
                 self.reg.split("sigW")
                 self.gemm = g.finalize().autotune()
-            else:
+            elif g is not None:
                 self.gemm = g.finalize()
+
+    def add_gemm_tasks(self, g, k):
+        """E[c][(s, K)][pq] = sum_rs D[c][(s, K)][rs] W_c[pq, rs] for spin class k into grouped
+        GEMM g (tensor cores, 3 x TF32, when self.tc)."""
+        cl = self.pl["classes"][k]
+        rows, npr = self.n * cl["n_K"], cl["n_p"]
+        if self.tc:
+            g.add(rows, npr, [(self.Dc[k], npr, self.W[k], npr, npr, 1.0)], self.Ec[k], npr, mode=0,
+                  groups=[("sig", "sigW")])
+        else:
+            g.add(rows, npr, [(self.Dc[k], npr, self.W[k], npr, npr, 1.0)], self.Ec[k], npr, mode=0)
 
     def set_V(self, V_block):
         """New integrals in place (the launch tables keep their pointers)."""
@@ -164,7 +173,7 @@ class SigmaTwoElectron:
         if self.pl is not None:
             for W, (u, v) in zip(self.W, self._uv):
                 W.copy_(4.0 * self.V[u[:, None], v[:, None], u[None, :], v[None, :]])
-            if self.tc:
+            if self.reg is not None:
                 self.reg.split("sigW")
 
     def _spin_conserving(self, space):
@@ -188,6 +197,8 @@ class SigmaTwoElectron:
                  ptr(sp.sorted_masks[c]), ptr(sp.sorted_pos[c]), sp.n_conf[c], ptr(sp.rank_table[c]),
                  sp.table_size[c], ptr(sp.binom), ptr(zT), self.n, ptr(self.sigmaT), stream_ptr())
             return
+        if self.gemm is None:
+            raise RuntimeError("this sigma runs inside a SigmaBatch")
         pl = self.pl
         self.scatter(zT, self.D)
         if self.tc:
@@ -195,6 +206,49 @@ class SigmaTwoElectron:
         self.gemm.run()
         call("xrh_pair_gather", sp.n_conf[c], ptr(pl["xptr_dev"]), ptr(self.off_dev), ptr(pl["sign_dev"]),
              ptr(self.E), self.n, ptr(self.stride_dev), ptr(self.sigmaT), stream_ptr())
+
+
+class SigmaBatch:
+    """Every pair-list sigma of a plan in four launches: one grouped pair scatter, one operand
+    split (tensor-core plans), one grouped GEMM over all spin classes, fragments and charges,
+    one grouped pair gather.  items: [(SigmaTwoElectron built with own_gemm=False, its zT)]."""
+
+    def __init__(self, items, device):
+        self.items = items
+        self.tc = bool(items) and items[0][0].tc
+        self.scatter = _lib.PairLaunch([(sg.pl, sg.off_dev, sg.stride_dev, zT, sg.D, sg.n) for sg, zT in items],
+                                       False, device)
+        self.gather = _lib.PairLaunch([(sg.pl, sg.off_dev, sg.stride_dev, sg.E, sg.sigmaT, sg.n)
+                                       for sg, zT in items], True, device)
+        self.reg = SplitRegistry("tf32x3", device) if self.tc else None
+        g = TCGroupedGemm(self.reg) if self.tc else GroupedGemm(device, precision="fp64")
+        for sg, _zT in items:
+            for k in range(len(sg.Dc)):
+                sg.add_gemm_tasks(g, k)
+        if self.tc:
+            self.reg.upload()
+            self.reg.split("sigW")
+            self.gemm = g.finalize().autotune()
+        else:
+            self.gemm = g.finalize()
+
+    def run(self):
+        if not self.items:
+            return
+        self.scatter.run()
+        if self.tc:
+            self.reg.split("sig")
+        self.gemm.run()
+        self.gather.run()
+
+    def refresh_W(self):
+        """Re-split W after the sigmas' set_V (tensor-core plans)."""
+        if self.tc:
+            self.reg.split("sigW")
+
+    def check(self):
+        if self.tc and self.items:
+            self.gemm.check()
 
 
 def monomer_two_electron(space, coeffs, V_block, c):
@@ -392,7 +446,7 @@ class XRDimerPlan:
                 n = ns[m][c]
                 ca = rho[m]["ca"][(c, c)]
                 sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m),
-                                      precision=_lib.PRECISIONS[self.sigma_precision])
+                                      precision=_lib.PRECISIONS[self.sigma_precision], own_gemm=False)
                 self.sigma[m][c] = sg
                 nconf = spaces[m].n_conf[c]
                 zrow = self.coeffs[m][c]
@@ -406,6 +460,8 @@ class XRDimerPlan:
                 for tgt in targets_du:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))
+        self.sigma_batch = SigmaBatch([(sg, self.builders[m].zT[c]) for m in (0, 1)
+                                       for c, sg in self.sigma[m].items() if sg.pl is not None], dev)
         # one-column terms (rho^ca . h) are row GEMVs: a 64 x 64 FP64 tile would spend 64x the
         # FMAs of the result on them, and an FP64 tile is slow on this part
         self.mono_gemv = [(sg_[0][0], sg_[0][2], out_, M_, sg_[0][4]) for (M_, N_, sg_, out_, _l, _s) in mono if N_ == 1]
@@ -589,6 +645,7 @@ class XRDimerPlan:
         for m in (0, 1):
             for c, sg in self.sigma[m].items():
                 sg.set_V(ints.V(m, m, m, m))
+        self.sigma_batch.refresh_W()
         if self.tc:
             self.reg.split("W")
         self.ints = ints
@@ -603,8 +660,11 @@ class XRDimerPlan:
         """Enqueue the whole build (densities, sigma, precontractions, final blocks)."""
         for m in (0, 1):
             self.builders[m].build(self.coeffs[m])
+        self.sigma_batch.run()
+        for m in (0, 1):
             for c, sg in self.sigma[m].items():
-                sg.run_sigma(self.builders[m].zT[c])
+                if sg.pl is None:
+                    sg.run_sigma(self.builders[m].zT[c])
         self.arena.buf.zero_()
         s = stream_ptr()
         if self.mono_gemv_tasks is not None:
@@ -656,10 +716,7 @@ class XRDimerPlan:
         for b in self.builders:
             if hasattr(b, "check"):
                 b.check()
-        for m in (0, 1):
-            for sg in self.sigma[m].values():
-                if sg.tc:
-                    sg.gemm.check()
+        self.sigma_batch.check()
 
 
 def lowest_eigenpairs(H, k=5):
