@@ -27,6 +27,7 @@ from .hamiltonian import _Arena, _splitk
 
 ADJ_UNIT_MAX = 16     # blocks with at most this many states per side use the lane-per-coupling adjoint
 ORBITAL_FUSED = True  # integral derivatives of the orbital gradient by xrh_orbital_terms
+GAMMA_TC_MIN = 0      # Gamma pair blocks with n * n_K >= this go to the tensor cores (3 x TF32)
 
 class XRDimerAdjoint:
     def __init__(self, plan, density_adjoint="simt"):
@@ -173,6 +174,7 @@ class XRDimerAdjoint:
         self._l3_tr = None
         self._mirror_adj_launch = None
         self._gamma_scatter = None
+        self._gam_tr = None
         if plan.tc:
             # tensor cores (split precision, FP32 chunk sums): d rho = dP W on K-major W^T; dW = dP^T rho
             # on rho^T, which the density build leaves in its pre-transpose buffer
@@ -257,7 +259,7 @@ class XRDimerAdjoint:
                     Dyc = Dy[b:b + n * nK * npr].view(n * nK, npr)
                     Gp = self.G[("Gpairs", m)][off:off + npr * npr].view(npr, npr)
                     off += npr * npr
-                    if sg.tc and n * nK >= 8192:
+                    if sg.tc and n * nK >= GAMMA_TC_MIN:
                         # Gamma_c = D^T Dy on the tensor cores (3 x TF32), from K-major transposed
                         # copies; n states x n_K intermediates is a long K: split-K, FP64 atomics
                         DT = torch.empty((npr, n * nK), **f64)
@@ -441,9 +443,10 @@ class XRDimerAdjoint:
                     [(sg.pl, sg.off_dev, sg.stride_dev, self.G[("YT", m, c)], Dy, sg.n) for (m, c, sg, Dy) in self.gamma_ri],
                     False, self.plan.device)
             self._gamma_scatter.run()
-        for src, dst in self.gam_T:
-            dst.copy_(src.t())
         if self.gam_T:
+            if self._gam_tr is None:
+                self._gam_tr = _lib.Transposes([(a, b, a.shape[0], a.shape[1]) for a, b in self.gam_T], self.plan.device)
+            self._gam_tr.run()
             self.gam_reg.split("gam")
         self.Lgamma.run()
         self.Lgamma_tc.run()
