@@ -68,16 +68,43 @@ __device__ __forceinline__ T ga_at(const xrh_orbital_inputs& in, int p, int q, i
     return dv_at<T>(in, p, q, r, s) - dv_at<T>(in, q, p, r, s) - dv_at<T>(in, p, q, s, r) + dv_at<T>(in, q, p, s, r);
 }
 
+// (i, j) with i <= j from a triangular index k = j (j + 1) / 2 + i (float estimate, fixed up)
+__device__ __forceinline__ void tri_decode(int64_t k, int64_t& i, int64_t& j) {
+    j = (int64_t)((sqrt(8.0 * (double)k + 1.0) - 1.0) * 0.5);
+    while (j * (j + 1) / 2 > k) --j;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    i = k - j * (j + 1) / 2;
+}
+
+// B has the symmetry B[pqrs] = -B[qprs] = -B[pqsr] = B[rspq] (and B = 0 for p = q or r = s, set
+// by the caller's zero fill): one thread per canonical element p < q, r < s, (pq) <= (rs)
+// evaluates it once and writes its up to eight images.
 template <typename T>
 __global__ void __launch_bounds__(256) orbital_B_kernel(xrh_orbital_inputs in, T* __restrict__ B) {
     const int t = in.N0 + in.N1;
-    const int64_t t2 = (int64_t)t * t, t4 = t2 * t2;
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= t4) return;
-    const int64_t pq = e / t2, rs = e - pq * t2;
-    const int p = (int)(pq / t), q = (int)(pq - (pq / t) * t);
-    const int r = (int)(rs / t), s = (int)(rs - (rs / t) * t);
-    B[e] = ga_at<T>(in, p, q, r, s) + ga_at<T>(in, r, s, p, q);
+    const int64_t np = (int64_t)t * (t - 1) / 2;                 // pairs p < q
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np * (np + 1) / 2) return;
+    int64_t P, R;
+    tri_decode(k, P, R);                                          // pair indices P <= R
+    int64_t p, q, r, s;
+    tri_decode(P, p, q);                                          // p <= q - 1 of pair P
+    tri_decode(R, r, s);
+    q += 1;                                                       // pair P = (p, q) with p < q
+    s += 1;
+    const T v = ga_at<T>(in, (int)p, (int)q, (int)r, (int)s) + ga_at<T>(in, (int)r, (int)s, (int)p, (int)q);
+    const int64_t t2 = (int64_t)t * t;
+    const int64_t pq = p * t + q, qp = q * t + p, rs = r * t + s, sr = s * t + r;
+    B[pq * t2 + rs] = v;
+    B[qp * t2 + rs] = -v;
+    B[pq * t2 + sr] = -v;
+    B[qp * t2 + sr] = v;
+    if (P != R) {
+        B[rs * t2 + pq] = v;
+        B[sr * t2 + pq] = -v;
+        B[rs * t2 + qp] = -v;
+        B[sr * t2 + qp] = v;
+    }
 }
 
 __global__ void __launch_bounds__(256) orbital_dT_kernel(xrh_orbital_inputs in, double* __restrict__ dT) {
@@ -106,13 +133,17 @@ extern "C" int xrh_orbital_terms(const xrh_orbital_inputs* in_host, double* dT_d
     cudaStream_t s = (cudaStream_t)stream;
     orbital_dT_kernel<<<(unsigned)((t * t + 255) / 256), 256, 0, s>>>(in, dT_dev);
     XRH_CHECK_LAUNCH();
-    const unsigned blocks = (unsigned)((t4 + 255) / 256);
-    if (precision == XRH_FP32)
+    const int64_t np = (int64_t)t * (t - 1) / 2;
+    const unsigned blocks = (unsigned)((np * (np + 1) / 2 + 255) / 256);
+    if (precision == XRH_FP32) {
+        if (cudaMemsetAsync(B_dev, 0, sizeof(float) * (size_t)t4, s) != cudaSuccess) return XRH_ERR_CUDA;
         orbital_B_kernel<float><<<blocks, 256, 0, s>>>(in, reinterpret_cast<float*>(B_dev));
-    else if (precision == XRH_FP64)
+    } else if (precision == XRH_FP64) {
+        if (cudaMemsetAsync(B_dev, 0, sizeof(double) * (size_t)t4, s) != cudaSuccess) return XRH_ERR_CUDA;
         orbital_B_kernel<double><<<blocks, 256, 0, s>>>(in, reinterpret_cast<double*>(B_dev));
-    else
+    } else {
         return XRH_ERR_ARG;
+    }
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }
