@@ -294,14 +294,15 @@ int xrh_lanczos_small(int n, int m, const double* H_dev, int64_t ld, const doubl
  * sums and the barrier words, reset by this call).  A barrier wait that exceeds its poll
  * limit sets *status_dev = XRH_ERR_TIMEOUT and the kernel returns early; *status_dev must be
  * XRH_OK on entry. */
-/* The same loop inside one thread-block cluster (8 or 16 CTAs, one per SM; hardware cluster
- * barriers, partial sums and V[j+1] exchanged through distributed shared memory, H rows kept
- * in shared memory when they fit).  XRH_ERR_CAPACITY when the sector does not fit the
- * cluster's shared memory (then use xrh_lanczos_coop). */
+/* The same loop inside one thread-block cluster (up to 16 CTAs, one per SM; at most max_ctas
+ * when max_ctas > 0; hardware cluster barriers, partial sums and V[j+1] exchanged through
+ * distributed shared memory, H rows kept in shared memory when they fit).  XRH_ERR_CAPACITY
+ * when the sector does not fit the cluster's shared memory (then use xrh_lanczos_coop). */
 int xrh_lanczos_cluster(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
-                        double* alpha_dev, double* beta_dev, void* stream);
-/* 1 when xrh_lanczos_cluster can take an n x n sector and m steps on the current device. */
-int xrh_lanczos_cluster_fits(int n, int m);
+                        double* alpha_dev, double* beta_dev, int max_ctas, void* stream);
+/* 1 when xrh_lanczos_cluster can take an n x n sector and m steps (same max_ctas) on the
+ * current device. */
+int xrh_lanczos_cluster_fits(int n, int m, int max_ctas);
 int64_t xrh_lanczos_coop_work(int m);
 int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
                      double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,

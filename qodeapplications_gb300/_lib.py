@@ -32,8 +32,8 @@ _SIGS = {
     "xrh_density_adjoint_tc_grouped": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "xrh_lanczos_small": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "xrh_lanczos_coop_work": (_i64, [_i32]),
-    "xrh_lanczos_cluster": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
-    "xrh_lanczos_cluster_fits": (_i32, [_i32, _i32]),
+    "xrh_lanczos_cluster": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _vp]),
+    "xrh_lanczos_cluster_fits": (_i32, [_i32, _i32, _i32]),
     "xrh_lanczos_coop": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "xrh_state_ctas": (_i32, [_i64]),
     "xrh_abt_ctas": (_i32, [_i64]),

@@ -593,12 +593,12 @@ static size_t lanczos_cluster_smem(int n, int m, int nb, int h_smem, int smem_op
 // else 8), H in shared memory or not, and the shared memory per CTA for an n x n sector and m
 // steps.  Decided once per shape (on the first, eager call) and cached, so no occupancy query
 // runs inside a stream capture.  Returns false when no cluster takes the sector.
-static bool lanczos_cluster_choice(int n, int m, int& nb, int& h_smem, size_t& smem) {
-    struct Choice { int n, m, nb, h_smem; size_t smem; bool ok; };
+static bool lanczos_cluster_choice(int n, int m, int max_ctas, int& nb, int& h_smem, size_t& smem) {
+    struct Choice { int n, m, max_ctas, nb, h_smem; size_t smem; bool ok; };
     static Choice cache[32];
     static int n_cache = 0;
     for (int i = 0; i < n_cache; ++i)
-        if (cache[i].n == n && cache[i].m == m) {
+        if (cache[i].n == n && cache[i].m == m && cache[i].max_ctas == max_ctas) {
             nb = cache[i].nb;
             h_smem = cache[i].h_smem;
             smem = cache[i].smem;
@@ -616,7 +616,8 @@ static bool lanczos_cluster_choice(int n, int m, int& nb, int& h_smem, size_t& s
             nonportable = cudaFuncSetAttribute(lanczos_cluster_kernel,
                                                cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess ? 1 : 0;
         static size_t smem_set = 48 * 1024;
-        for (int want = nonportable ? 16 : 8; !ok && want >= 8; want -= 8) {
+        const int top = (nonportable ? 16 : 8) < max_ctas || max_ctas <= 0 ? (nonportable ? 16 : 8) : max_ctas;
+        for (int want = top; !ok && want >= 1; want = want > 8 ? 8 : want / 2) {
             nb = want < n ? want : n;
             h_smem = 1;
             smem = lanczos_cluster_smem(n, m, nb, 1, smem_optin);
@@ -647,24 +648,24 @@ static bool lanczos_cluster_choice(int n, int m, int& nb, int& h_smem, size_t& s
         }
         cudaGetLastError();
     }
-    if (n_cache < 32) cache[n_cache++] = Choice{n, m, nb, h_smem, smem, ok};
+    if (n_cache < 32) cache[n_cache++] = Choice{n, m, max_ctas, nb, h_smem, smem, ok};
     return ok;
 }
 
-extern "C" int xrh_lanczos_cluster_fits(int n, int m) {
+extern "C" int xrh_lanczos_cluster_fits(int n, int m, int max_ctas) {
     if (n <= 0 || m <= 0) return 0;
     int nb, h_smem;
     size_t smem;
-    return lanczos_cluster_choice(n, m, nb, h_smem, smem) ? 1 : 0;
+    return lanczos_cluster_choice(n, m, max_ctas, nb, h_smem, smem) ? 1 : 0;
 }
 
 extern "C" int xrh_lanczos_cluster(int n, int m, const double* H_dev, int64_t ld, const double* v0_dev, double* V_dev,
-                                   double* alpha_dev, double* beta_dev, void* stream) {
+                                   double* alpha_dev, double* beta_dev, int max_ctas, void* stream) {
     if (n <= 0 || m <= 0 || ld < n) return XRH_ERR_ARG;
     if (!H_dev || !v0_dev || !V_dev || !alpha_dev || !beta_dev) return XRH_ERR_ARG;
     int nb = 0, h_smem = 0;
     size_t smem = 0;
-    if (!lanczos_cluster_choice(n, m, nb, h_smem, smem)) return XRH_ERR_CAPACITY;
+    if (!lanczos_cluster_choice(n, m, max_ctas, nb, h_smem, smem)) return XRH_ERR_CAPACITY;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

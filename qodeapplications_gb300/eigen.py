@@ -20,10 +20,12 @@ from ._lib import call, ptr, stream_ptr
 
 SMALL_SECTOR = 2048
 MODES = ("auto", "cluster", "coop", "small", "steps")
+CLUSTER_MAX_CTAS = 0     # CTAs of the cluster loop at most (0: the largest cluster the part runs)
+CLUSTER_MAX_N = 512      # "auto" takes the cluster loop up to this sector size, the cooperative one above
 
 
 class Lanczos:
-    def __init__(self, n, m=96, device="cuda", seed=7, mode="auto"):
+    def __init__(self, n, m=96, device="cuda", seed=7, mode="auto", cluster_ctas=None):
         self.n = int(n)
         self.m = int(min(m, n))
         dev = torch.device(device)
@@ -44,9 +46,12 @@ class Lanczos:
             raise ValueError(f"mode must be one of {MODES}")
         if mode == "small" and self.n > SMALL_SECTOR:
             mode = "steps"
+        self.cluster_ctas = CLUSTER_MAX_CTAS if cluster_ctas is None else int(cluster_ctas)
         if mode in ("auto", "cluster"):
             from ._lib import lib
-            fits = bool(lib().xrh_lanczos_cluster_fits(self.n, self.m))
+            fits = bool(lib().xrh_lanczos_cluster_fits(self.n, self.m, self.cluster_ctas))
+            if mode == "auto" and self.n > CLUSTER_MAX_N:
+                fits = False
             if mode == "cluster" and not fits:
                 raise ValueError("sector too large for the cluster Lanczos loop")
             mode = "cluster" if fits else "coop"
@@ -65,7 +70,7 @@ class Lanczos:
         ld = n if ld is None else ld
         if self.mode == "cluster":
             call("xrh_lanczos_cluster", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab), ptr(self.ab[m:]),
-                 s)
+                 self.cluster_ctas, s)
             return
         if self.mode == "coop":
             call("xrh_lanczos_coop", n, m, ptr(H), ld, ptr(self.v0), ptr(self.V), ptr(self.ab), ptr(self.ab[m:]),

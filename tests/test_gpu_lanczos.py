@@ -25,7 +25,7 @@ def _matrix(n, seed):
 def test_lanczos_modes(n, m, mode):
     from qodeapplications_gb300 import _lib
     from qodeapplications_gb300.eigen import Lanczos
-    if mode == "cluster" and not _lib.lib().xrh_lanczos_cluster_fits(n, m):
+    if mode == "cluster" and not _lib.lib().xrh_lanczos_cluster_fits(n, m, 0):
         pytest.skip("sector larger than the cluster loop takes")
     A, w0 = _matrix(n, n + m)
     Ad = A.cuda()
@@ -49,7 +49,7 @@ def test_lanczos_coop_matches_steps(n, m):
     A, _ = _matrix(n, 5)
     Ad = A.cuda()
     out = {}
-    modes = ["coop", "steps"] + (["cluster"] if _lib.lib().xrh_lanczos_cluster_fits(n, m) else [])
+    modes = ["coop", "steps"] + (["cluster"] if _lib.lib().xrh_lanczos_cluster_fits(n, m, 0) else [])
     for mode in modes:
         lz = Lanczos(n, m=m, mode=mode)
         lz.krylov(Ad)
@@ -85,3 +85,19 @@ def test_lanczos_in_graph(mode):
     torch.cuda.synchronize()
     w, resid = lz.solve(1)
     assert abs(w[0] - w0) <= 1e-10 * abs(w0) + resid
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 4, 8])
+def test_lanczos_cluster_sizes_agree(ctas):
+    """The cluster loop with at most 1, 2, 4 or 8 CTAs gives the per-step launches' result."""
+    from qodeapplications_gb300.eigen import Lanczos
+    A, _ = _matrix(300, 11)
+    Ad = A.cuda()
+    out = {}
+    for mode, kw in (("steps", {}), ("cluster", {"cluster_ctas": ctas})):
+        lz = Lanczos(300, m=24, mode=mode, **kw)
+        lz.krylov(Ad)
+        lz.stage_to_host()
+        torch.cuda.synchronize()
+        out[mode] = lz._host[:48].numpy().copy()
+    assert np.abs(out["cluster"] - out["steps"]).max() <= 1e-11 * np.abs(out["steps"]).max()
