@@ -10,6 +10,7 @@ energy/gradient copied back every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|3] [--precision P]
   python bench.py --impl reference ...   (the FP64 CPU oracle on the host cores)
+  python bench.py --config 2 ...         (trimer: pair builds + matrix-free H x v Lanczos ground state)
 
 Multi-GPU: the path does not shard (one dimer), so N>1 runs N independent replicas
 (one per rank, launched by torchrun); value = total iterations / max time over ranks.
@@ -26,6 +27,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 CONFIGS = {
+    2: dict(n_orb=14, n_states=40, n_frag=3,
+            name="linear trimer 3x14 spatial orbitals (28 spin orbitals each), 40 states per charge sector "
+                 "(+1,0,-1), neutral sector of the product space (448 000 states), matrix-free H x v"),
     1: dict(n_orb=9, n_states=10, name="dimer 2x9 spatial orbitals (18 spin orbitals each), 10 states per charge "
                                       "sector (+1,0,-1; 3/4/5 electrons), order-0 XR-H 900x900"),
     3: dict(n_orb=14, n_states=60, name="dimer 2x14 spatial orbitals (28 spin orbitals each), 60 states per charge "
@@ -45,6 +49,7 @@ def parse():
     p.add_argument("--precision", default="tf32x3")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-variants", action="store_true")
+    p.add_argument("--states", type=int, default=None, help="states per charge sector (default: the config's)")
     return p.parse_args()
 
 
@@ -399,9 +404,126 @@ def accuracy_check(sysd):
     return out
 
 
+def run_trimer(args):
+    """Linear trimer: one step = the three pair builds (densities, monomer and dimer blocks),
+    the per-build trimer stage and an FP64 Lanczos of lanczos_m matrix-free H x v products in
+    the neutral sector -> lowest eigenvalue.  Variants: fp64 (pair builds and H x v in FP64)
+    and the split form (3xTF32 pair builds, FP32-product / FP64-sum H x v)."""
+    import torch
+    import numpy as np
+    from qodeapplications_gb300 import _lib
+    from qodeapplications_gb300 import synthetic as S
+    from qodeapplications_gb300.densities import FragmentSpace
+    from qodeapplications_gb300.hamiltonian import DeviceIntegrals
+    from qodeapplications_gb300.trimer_hv import XRTrimerHamiltonian
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    c = dict(CONFIGS[2])
+    if args.states:
+        c["n_states"] = args.states
+        c["name"] = c["name"].replace("40 states", f"{args.states} states").replace("(448 000 states)", "")
+    charges = [+1, 0, -1]
+    sysd = S.make_system(n_frag=3, n_orb=c["n_orb"], n_states=c["n_states"], charges=charges, seed=SEED)
+    spaces = [FragmentSpace({q: sysd["states"][m][q][1] for q in charges}, c["n_orb"], 0, sysd["n_elec_ref"])
+              for m in range(3)]
+    ns = [{q: c["n_states"] for q in charges}] * 3
+    ints = DeviceIntegrals(h=sysd["h"], V=sysd["V"], Ns=sysd["Ns"])
+    host = [{q: torch.as_tensor(sysd["states"][m][q][0]).pin_memory() for q in charges} for m in range(3)]
+    dev = [{q: t.to("cuda") for q, t in d.items()} for d in host]
+    lanczos_m = 30
+    forms = {"fp64": ("fp64", "fp64"), "split": ("tf32x3", "fp32")}
+    want = ["fp64", "split"] if args.precision in ("fp64", "tf32x3") and not args.no_variants else \
+        ["fp64" if args.precision == "fp64" else "split"]
+    head = "fp64" if args.precision == "fp64" else "split"
+    out = {}
+    for form in [head] + [f for f in want if f != head]:
+        prec, hvp = forms[form]
+        ham = XRTrimerHamiltonian(spaces, ns, [charges] * 3, ints, precision=prec, hv_precision=hvp, total_charge=0)
+        ham.set_coeffs(dev)
+
+        def step():
+            ham.build()
+            w, resid = ham.lowest(k=1, m=lanczos_m)
+            return float(w[0]), float(resid)
+
+        for _ in range(max(args.warmup, 3) if form == head else 1):
+            step()
+        torch.cuda.synchronize()
+        n_steps = args.steps if form == head else max(1, min(args.steps, 2))
+        _lib.LaunchCounter.count = 0
+        ms, Es = [], []
+        clock_path = os.path.join(tempfile.gettempdir(), f"xrh_clocks_t_{os.getpid()}.csv")
+        with ClockSampler(clock_path) as cs:
+            for _ in range(n_steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                Es.append(step())
+                e1.record()
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+        rec = {"s_per_iter": sum(ms) / 1e3 / n_steps, "E0": Es[-1][0], "resid": Es[-1][1],
+               "gpu_launches": _lib.LaunchCounter.count, "clocks": cs.summary(int(os.environ.get("LOCAL_RANK", "0")))}
+        # dominant kernel: stage B of H x v (x' segments, 2 n^4 N^2 FLOPs per trimer block)
+        st = ham.stages[1]
+        st.run()
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(5):
+            st.run()
+        t1.record()
+        torch.cuda.synchronize()
+        rec["stageB_ms"] = t0.elapsed_time(t1) / 5
+        rec["stageB_tflops"] = st.flops / (rec["stageB_ms"] * 1e-3) / 1e12
+        rec["hv_gflop"] = ham.flops_apply / 1e9
+        if form == head:
+            # e2e: coefficients from pinned host memory in, the energy out, every step
+            e2e = []
+            for _ in range(n_steps):
+                t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                t0.record()
+                for m in range(3):
+                    for q in charges:
+                        dev[m][q].copy_(host[m][q], non_blocking=True)
+                ham.set_coeffs(dev)
+                step()
+                t1.record()
+                torch.cuda.synchronize()
+                e2e.append(t0.elapsed_time(t1))
+            rec["e2e"] = sum(e2e) / 1e3 / n_steps
+            rec["h2d"] = sum(t.numel() * 8 for d in host for t in d.values())
+        out[form] = rec
+        del ham
+        torch.cuda.empty_cache()
+    r = out[head]
+    line = {
+        "metric": "XR-H trimer build + matrix-free Lanczos ground state s/iter", "value": r["s_per_iter"],
+        "unit": "s/iter", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["s_per_iter"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if head == "fp64" else "tf32x3 pair builds, fp32-product H x v",
+        "data": "synthetic (seeded h ~ N(0,0.1), V = sum_K L L with K=40, Sz-definite QR-orthonormal Gaussian CI vectors)",
+        "config": {"workload": c["name"], "lanczos_steps": lanczos_m,
+                   "l2": "inputs larger than L2 (pair sector matrices and intermediates of several GB)",
+                   "step": "three pair builds + trimer stage 1 + 30 Lanczos steps of H x v (FP64 Lanczos)"},
+        "e2e": {"value": r["e2e"], "unit": "s/iter", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": 8},
+        "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "E0": r["E0"], "resid": r["resid"],
+        "roofline": {"bound": "fp64 pipe" if head == "fp64" else "fp32 pipe", "kernel": "gemm_fp64_kernel (H x v stage B)",
+                     "achieved": r["stageB_tflops"], "unit": "TFLOP/s", "launch_ms": r["stageB_ms"],
+                     "peak": None, "frac": None, "traffic": None},
+        "variants": out,
+    }
+    if "fp64" in out and "split" in out:
+        line["dE0_split_vs_fp64"] = abs(out["split"]["E0"] - out["fp64"]["E0"])
+        line["speedup_split_vs_fp64"] = out["fp64"]["s_per_iter"] / out["split"]["s_per_iter"]
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.config == 2:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference diagonalises the dense three-fragment "
+                          "H, 1.7 M x 1.7 M at this size (23 TB in FP64); no CPU run of it is possible"}))
         return
     sysd = make_system(args.config)
     times = []
@@ -425,5 +547,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == 2:
+        run_trimer(a)
     else:
         run_ours(a)

@@ -1,0 +1,467 @@
+"""Hamiltonian-vector products of the order-0 general-XRCC Hamiltonian of three fragments,
+without forming H.
+
+general-XRCC builds H one element at a time (build_H.py:38-188: monomer, dimer and trimer
+elements, embedded into the product basis by general-XRCC/hamiltonian.py:18-80) and
+diagonalises it densely.  For three fragments of 14 spatial orbitals with 40 states per
+charge (+1, 0, -1) the product space has 120^3 = 1.7 M states and one trimer charge block
+alone is 64 000 x 64 000 (33 GB in FP64), so here H is never formed.  w = H v is evaluated
+term by term on a vector stored block by block over charge triples (c0, c1, c2), each block
+a row-major (n_c0, n_c1, n_c2) array:
+
+  monomers  w[i0,i1,i2] += H1_f[i_f, j_f] v[..., j_f, ...]          f = 0, 1, 2
+  pairs     w += (H2_ab x 1_s) v                                       (a,b) = (0,1), (1,2), (0,2)
+            H2_ab: the pair's dimer blocks (build_H.py:48-102) as dense per-total-charge
+            sector matrices from XRDimerPlan; on (0,2) the spectator phase (-1)^(n_1 dq)
+            of moving an odd number of operators past fragment 1's creation string
+  triples   w[x,y,z] += a sum P[x,x',r,s] R2[y,y',r] R3[z,z',s] v[x',y',z']
+            P = R1 . W (+ delta U / 4), the first stage of trimer.XRTrimerPlan, once per build
+
+For a trimer charge block with fragment order (x, y, z) (build_H.py:103-188 case analysis,
+the fragment carrying the two-index density first), the product runs in three GEMM stages
+that never touch an n^3 x n^3 object:
+
+  A  T1[x',y',z,s]  = sum_z'     v[x',y',z'] R3[z,z',s]          (batched over z)
+  B  T2[x,r,y',z]   = sum_x',s   P[x',x,r,s] T1[x',y',z,s]        (x' as K-concatenated segments)
+  C  w[x,y,z]      += a sum_r,y' R2[y,r,y'] T2[x,r,y',z]         (batched over x)
+
+about 2 n^4 N^2 FLOPs per block instead of the 2 n^6 of a stored block.  Blocks of a fragment
+order other than (0, 1, 2) read a permuted copy of v and add into a permuted accumulator.
+
+TrimerHvPlan is the plan as host data (GEMM task records over named flat buffers), so the
+same plan drives the device (XRTrimerHamiltonian, grouped launches of libxrh's GEMM) and can
+be executed by a NumPy interpreter in the tests.  Every GEMM record follows the
+xrh_gemm_task / xrh_gemm_segment contract of include/xrh.h.
+"""
+import numpy as np
+import torch
+
+from .gemm import GroupedGemm
+from .trimer import _case, _phase
+
+IDENTITY = (0, 1, 2)
+PAIRS = ((0, 1), (1, 2), (0, 2))         # the spectator of each pair: 2, 0, 1
+
+
+def pair_sector_layout(chg_a, chg_b, ns_a, ns_b):
+    """Sector layout of XRDimerPlan(layout='sector'): {total charge t: (base, dim)} with
+    base[c_a] the first row of charge block (c_a, t - c_a), rows (i_a, i_b) row-major."""
+    out = {}
+    for ca in chg_a:
+        for cb in chg_b:
+            base, dim = out.get(ca + cb, ({}, 0))
+            base[ca] = dim
+            out[ca + cb] = (base, dim + ns_a[ca] * ns_b[cb])
+    return out
+
+
+def _seg(A, lda, B, ldb, K, alpha=1.0, flags=0, sA=0, sB=0):
+    return dict(A=A, lda=lda, B=B, ldb=ldb, K=K, alpha=float(alpha), flags=flags, sA=sA, sB=sB)
+
+
+def _task(M, N, C, ldc, segs, mode=1, batch=1, sC=0):
+    return dict(M=M, N=N, C=C, ldc=ldc, segs=segs, mode=mode, batch=batch, sC=sC)
+
+
+def _vname(order):
+    return "v" if order == IDENTITY else "v%d%d%d" % order
+
+
+def _wname(order):
+    return "w" if order == IDENTITY else "w%d%d%d" % order
+
+
+class TrimerHvPlan:
+    """GEMM records of one three-fragment H x v (host data only).
+
+    charges:     three charge lists (state order of each fragment: charge blocks in this order)
+    n_states:    three {charge: number of states}
+    n_elec:      three reference electron counts (charge c holds n_elec - c electrons)
+    Ns:          spin orbitals per fragment
+    avail:       avail(f, op, bra_chg, ket_chg) -> True when fragment f has that density block
+    total_charge: None for the whole product space, or one total charge (H conserves it)
+
+    Buffers are named: 'v', 'w' (the vectors), 'vXYZ'/'wXYZ' (permuted copies for fragment
+    order XYZ), 'Pt', 'R2t', 'T1', 'T2' (intermediates, sizes in self.sizes) and external
+    keys ('rho', f, op, bc, kc), ('H1', f, c), ('H2', pair, t), ('W', kind, order),
+    ('Uq', order), ('eye', n).  A reference is (buffer, element offset)."""
+
+    def __init__(self, charges, n_states, n_elec, Ns, avail, total_charge=None):
+        self.charges = [list(c) for c in charges]
+        self.ns = [dict(n) for n in n_states]
+        self.n_elec = list(n_elec)
+        self.Ns = list(Ns)
+        ns, N = self.ns, self.Ns
+        triples = [(a, b, c) for a in self.charges[0] for b in self.charges[1] for c in self.charges[2]]
+        if total_charge is not None:
+            triples = [t for t in triples if sum(t) == total_charge]
+        self.triples = triples
+        self.off, self.shape = {}, {}
+        dim = 0
+        for t in triples:
+            self.off[t] = dim
+            self.shape[t] = tuple(ns[f][t[f]] for f in range(3))
+            dim += int(np.prod(self.shape[t]))
+        self.dim = dim
+        self.sizes = {"v": dim, "w": dim}
+        self.build_tasks, self.permutes = [], []
+        self.launches = [[], [], []]
+        self.orders = set()
+        self.pair_layout = [pair_sector_layout(self.charges[a], self.charges[b], ns[a], ns[b]) for a, b in PAIRS]
+        self._monomers(avail)
+        self._pairs()
+        self._trimers(avail)
+        for o in sorted(self.orders):
+            if o != IDENTITY:
+                self.sizes[_vname(o)] = dim
+                self.sizes[_wname(o)] = dim
+        self.flops_apply = sum(_task_flops(t) for L in self.launches for t in L)
+        self.flops_build = sum(_task_flops(t) for t in self.build_tasks)
+
+    # ---------------------------------------------------------------------------------
+    def _alloc(self, name, n):
+        o = self.sizes.get(name, 0)
+        self.sizes[name] = o + int(n)
+        return o
+
+    def _monomers(self, avail):
+        """H1_f on axis f of every block (build_H.py:38-47); fragment f has a monomer block
+        for charge c when it has the rho^ca block (c, c)."""
+        for t in self.triples:
+            n0, n1, n2 = self.shape[t]
+            o = self.off[t]
+            if avail(0, "ca", t[0], t[0]):
+                self.launches[0].append(_task(n0, n1 * n2, ("w", o), n1 * n2,
+                                              [_seg((("H1", 0, t[0]), 0), n0, ("v", o), n1 * n2, n0, flags=2)]))
+            if avail(1, "ca", t[1], t[1]):
+                self.launches[0].append(_task(n1, n2, ("w", o), n2,
+                                              [_seg((("H1", 1, t[1]), 0), n1, ("v", o), n2, n1, flags=2, sB=n1 * n2)],
+                                              batch=n0, sC=n1 * n2))
+            if avail(2, "ca", t[2], t[2]):
+                self.launches[0].append(_task(n0 * n1, n2, ("w", o), n2,
+                                              [_seg(("v", o), n2, (("H1", 2, t[2]), 0), n2, n2)]))
+
+    def _pairs(self):
+        """(H2_ab x 1_s) v for the three pairs, every source block in one task per output block."""
+        in_layout = set(self.triples)
+        for p, (a, b) in enumerate(PAIRS):
+            s = 3 - a - b
+            lay = self.pair_layout[p]
+            for t in self.triples:
+                tot = t[a] + t[b]
+                base, dimt = lay[tot]
+                segs = []
+                for ca2 in self.charges[a]:
+                    cb2 = tot - ca2
+                    if cb2 not in self.charges[b] or abs(ca2 - t[a]) > 2:
+                        continue
+                    src = [0, 0, 0]
+                    src[a], src[b], src[s] = ca2, cb2, t[s]
+                    src = tuple(src)
+                    if src not in in_layout:
+                        continue
+                    H = (("H2", p, tot), base[t[a]] * dimt + base[ca2])
+                    na2, nb2 = self.ns[a][ca2], self.ns[b][cb2]
+                    if (a, b) == (0, 1):
+                        segs.append(_seg(H, dimt, ("v", self.off[src]), self.ns[2][t[2]], na2 * nb2, flags=2))
+                    elif (a, b) == (1, 2):
+                        segs.append(_seg(("v", self.off[src]), na2 * nb2, H, dimt, na2 * nb2))
+                    else:
+                        # spectator 1: (-1)^(n_1 dq), n_1 its electron-count parity, dq the parity of
+                        # the charge moved between fragments 0 and 2
+                        odd = (self.n_elec[1] - t[1]) % 2 == 1 and (t[0] - ca2) % 2 == 1
+                        self.orders.add((1, 0, 2))
+                        segs.append(_seg(("v102", self.off[src]), na2 * nb2, H, dimt, na2 * nb2,
+                                         alpha=-1.0 if odd else 1.0))
+                if not segs:
+                    continue
+                n0, n1, n2 = self.shape[t]
+                o = self.off[t]
+                if (a, b) == (0, 1):
+                    self.launches[0].append(_task(n0 * n1, n2, ("w", o), n2, segs))
+                elif (a, b) == (1, 2):
+                    self.launches[0].append(_task(n0, n1 * n2, ("w", o), n1 * n2, segs))
+                else:
+                    self.launches[0].append(_task(n1, n0 * n2, ("w102", o), n0 * n2, segs))
+
+    def _trimers(self, avail):
+        """Three-stage products of every trimer charge block (build_H.py:103-188)."""
+        ns, N = self.ns, self.Ns
+        P_off, T1_off, T2_off, R2_off = {}, {}, {}, {}
+        out_tasks = {}
+        self.integral_keys = set()          # (kind, order) of every W matrix the stage-1 tasks read
+        self.n_trimer_blocks = 0
+        for ci in self.triples:
+            for cj in self.triples:
+                case = _case(ci, cj)
+                if case is None:
+                    continue
+                kind, order, ops, _vfr = case
+                x, y, z = order
+                if not all(avail(order[k], ops[k], ci[order[k]], cj[order[k]]) for k in range(3)):
+                    continue
+                self.n_trimer_blocks += 1
+                self.orders.add(order)
+                nx, nxp = ns[x][ci[x]], ns[x][cj[x]]
+                ny, nyp = ns[y][ci[y]], ns[y][cj[y]]
+                nz, nzp = ns[z][ci[z]], ns[z][cj[z]]
+                Ny, Nz = N[y], N[z]
+                Kx = N[x] * N[x]
+                # stage 1 (per build): Pt[x'][x][r][s] = sum_k R1[x,x',k] W[(r,s),k] (+ delta U/4)
+                pkey = (kind, order, ci[x], cj[x])
+                if pkey not in P_off:
+                    self.integral_keys.add((kind, order))
+                    P_off[pkey] = self._alloc("Pt", nxp * nx * Ny * Nz)
+                    segs = [_seg((("rho", x, ops[0], ci[x], cj[x]), 0), Kx, (("W", kind, order), 0), Kx, Kx, sA=nxp * Kx)]
+                    if kind == "tex":
+                        segs.append(_seg((("eye", nx), 0), 1, (("Uq", order), 0), 1, 1, sA=nx))
+                    self.build_tasks.append(_task(nxp, Ny * Nz, ("Pt", P_off[pkey]), nx * Ny * Nz, segs, mode=0,
+                                                  batch=nx, sC=Ny * Nz))
+                # R2 as [y][r][y'] (per build)
+                rkey = (y, ops[1], ci[y], cj[y])
+                if rkey not in R2_off:
+                    R2_off[rkey] = self._alloc("R2t", ny * Ny * nyp)
+                    self.permutes.append(((("rho",) + rkey, 0), (ny, nyp, Ny), (0, 2, 1), ("R2t", R2_off[rkey])))
+                # A: T1[x'][y'][z][s] = sum_z' v[x',y',z'] R3[z,z',s]
+                t1key = (order, cj, z, ops[2], ci[z])
+                if t1key not in T1_off:
+                    T1_off[t1key] = self._alloc("T1", nxp * nyp * nz * Nz)
+                    self.launches[0].append(_task(
+                        nxp * nyp, Nz, ("T1", T1_off[t1key]), nz * Nz,
+                        [_seg((_vname(order), self.off[cj]), nzp, (("rho", z, ops[2], ci[z], cj[z]), 0), Nz, nzp,
+                              flags=2, sB=nzp * Nz)], mode=0, batch=nz, sC=Nz))
+                # B: T2[x][r][y'][z] = sum_x' sum_s Pt[x'][x][r][s] T1[x'][y'][z][s]
+                t2key = (pkey, t1key)
+                if t2key not in T2_off:
+                    T2_off[t2key] = self._alloc("T2", nx * Ny * nyp * nz)
+                    p0, q0 = P_off[pkey], T1_off[t1key]
+                    segs = [_seg(("Pt", p0 + xp * nx * Ny * Nz), Nz, ("T1", q0 + xp * nyp * nz * Nz), Nz, Nz)
+                            for xp in range(nxp)]
+                    self.launches[1].append(_task(nx * Ny, nyp * nz, ("T2", T2_off[t2key]), nyp * nz, segs, mode=0))
+                # C: w[x][y][z] += a sum_(r,y') R2t[y][r][y'] T2[x][r][y'][z]
+                s2 = -1.0 if (self.n_elec[1] - ci[1]) % 2 else 1.0
+                s3 = -1.0 if (self.n_elec[2] - ci[2]) % 2 else 1.0
+                alpha = (4.0 if kind == "tex" else 2.0) * _phase(kind, order, s2, s3)
+                okey = (order, ci)
+                if okey not in out_tasks:
+                    out_tasks[okey] = _task(ny, nz, (_wname(order), self.off[ci]), nz, [], batch=nx, sC=ny * nz)
+                    self.launches[2].append(out_tasks[okey])
+                out_tasks[okey]["segs"].append(_seg(("R2t", R2_off[rkey]), Ny * nyp, ("T2", T2_off[t2key]), nz,
+                                                    Ny * nyp, alpha=alpha, flags=2, sB=Ny * nyp * nz))
+
+    # ---------------------------------------------------------------------------------
+    def permutation(self, order):
+        """Gather index of the copy of v in fragment order `order`: v_order = v[idx]; the
+        permuted accumulator goes back with w[idx] += w_order."""
+        idx = np.empty(self.dim, dtype=np.int64)
+        for t in self.triples:
+            o, sh = self.off[t], self.shape[t]
+            n = int(np.prod(sh))
+            idx[o:o + n] = o + np.arange(n).reshape(sh).transpose(order).ravel()
+        return idx
+
+    def product_index(self):
+        """Position of every vector element in the reference's product order
+        (I0 I1 I2 row-major over the three fragments' charge-blocked state lists)."""
+        offs, tots = [], []
+        for f in range(3):
+            acc, o = 0, {}
+            for c in self.charges[f]:
+                o[c] = acc
+                acc += self.ns[f][c]
+            offs.append(o)
+            tots.append(acc)
+        idx = np.empty(self.dim, dtype=np.int64)
+        for t in self.triples:
+            n0, n1, n2 = self.shape[t]
+            i0, i1, i2 = np.meshgrid(np.arange(n0), np.arange(n1), np.arange(n2), indexing="ij")
+            g = ((offs[0][t[0]] + i0) * tots[1] + offs[1][t[1]] + i1) * tots[2] + offs[2][t[2]] + i2
+            idx[self.off[t]:self.off[t] + n0 * n1 * n2] = g.ravel()
+        return idx, tots[0] * tots[1] * tots[2]
+
+
+def _task_flops(t):
+    return sum(2.0 * t["M"] * t["N"] * s["K"] * t["batch"] for s in t["segs"])
+
+
+def trimer_integral_matrices(V, U, order_kinds, Ns):
+    """W[(kind, order)] = the V block of the case with R1's indices last, (Ny Nz, Nx Nx)
+    (as trimer.XRTrimerPlan), and Uq[order] = U[x,y,z] / 4 for the Ex1min1pls cases;
+    V(m,n,o,p) and U(k,m,n) return torch tensors or NumPy arrays."""
+    W, Uq = {}, {}
+    for kind, order in sorted(order_kinds):
+        x, y, z = order
+        Nx, Ny, Nz = Ns[x], Ns[y], Ns[z]
+        if kind == "t2m":        # V[x,x,y,z] = V[p,q,r,s], R1 indexed (q, p)
+            Vb, ax = V(x, x, y, z), (2, 3, 1, 0)
+        elif kind == "t2p":      # V[y,z,x,x] = V[r,s,p,q], R1 indexed (q, p)
+            Vb, ax = V(y, z, x, x), (0, 1, 3, 2)
+        else:                    # V[x,y,x,z] = V[p,r,q,s], R1 indexed (p, q)
+            Vb, ax = V(x, y, x, z), (1, 3, 0, 2)
+        Wt = Vb.permute(*ax) if hasattr(Vb, "permute") else Vb.transpose(ax)
+        W[(kind, order)] = Wt.reshape(Ny * Nz, Nx * Nx)
+        if kind == "tex":
+            Uq[order] = 0.25 * U(x, y, z).reshape(Ny * Nz, 1)
+    return W, Uq
+
+
+class _PairIntegrals:
+    """The integral accessors of fragments (a, b) of a larger system, numbered (0, 1)."""
+
+    def __init__(self, ints, frags):
+        self.ints, self.f = ints, tuple(frags)
+
+    def T(self, m, n):
+        return self.ints.T(self.f[m], self.f[n])
+
+    def U(self, k, m, n):
+        return self.ints.U(self.f[k], self.f[m], self.f[n])
+
+    def V(self, m, n, o, p):
+        return self.ints.V(self.f[m], self.f[n], self.f[o], self.f[p])
+
+
+class XRTrimerHamiltonian:
+    """w = H v for the order-0 general-XRCC Hamiltonian of three fragments on the device.
+
+    spaces:       three FragmentSpace objects;  n_states: three {charge: n};  charges: three lists
+    ints:         DeviceIntegrals over the three fragments (T, U, V block accessors)
+    precision:    arithmetic of the pair builds (XRDimerPlan: 'fp64', 'bf16x3', 'tf32x3')
+    hv_precision: arithmetic of the H x v GEMMs: 'fp64', or 'fp32' (FP32 products, FP64 sums)
+    total_charge: restrict the vector to one total charge (None: the whole product space)
+
+    build(coeffs) runs the three pair builds (densities, monomer and dimer blocks) and the
+    per-build trimer stage; apply(x) then returns H x as a device vector in block layout
+    (product_index() maps it to the reference's product order).  Nothing is
+    allocated after construction: every launch reads persistent buffers through task tables
+    uploaded once, so a build or a product can be captured in a CUDA graph."""
+
+    def __init__(self, spaces, n_states, charges, ints, precision="fp64", hv_precision="fp64", total_charge=None,
+                 autotune=True):
+        from .hamiltonian import XRDimerPlan
+        dev = spaces[0].device
+        self.device = dev
+        self.charges = [list(c) for c in charges]
+        self.n_states = [dict(n) for n in n_states]
+        self.plans = [XRDimerPlan([spaces[a], spaces[b]], [self.n_states[a], self.n_states[b]],
+                                  [self.charges[a], self.charges[b]], _PairIntegrals(ints, (a, b)), output="split",
+                                  precision=precision, convention="general", layout="sector", autotune=autotune)
+                      for a, b in PAIRS]
+        # each fragment's densities and monomer blocks from one pair plan that holds it
+        holder = {0: (0, 0), 1: (0, 1), 2: (1, 1)}
+        self.rho = [self.plans[p].builders[k].rho for p, k in (holder[f] for f in range(3))]
+        self.H1blk = [self.plans[p].H1blk[k] for p, k in (holder[f] for f in range(3))]
+
+        def avail(f, op, bc, kc):
+            return (bc, kc) in self.rho[f].get(op, {})
+
+        plan = TrimerHvPlan(self.charges, self.n_states, [sp.n_elec_ref for sp in spaces], [sp.N for sp in spaces],
+                            avail, total_charge)
+        self.plan = plan
+        for p, lay in enumerate(plan.pair_layout):
+            for t, (base, dimt) in lay.items():
+                sec = self.plans[p].sectors[t]
+                assert sec["dim"] == dimt and sec["base"] == base, "pair sector layout mismatch"
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.bufs = {k: torch.zeros(max(int(n), 1), **f64) for k, n in plan.sizes.items()}
+        W, Uq = trimer_integral_matrices(ints.V, ints.U, plan.integral_keys, plan.Ns)
+        self.W = {k: w.contiguous().reshape(-1) for k, w in W.items()}
+        self.Uq = {k: u.contiguous().reshape(-1) for k, u in Uq.items()}
+        self.eyes = {}
+        self._perm_idx = {o: torch.as_tensor(plan.permutation(o), device=dev)
+                          for o in sorted(plan.orders) if o != IDENTITY}
+        self._permutes = [(self._resolve(src), shape, ax, self._resolve(dst)) for src, shape, ax, dst in plan.permutes]
+        self.stage1 = self._grouped(plan.build_tasks, hv_precision)
+        self.stages = [self._grouped(L, hv_precision) for L in plan.launches]
+        self.flops_apply = plan.flops_apply
+        self.dim = plan.dim
+
+    # ---------------------------------------------------------------------------------
+    def _ext(self, key):
+        kind = key[0]
+        if kind == "rho":
+            _, f, op, bc, kc = key
+            return self.rho[f][op][(bc, kc)].reshape(-1)
+        if kind == "H1":
+            return self.H1blk[key[1]][key[2]].reshape(-1)
+        if kind == "H2":
+            return self.plans[key[1]].sectors[key[2]]["H"].reshape(-1)
+        if kind == "W":
+            return self.W[(key[1], key[2])]
+        if kind == "Uq":
+            return self.Uq[key[1]]
+        if kind == "eye":
+            n = key[1]
+            if n not in self.eyes:
+                self.eyes[n] = torch.eye(n, dtype=torch.float64, device=self.device).reshape(-1)
+            return self.eyes[n]
+        return self.bufs[key]
+
+    def _resolve(self, ref):
+        buf, off = ref
+        t = self._ext(buf)
+        return t[off:]
+
+    def _grouped(self, tasks, precision):
+        g = GroupedGemm(self.device, precision=precision)
+        for t in tasks:
+            segs = []
+            for s in t["segs"]:
+                segs.append((self._resolve(s["A"]), s["lda"], self._resolve(s["B"]), s["ldb"], s["K"], s["alpha"],
+                             s["flags"], s["sA"], s["sB"]))
+            g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], batch=t["batch"], sC=t["sC"])
+        return g.finalize()
+
+    # ---------------------------------------------------------------------------------
+    def set_coeffs(self, coeffs):
+        """coeffs: three {charge: CUDA float64 (n_states, n_conf)} dicts."""
+        for p, (a, b) in enumerate(PAIRS):
+            self.plans[p].set_coeffs([coeffs[a], coeffs[b]])
+
+    def build(self, coeffs=None):
+        """Enqueue the pair builds and the per-build trimer stage (no host synchronisation)."""
+        if coeffs is not None:
+            self.set_coeffs(coeffs)
+        for pl in self.plans:
+            pl.launch()
+        for src, shape, ax, dst in self._permutes:
+            n = int(np.prod(shape))
+            dst[:n].view(shape[ax[0]], shape[ax[1]], shape[ax[2]]).copy_(src[:n].view(shape).permute(*ax))
+        self.stage1.run()
+
+    def apply(self, x, out=None):
+        """out = H x (device vectors of length self.dim, block layout); returns out."""
+        v, w = self.bufs["v"], self.bufs["w"]
+        if x.data_ptr() != v.data_ptr():
+            v.copy_(x)
+        w.zero_()
+        for o, idx in self._perm_idx.items():
+            self.bufs[_wname(o)].zero_()
+            torch.index_select(v, 0, idx, out=self.bufs[_vname(o)])
+        for st in self.stages:
+            st.run()
+        for o, idx in self._perm_idx.items():
+            w.index_add_(0, idx, self.bufs[_wname(o)])
+        if out is not None and out.data_ptr() != w.data_ptr():
+            out.copy_(w)
+            return out
+        return w
+
+    def product_index(self):
+        """(device int64 index, product-space dimension): element e of a block-layout vector is
+        element idx[e] of the vector in the reference's product order."""
+        idx, dim = self.plan.product_index()
+        return torch.as_tensor(idx, device=self.device), dim
+
+    def lowest(self, k=1, m=60, seed=7):
+        """Lowest k eigenvalues (FP64 Lanczos on the matrix-free product) and the residual
+        estimate of the lowest; the ground-state vector is self.lanczos.ground_vector()."""
+        from .eigen import Lanczos
+        if getattr(self, "lanczos", None) is None or self.lanczos.m != min(m, self.dim):
+            self.lanczos = Lanczos(self.dim, m=m, device=self.device, seed=seed, mode="steps")
+        lz = self.lanczos
+        lz.krylov_operator(lambda x, y: self.apply(x, y))
+        lz.stage_to_host()
+        torch.cuda.current_stream().synchronize()
+        return lz.solve(k)
+
