@@ -430,12 +430,12 @@ def run_trimer(args):
     host = [{q: torch.as_tensor(sysd["states"][m][q][0]).pin_memory() for q in charges} for m in range(3)]
     dev = [{q: t.to("cuda") for q, t in d.items()} for d in host]
     lanczos_m = 30
-    forms = {"fp64": ("fp64", "fp64"), "split": ("tf32x3", "fp32")}
-    want = ["fp64", "split"] if args.precision in ("fp64", "tf32x3") and not args.no_variants else \
-        ["fp64" if args.precision == "fp64" else "split"]
-    head = "fp64" if args.precision == "fp64" else "split"
+    forms = {"fp64": ("fp64", "fp64"), "fp32": ("tf32x3", "fp32"), "tf32x3": ("tf32x3", "tf32x3"),
+             "bf16x3": ("bf16x3", "bf16x3")}
+    head = args.precision if args.precision in forms else "tf32x3"
+    want = [head] if args.no_variants else [head] + [f for f in ("fp64", "fp32", "tf32x3") if f != head]
     out = {}
-    for form in [head] + [f for f in want if f != head]:
+    for form in want:
         prec, hvp = forms[form]
         ham = XRTrimerHamiltonian(spaces, ns, [charges] * 3, ints, precision=prec, hv_precision=hvp, total_charge=0)
         ham.set_coeffs(dev)
@@ -453,6 +453,7 @@ def run_trimer(args):
         ms, Es = [], []
         clock_path = os.path.join(tempfile.gettempdir(), f"xrh_clocks_t_{os.getpid()}.csv")
         with ClockSampler(clock_path) as cs:
+            torch.cuda.nvtx.range_push("xrh_timed")
             for _ in range(n_steps):
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record()
@@ -460,6 +461,7 @@ def run_trimer(args):
                 e1.record()
                 torch.cuda.synchronize()
                 ms.append(e0.elapsed_time(e1))
+            torch.cuda.nvtx.range_pop()
         rec = {"s_per_iter": sum(ms) / 1e3 / n_steps, "E0": Es[-1][0], "resid": Es[-1][1],
                "gpu_launches": _lib.LaunchCounter.count, "clocks": cs.summary(int(os.environ.get("LOCAL_RANK", "0")))}
         # dominant kernel: stage B of H x v (x' segments, 2 n^4 N^2 FLOPs per trimer block)
@@ -495,25 +497,38 @@ def run_trimer(args):
         del ham
         torch.cuda.empty_cache()
     r = out[head]
+    peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0)) if head in ("tf32x3", "bf16x3") else None
     line = {
         "metric": "XR-H trimer build + matrix-free Lanczos ground state s/iter", "value": r["s_per_iter"],
         "unit": "s/iter", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": r["s_per_iter"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if head == "fp64" else "tf32x3 pair builds, fp32-product H x v",
+        "dtype": {"fp64": "f64", "fp32": "tf32x3 pair builds, fp32-product H x v"}.get(
+            head, f"{head} (pair builds and the dominant H x v stage on tcgen05)"),
         "data": "synthetic (seeded h ~ N(0,0.1), V = sum_K L L with K=40, Sz-definite QR-orthonormal Gaussian CI vectors)",
         "config": {"workload": c["name"], "lanczos_steps": lanczos_m,
                    "l2": "inputs larger than L2 (pair sector matrices and intermediates of several GB)",
                    "step": "three pair builds + trimer stage 1 + 30 Lanczos steps of H x v (FP64 Lanczos)"},
         "e2e": {"value": r["e2e"], "unit": "s/iter", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": 8},
         "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "E0": r["E0"], "resid": r["resid"],
-        "roofline": {"bound": "fp64 pipe" if head == "fp64" else "fp32 pipe", "kernel": "gemm_fp64_kernel (H x v stage B)",
+        "roofline": {"bound": {"fp64": "fp64 pipe", "fp32": "fp32 pipe"}.get(head, "tensor"),
+                     "kernel": "H x v stage B (" + ("gemm_tc_kernel" if head in ("tf32x3", "bf16x3") else "gemm_fp64_kernel") + ")",
                      "achieved": r["stageB_tflops"], "unit": "TFLOP/s", "launch_ms": r["stageB_ms"],
-                     "peak": None, "frac": None, "traffic": None},
+                     "peak": peak, "frac": (r["stageB_tflops"] / peak) if peak else None, "traffic": None,
+                     "note": "achieved = algorithmic FLOPs (2 n^4 N^2 per trimer block) / CUDA-event time of the "
+                             "launch; tensor forms issue 3 MMAs per algorithmic FLOP and TF32 runs at half the BF16 "
+                             "rate, peak = MEASURED_PEAKS.json bf16_tflops (of measured); no FP64/FP32 peak is "
+                             "measured, so the SIMT forms carry none"},
         "variants": out,
     }
-    if "fp64" in out and "split" in out:
-        line["dE0_split_vs_fp64"] = abs(out["split"]["E0"] - out["fp64"]["E0"])
-        line["speedup_split_vs_fp64"] = out["fp64"]["s_per_iter"] / out["split"]["s_per_iter"]
+    if "fp64" in out:
+        for f, rec in out.items():
+            if f != "fp64":
+                rec["dE0_vs_fp64"] = abs(rec["E0"] - out["fp64"]["E0"])
+                rec["speedup_vs_fp64"] = out["fp64"]["s_per_iter"] / rec["s_per_iter"]
+        if head != "fp64":
+            line["speedup_vs_fp64_gpu"] = out[head]["speedup_vs_fp64"]
     print(json.dumps(line))
 
 

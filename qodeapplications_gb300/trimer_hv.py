@@ -327,7 +327,9 @@ class XRTrimerHamiltonian:
     spaces:       three FragmentSpace objects;  n_states: three {charge: n};  charges: three lists
     ints:         DeviceIntegrals over the three fragments (T, U, V block accessors)
     precision:    arithmetic of the pair builds (XRDimerPlan: 'fp64', 'bf16x3', 'tf32x3')
-    hv_precision: arithmetic of the H x v GEMMs: 'fp64', or 'fp32' (FP32 products, FP64 sums)
+    hv_precision: arithmetic of the H x v GEMMs: 'fp64'; 'fp32' (FP32 products, FP64 sums); or
+                  'tf32x3' / 'bf16x3' (the dominant stage on the tensor cores in split precision,
+                  the rest with FP32 products and FP64 sums)
     total_charge: restrict the vector to one total charge (None: the whole product space)
 
     build(coeffs) runs the three pair builds (densities, monomer and dimer blocks) and the
@@ -371,8 +373,27 @@ class XRTrimerHamiltonian:
         self._perm_idx = {o: torch.as_tensor(plan.permutation(o), device=dev)
                           for o in sorted(plan.orders) if o != IDENTITY}
         self._permutes = [(self._resolve(src), shape, ax, self._resolve(dst)) for src, shape, ax, dst in plan.permutes]
-        self.stage1 = self._grouped(plan.build_tasks, hv_precision)
-        self.stages = [self._grouped(L, hv_precision) for L in plan.launches]
+        # stage B (2 n^4 N^2 FLOPs per trimer block, nearly all of a product) on the tensor cores
+        # for the split forms: Pt slices split once per build, T1 slices once per product; the
+        # small stages and the pair terms then run with FP32 products and FP64 sums
+        self.tc = hv_precision in ("bf16x3", "tf32x3")
+        simt = "fp32" if self.tc else hv_precision
+        self.stage1 = self._grouped(plan.build_tasks, simt)
+        self.stages = [self._grouped(L, simt) for L in plan.launches]
+        if self.tc:
+            from .gemm import SplitRegistry, TCGroupedGemm
+            self.reg = SplitRegistry(hv_precision, dev)
+            tcg = TCGroupedGemm(self.reg)
+            for t in plan.launches[1]:
+                assert t["batch"] == 1 and all(sg["flags"] == 0 for sg in t["segs"])
+                segs = [(self._resolve(sg["A"]), sg["lda"], self._resolve(sg["B"]), sg["ldb"], sg["K"], sg["alpha"])
+                        for sg in t["segs"]]
+                tcg.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"],
+                        groups=[("Pt", "T1")] * len(segs))
+            self.reg.upload()
+            self.stages[1] = tcg.finalize()
+            if autotune:
+                self.stages[1].autotune()
         self.flops_apply = plan.flops_apply
         self.dim = plan.dim
 
@@ -428,6 +449,8 @@ class XRTrimerHamiltonian:
             n = int(np.prod(shape))
             dst[:n].view(shape[ax[0]], shape[ax[1]], shape[ax[2]]).copy_(src[:n].view(shape).permute(*ax))
         self.stage1.run()
+        if self.tc:
+            self.reg.split("Pt")
 
     def apply(self, x, out=None):
         """out = H x (device vectors of length self.dim, block layout); returns out."""
@@ -438,14 +461,24 @@ class XRTrimerHamiltonian:
         for o, idx in self._perm_idx.items():
             self.bufs[_wname(o)].zero_()
             torch.index_select(v, 0, idx, out=self.bufs[_vname(o)])
-        for st in self.stages:
-            st.run()
+        self.stages[0].run()
+        if self.tc:
+            self.reg.split("T1")
+        self.stages[1].run()
+        self.stages[2].run()
         for o, idx in self._perm_idx.items():
             w.index_add_(0, idx, self.bufs[_wname(o)])
         if out is not None and out.data_ptr() != w.data_ptr():
             out.copy_(w)
             return out
         return w
+
+    def check_status(self):
+        """Raise if a bounded device wait of a tensor-core launch timed out (syncs)."""
+        for pl in self.plans:
+            pl.check_status()
+        if self.tc:
+            self.stages[1].check()
 
     def product_index(self):
         """(device int64 index, product-space dimension): element e of a block-layout vector is

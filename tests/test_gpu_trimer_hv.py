@@ -2,7 +2,8 @@
 oracle's dense order-0 general-XRCC Hamiltonian of three fragments (general_xr_H_full:
 build_H.py:38-188 restated and pinned by test_oracle.py to the compiled reference kernels and
 to the three-fragment FCI identity).  Tolerances: FP64 1e-12 relative to the largest element
-of the product; FP32 products (FP64 sums) and 3xTF32 pair builds 1e-6 relative; Lanczos
+of the product; FP32 products (FP64 sums), 3xTF32 pair builds and the 3xTF32 tensor-core
+stage 1e-6 relative; Lanczos
 ground state within 1e-9 Eh (plus its residual estimate) of the FCI ground state."""
 import numpy as np
 import pytest
@@ -108,10 +109,13 @@ def test_trimer_hv_lanczos_is_fci_ground_state():
     assert abs(w[0] - E_fci) <= 1e-9 + resid, (w[0], E_fci, resid)
 
 
-@pytest.mark.parametrize("precision,hv_precision", [("fp64", "fp32"), ("tf32x3", "fp64")])
+@pytest.mark.parametrize("precision,hv_precision", [("fp64", "fp32"), ("tf32x3", "fp64"), ("fp64", "tf32x3"),
+                                                    ("tf32x3", "tf32x3")])
 def test_trimer_hv_reduced_precision_close(precision, hv_precision):
     system = _random_system(seed=31, n_orb=3, n_states=3)
-    _check_products(_device(system, 0, precision, hv_precision), _oracle(system), 1e-6)
+    ham = _device(system, 0, precision, hv_precision)
+    _check_products(ham, _oracle(system), 1e-6)
+    ham.check_status()
 
 
 def test_trimer_hv_rebuild_tracks_new_states():
