@@ -266,6 +266,17 @@ int xrh_gemv_rows(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, 
 int xrh_gemv_cols(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* c_dev,
                   double scale, double* y_dev, void* stream);
 int xrh_lanczos_normalize(int64_t n, const double* w_dev, double* v_dev, double* beta_dev, void* stream);
+/* The same products for few rows over long vectors (the matrix-free Lanczos of a product space,
+ * n ~ 10^5..10^6; replaces the same dense eigensolve as above): the columns are split over CTAs
+ * of 2048 columns, each writing one partial per row into work_dev, and a second launch adds the
+ * partials of a row in CTA order (deterministic).  work_len >= xrh_gemv_split_work(rows, cols)
+ * doubles for xrh_gemv_rows_split and >= xrh_gemv_split_work(1, n) for
+ * xrh_lanczos_normalize_split; XRH_ERR_CAPACITY when smaller. */
+int64_t xrh_gemv_split_work(int64_t rows, int64_t cols);
+int xrh_gemv_rows_split(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* x_dev,
+                        double alpha, double beta, double* y_dev, double* work_dev, int64_t work_len, void* stream);
+int xrh_lanczos_normalize_split(int64_t n, const double* w_dev, double* v_dev, double* beta_dev, double* work_dev,
+                                int64_t work_len, void* stream);
 /* xrh_gemv_rows for a table of GEMVs in one launch: task t computes rows [0, rows) of
  * y = alpha A x + beta y and owns the launch's rows [row_begin, row_begin + round_up(rows, 8));
  * tasks sorted by row_begin, total_rows8 = the sum of the rounded row counts.  With beta == 1

@@ -69,6 +69,9 @@ _SIGS = {
     "xrh_gemm_simt_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp, _vp]),
     "xrh_gemv_rows": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _dbl, _vp, _vp]),
     "xrh_gemv_cols": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _vp, _vp]),
+    "xrh_gemv_split_work": (_i64, [_i64, _i64]),
+    "xrh_gemv_rows_split": (_i32, [_i64, _i64, _vp, _i64, _vp, _dbl, _dbl, _vp, _vp, _i64, _vp]),
+    "xrh_lanczos_normalize_split": (_i32, [_i64, _vp, _vp, _vp, _vp, _i64, _vp]),
     "xrh_lanczos_normalize": (_i32, [_i64, _vp, _vp, _vp, _vp]),
     "xrh_density_adjoint": (_i32, [_i32, _i64, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp]),
     "xrh_ccaa_weighted": (_i32, [_i32, _i32, _vp, _i32, _vp, _vp, _i32, _vp, _i64, _vp, _vp, _vp, _i32, _vp, _vp]),
@@ -114,10 +117,10 @@ class LaunchCounter:
     """Counts library calls that launch a kernel (the gpu_launches figure): every entry point
     except the host-only ones below launches one kernel of this library (those in `multi` the
     number given)."""
-    multi = {"xrh_orbital_terms": 2}
+    multi = {"xrh_orbital_terms": 2, "xrh_gemv_rows_split": 2, "xrh_lanczos_normalize_split": 2}
     host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems",
                  "xrh_tc_encode_map", "xrh_state_ctas", "xrh_abt_ctas", "xrh_lanczos_coop_work",
-                 "xrh_lanczos_cluster_fits"}
+                 "xrh_lanczos_cluster_fits", "xrh_gemv_split_work"}
     count = 0
 
 

@@ -7,6 +7,8 @@
 //   xrh_gemv_cols:  y[j] += sum_i c[i] * scale * A[i*lda + j]              (thread per column)
 //   xrh_lanczos_normalize: beta[k] = ||w||, v = w / beta[k]  (one CTA; the norm stays on the
 //       device so the whole Krylov loop can be replayed as one CUDA graph)
+//   xrh_gemv_rows_split / xrh_lanczos_normalize_split: the same for long vectors, columns split
+//       over CTAs with partials added in a fixed order by a second launch
 // All FP64: the eigensolve is kept in double precision on every precision path.
 #include <cooperative_groups.h>
 
@@ -36,6 +38,89 @@ __global__ void __launch_bounds__(256) gemv_cols_kernel(int64_t rows, int64_t co
     double s = 0.0;
     for (int64_t i = 0; i < rows; ++i) s = fma(c[i], A[i * lda + j], s);
     y[j] += scale * s;
+}
+
+// Column-split forms for few rows over long vectors (the matrix-free Lanczos of a product space
+// of 10^5..10^6 states, where a warp per row leaves most SMs idle).  A CTA takes SPLIT_COLS
+// columns: pass 1 writes one partial per (CTA, row), pass 2 sums the partials of a row in CTA
+// order, so results do not depend on scheduling.
+constexpr int SPLIT_COLS = 2048;
+
+__global__ void __launch_bounds__(256) gemv_rows_partial_kernel(int64_t rows, int64_t cols,
+                                                              const double* __restrict__ A, int64_t lda,
+                                                              const double* __restrict__ x,
+                                                              double* __restrict__ partial) {
+    __shared__ double xs[SPLIT_COLS];
+    const int64_t c0 = (int64_t)blockIdx.x * SPLIT_COLS;
+    const int cn = (int)min((int64_t)SPLIT_COLS, cols - c0);
+    for (int j = threadIdx.x; j < cn; j += blockDim.x) xs[j] = x[c0 + j];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t r = warp; r < rows; r += (blockDim.x >> 5)) {
+        const double* a = A + r * lda + c0;
+        double s0 = 0.0, s1 = 0.0;
+        int j = lane;
+        for (; j + 32 < cn; j += 64) {
+            s0 = fma(a[j], xs[j], s0);
+            s1 = fma(a[j + 32], xs[j + 32], s1);
+        }
+        if (j < cn) s0 = fma(a[j], xs[j], s0);
+        double s = s0 + s1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) partial[(int64_t)blockIdx.x * rows + r] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) gemv_rows_reduce_kernel(int64_t rows, int64_t n_parts,
+                                                             const double* __restrict__ partial, double alpha,
+                                                             double beta, double* __restrict__ y) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    double s = 0.0;
+    for (int64_t b = 0; b < n_parts; ++b) s += partial[b * rows + r];
+    y[r] = alpha * s + (beta == 0.0 ? 0.0 : beta * y[r]);
+}
+
+__global__ void __launch_bounds__(256) sumsq_partial_kernel(int64_t n, const double* __restrict__ w,
+                                                          double* __restrict__ partial) {
+    __shared__ double red[8];
+    const int64_t c0 = (int64_t)blockIdx.x * SPLIT_COLS;
+    const int cn = (int)min((int64_t)SPLIT_COLS, n - c0);
+    double s = 0.0;
+    for (int j = threadIdx.x; j < cn; j += blockDim.x) s = fma(w[c0 + j], w[c0 + j], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+        partial[blockIdx.x] = t;
+    }
+}
+
+// Every CTA sums the partials in the same order (lane-strided, then a fixed shuffle tree), so
+// all CTAs scale by the same beta; CTA 0 stores it.
+__global__ void __launch_bounds__(256) scale_by_norm_kernel(int64_t n, int64_t n_parts,
+                                                          const double* __restrict__ partial,
+                                                          const double* __restrict__ w, double* __restrict__ v,
+                                                          double* __restrict__ beta_out) {
+    __shared__ double bsh;
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int64_t b = threadIdx.x; b < n_parts; b += 32) s += partial[b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) bsh = sqrt(s);
+    }
+    __syncthreads();
+    const double b = bsh;
+    const double inv = b > 0.0 ? 1.0 / b : 0.0;
+    const int64_t c0 = (int64_t)blockIdx.x * SPLIT_COLS;
+    const int cn = (int)min((int64_t)SPLIT_COLS, n - c0);
+    for (int j = threadIdx.x; j < cn; j += blockDim.x) v[c0 + j] = w[c0 + j] * inv;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *beta_out = b;
 }
 
 __global__ void __launch_bounds__(1024) normalize_kernel(int64_t n, const double* __restrict__ w, double* __restrict__ v,
@@ -514,6 +599,44 @@ extern "C" int xrh_gemv_cols(int64_t rows, int64_t cols, const double* A_dev, in
     if (!A_dev || !c_dev || !y_dev) return XRH_ERR_ARG;
     gemv_cols_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, (cudaStream_t)stream>>>(rows, cols, A_dev, lda, c_dev,
                                                                                       scale, y_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int64_t xrh_gemv_split_work(int64_t rows, int64_t cols) {
+    if (rows < 0 || cols < 0) return -1;
+    return ((cols + SPLIT_COLS - 1) / SPLIT_COLS) * (rows > 1 ? rows : 1);
+}
+
+extern "C" int xrh_gemv_rows_split(int64_t rows, int64_t cols, const double* A_dev, int64_t lda, const double* x_dev,
+                                   double alpha, double beta, double* y_dev, double* work_dev, int64_t work_len,
+                                   void* stream) {
+    if (rows < 0 || cols < 0 || lda < cols) return XRH_ERR_ARG;
+    if (rows == 0) return XRH_OK;
+    if (!A_dev || !x_dev || !y_dev || !work_dev) return XRH_ERR_ARG;
+    const int64_t parts = (cols + SPLIT_COLS - 1) / SPLIT_COLS;
+    if (parts > 0x7fffffffLL || (rows + 255) / 256 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    if (work_len < parts * rows) return XRH_ERR_CAPACITY;
+    if (parts > 0) {
+        gemv_rows_partial_kernel<<<(unsigned)parts, 256, 0, (cudaStream_t)stream>>>(rows, cols, A_dev, lda, x_dev,
+                                                                                   work_dev);
+        XRH_CHECK_LAUNCH();
+    }
+    gemv_rows_reduce_kernel<<<(unsigned)((rows + 255) / 256), 256, 0, (cudaStream_t)stream>>>(rows, parts, work_dev,
+                                                                                             alpha, beta, y_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_lanczos_normalize_split(int64_t n, const double* w_dev, double* v_dev, double* beta_dev,
+                                           double* work_dev, int64_t work_len, void* stream) {
+    if (n <= 0 || !w_dev || !v_dev || !beta_dev || !work_dev) return XRH_ERR_ARG;
+    const int64_t parts = (n + SPLIT_COLS - 1) / SPLIT_COLS;
+    if (parts > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    if (work_len < parts) return XRH_ERR_CAPACITY;
+    sumsq_partial_kernel<<<(unsigned)parts, 256, 0, (cudaStream_t)stream>>>(n, w_dev, work_dev);
+    XRH_CHECK_LAUNCH();
+    scale_by_norm_kernel<<<(unsigned)parts, 256, 0, (cudaStream_t)stream>>>(n, parts, work_dev, w_dev, v_dev, beta_dev);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }

@@ -93,15 +93,21 @@ class Lanczos:
         y = H x for device vectors of length n, enqueued on the current stream."""
         if self.small:
             raise ValueError("krylov_operator needs mode='steps'")
+        from ._lib import lib
         s = stream_ptr()
         n, m = self.n, self.m
+        if getattr(self, "_split_work", None) is None:
+            self._split_work = torch.zeros(int(lib().xrh_gemv_split_work(m + 1, n)), dtype=torch.float64,
+                                           device=self.V.device)
+        wk, nwk = self._split_work, self._split_work.numel()
         self.V[0].copy_(self.v0)
         for j in range(m):
             apply(self.V[j], self.w)
             for C in (self.CC, self.CC2):
-                call("xrh_gemv_rows", j + 1, n, ptr(self.V), n, ptr(self.w), 1.0, 0.0, ptr(C[j]), s)
+                call("xrh_gemv_rows_split", j + 1, n, ptr(self.V), n, ptr(self.w), 1.0, 0.0, ptr(C[j]), ptr(wk), nwk, s)
                 call("xrh_gemv_cols", j + 1, n, ptr(self.V), n, ptr(C[j]), -1.0, ptr(self.w), s)
-            call("xrh_lanczos_normalize", n, ptr(self.w), ptr(self.V[j + 1]), ptr(self.beta[j:j + 1]), s)
+            call("xrh_lanczos_normalize_split", n, ptr(self.w), ptr(self.V[j + 1]), ptr(self.beta[j:j + 1]),
+                 ptr(wk), nwk, s)
 
     def stage_to_host(self):
         """Queue the copy of the tridiagonal coefficients (alpha_j, beta_j) to pinned memory."""

@@ -163,7 +163,9 @@ class TrimerHvPlan:
                     H = (("H2", p, tot), base[t[a]] * dimt + base[ca2])
                     na2, nb2 = self.ns[a][ca2], self.ns[b][cb2]
                     if (a, b) == (0, 1):
-                        segs.append(_seg(H, dimt, ("v", self.off[src]), self.ns[2][t[2]], na2 * nb2, flags=2))
+                        # v in fragment order (2, 0, 1): the block is [i2][(j0 j1)], K-contiguous
+                        self.orders.add((2, 0, 1))
+                        segs.append(_seg(H, dimt, ("v201", self.off[src]), na2 * nb2, na2 * nb2))
                     elif (a, b) == (1, 2):
                         segs.append(_seg(("v", self.off[src]), na2 * nb2, H, dimt, na2 * nb2))
                     else:
@@ -178,11 +180,13 @@ class TrimerHvPlan:
                 n0, n1, n2 = self.shape[t]
                 o = self.off[t]
                 if (a, b) == (0, 1):
-                    self.launches[0].append(_task(n0 * n1, n2, ("w", o), n2, segs))
+                    task = _task(n0 * n1, n2, ("w", o), n2, segs)
                 elif (a, b) == (1, 2):
-                    self.launches[0].append(_task(n0, n1 * n2, ("w", o), n1 * n2, segs))
+                    task = _task(n0, n1 * n2, ("w", o), n1 * n2, segs)
                 else:
-                    self.launches[0].append(_task(n1, n0 * n2, ("w102", o), n0 * n2, segs))
+                    task = _task(n1, n0 * n2, ("w102", o), n0 * n2, segs)
+                task["role"] = "pair"
+                self.launches[0].append(task)
 
     def _trimers(self, avail):
         """Three-stage products of every trimer charge block (build_H.py:103-188)."""
@@ -379,9 +383,27 @@ class XRTrimerHamiltonian:
         self.tc = hv_precision in ("bf16x3", "tf32x3")
         simt = "fp32" if self.tc else hv_precision
         self.stage1 = self._grouped(plan.build_tasks, simt)
-        self.stages = [self._grouped(L, simt) for L in plan.launches]
+        pair_tasks = [t for t in plan.launches[0] if t.get("role") == "pair"] if self.tc else []
+        self.stages = [self._grouped([t for t in L if not (self.tc and t.get("role") == "pair")], simt)
+                       for L in plan.launches]
+        self.pairs_tc = None
         if self.tc:
             from .gemm import SplitRegistry, TCGroupedGemm
+            # pair terms: H2 sub-blocks split once per build, the vector blocks once per product
+            self.reg_pairs = SplitRegistry(hv_precision, dev)
+            tcp = TCGroupedGemm(self.reg_pairs)
+            for t in pair_tasks:
+                assert t["batch"] == 1 and all(sg["flags"] == 0 for sg in t["segs"])
+                segs, groups = [], []
+                for sg in t["segs"]:
+                    segs.append((self._resolve(sg["A"]), sg["lda"], self._resolve(sg["B"]), sg["ldb"], sg["K"],
+                                 sg["alpha"]))
+                    groups.append(tuple("H2" if isinstance(r[0], tuple) else "vec" for r in (sg["A"], sg["B"])))
+                tcp.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=1, groups=groups)
+            self.reg_pairs.upload()
+            self.pairs_tc = tcp.finalize()
+            if autotune:
+                self.pairs_tc.autotune()
             self.reg = SplitRegistry(hv_precision, dev)
             tcg = TCGroupedGemm(self.reg)
             for t in plan.launches[1]:
@@ -451,6 +473,7 @@ class XRTrimerHamiltonian:
         self.stage1.run()
         if self.tc:
             self.reg.split("Pt")
+            self.reg_pairs.split("H2")
 
     def apply(self, x, out=None):
         """out = H x (device vectors of length self.dim, block layout); returns out."""
@@ -463,6 +486,8 @@ class XRTrimerHamiltonian:
             torch.index_select(v, 0, idx, out=self.bufs[_vname(o)])
         self.stages[0].run()
         if self.tc:
+            self.reg_pairs.split("vec")
+            self.pairs_tc.run()
             self.reg.split("T1")
         self.stages[1].run()
         self.stages[2].run()
@@ -479,6 +504,7 @@ class XRTrimerHamiltonian:
             pl.check_status()
         if self.tc:
             self.stages[1].check()
+            self.pairs_tc.check()
 
     def product_index(self):
         """(device int64 index, product-space dimension): element e of a block-layout vector is

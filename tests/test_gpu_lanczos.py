@@ -101,3 +101,57 @@ def test_lanczos_cluster_sizes_agree(ctas):
         torch.cuda.synchronize()
         out[mode] = lz._host[:48].numpy().copy()
     assert np.abs(out["cluster"] - out["steps"]).max() <= 1e-11 * np.abs(out["steps"]).max()
+
+
+@pytest.mark.parametrize("n", [1, 2047, 2048, 100_003])
+def test_split_gemv_and_normalize(n):
+    """Column-split products for few rows over long vectors against FP64 PyTorch (1e-13)."""
+    from qodeapplications_gb300 import _lib
+    L = _lib.lib()
+    g = torch.Generator().manual_seed(n)
+    rows = 31
+    A = torch.randn(rows, n, generator=g, dtype=torch.float64).cuda()
+    x = torch.randn(n, generator=g, dtype=torch.float64).cuda()
+    y = torch.randn(rows, generator=g, dtype=torch.float64).cuda()
+    y0 = y.clone()
+    work = torch.zeros(int(L.xrh_gemv_split_work(rows, n)), dtype=torch.float64, device="cuda")
+    _lib.call("xrh_gemv_rows_split", rows, n, _lib.ptr(A), n, _lib.ptr(x), 2.0, 0.5, _lib.ptr(y), _lib.ptr(work),
+              work.numel(), _lib.stream_ptr())
+    ref = 2.0 * (A @ x) + 0.5 * y0
+    torch.cuda.synchronize()
+    assert float((y - ref).abs().max()) <= 1e-13 * float(ref.abs().max())
+    v = torch.empty_like(x)
+    beta = torch.zeros(1, dtype=torch.float64, device="cuda")
+    _lib.call("xrh_lanczos_normalize_split", n, _lib.ptr(x), _lib.ptr(v), _lib.ptr(beta), _lib.ptr(work),
+              work.numel(), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    nrm = float(x.norm())
+    assert abs(float(beta) - nrm) <= 1e-13 * nrm
+    assert float((v - x / nrm).abs().max()) <= 1e-15 * float((x / nrm).abs().max()) * 10
+    assert L.xrh_gemv_rows_split(rows, n, _lib.ptr(A), n, _lib.ptr(x), 1.0, 0.0, _lib.ptr(y), _lib.ptr(work),
+                                 work.numel() - 1, None) == _lib.XRH_ERR_CAPACITY
+
+
+def test_krylov_operator_known_spectrum():
+    """The matrix-free loop (split products) on an operator with a known spectrum:
+    A = Q diag(d) Q with the Householder reflection Q = 1 - 2 u u^T, n = 100 003."""
+    from qodeapplications_gb300.eigen import Lanczos
+    n = 100_003
+    g = torch.Generator().manual_seed(2)
+    d = torch.linspace(-3.0, 5.0, n, dtype=torch.float64)
+    d[0] = -4.0
+    u = torch.randn(n, generator=g, dtype=torch.float64)
+    u = (u / u.norm()).cuda()
+    d = d.cuda()
+
+    def apply(x, y):
+        t = x - 2.0 * u * torch.dot(u, x)
+        t = d * t
+        y.copy_(t - 2.0 * u * torch.dot(u, t))
+
+    lz = Lanczos(n, m=60, mode="steps")
+    lz.krylov_operator(apply)
+    lz.stage_to_host()
+    torch.cuda.synchronize()
+    w, resid = lz.solve(1)
+    assert abs(w[0] + 4.0) <= 1e-10 * 4.0 + resid and resid < 1e-6
