@@ -465,7 +465,7 @@ def run_trimer(args):
         rec = {"s_per_iter": sum(ms) / 1e3 / n_steps, "E0": Es[-1][0], "resid": Es[-1][1],
                "gpu_launches": _lib.LaunchCounter.count, "clocks": cs.summary(int(os.environ.get("LOCAL_RANK", "0")))}
         # dominant kernel: stage B of H x v (x' segments, 2 n^4 N^2 FLOPs per trimer block)
-        st = ham.stages[1]
+        st = ham.stage_b
         st.run()
         torch.cuda.synchronize()
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

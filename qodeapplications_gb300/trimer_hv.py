@@ -21,12 +21,14 @@ For a trimer charge block with fragment order (x, y, z) (build_H.py:103-188 case
 the fragment carrying the two-index density first), the product runs in three GEMM stages
 that never touch an n^3 x n^3 object:
 
-  A  T1[x',y',z,s]  = sum_z'     v[x',y',z'] R3[z,z',s]          (batched over z)
+  A  T1[x',y',z,s]  = sum_z'     v[x',y',z'] R3t[z,s,z']          (R3 transposed once per build)
   B  T2[x,r,y',z]   = sum_x',s   P[x',x,r,s] T1[x',y',z,s]        (x' as K-concatenated segments)
-  C  w[x,y,z]      += a sum_r,y' R2[y,r,y'] T2[x,r,y',z]         (batched over x)
+     T2p[x,z,y',r]  = a T2[x,r,y',z]                               (factor and phase folded in)
+  C  w[x,z,y]      += sum_y',r   T2p[x,z,y',r] R2[y,y',r]
 
-about 2 n^4 N^2 FLOPs per block instead of the 2 n^6 of a stored block.  Blocks of a fragment
-order other than (0, 1, 2) read a permuted copy of v and add into a permuted accumulator.
+each one GEMM with K contiguous in both operands, about 2 n^4 N^2 FLOPs per block instead of
+the 2 n^6 of a stored block.  Blocks of a fragment order other than (0, 1, 2) read a permuted
+copy of v (order x, y, z) and add into a permuted accumulator (order x, z, y).
 
 TrimerHvPlan is the plan as host data (GEMM task records over named flat buffers), so the
 same plan drives the device (XRTrimerHamiltonian, grouped launches of libxrh's GEMM) and can
@@ -104,17 +106,17 @@ class TrimerHvPlan:
             dim += int(np.prod(self.shape[t]))
         self.dim = dim
         self.sizes = {"v": dim, "w": dim}
-        self.build_tasks, self.permutes = [], []
+        self.build_tasks, self.permutes, self.mid_permutes = [], [], []
         self.launches = [[], [], []]
-        self.orders = set()
+        self.orders_v, self.orders_w = set(), set()
         self.pair_layout = [pair_sector_layout(self.charges[a], self.charges[b], ns[a], ns[b]) for a, b in PAIRS]
         self._monomers(avail)
         self._pairs()
         self._trimers(avail)
-        for o in sorted(self.orders):
-            if o != IDENTITY:
-                self.sizes[_vname(o)] = dim
-                self.sizes[_wname(o)] = dim
+        for o in sorted(self.orders_v - {IDENTITY}):
+            self.sizes[_vname(o)] = dim
+        for o in sorted(self.orders_w - {IDENTITY}):
+            self.sizes[_wname(o)] = dim
         self.flops_apply = sum(_task_flops(t) for L in self.launches for t in L)
         self.flops_build = sum(_task_flops(t) for t in self.build_tasks)
 
@@ -164,7 +166,7 @@ class TrimerHvPlan:
                     na2, nb2 = self.ns[a][ca2], self.ns[b][cb2]
                     if (a, b) == (0, 1):
                         # v in fragment order (2, 0, 1): the block is [i2][(j0 j1)], K-contiguous
-                        self.orders.add((2, 0, 1))
+                        self.orders_v.add((2, 0, 1))
                         segs.append(_seg(H, dimt, ("v201", self.off[src]), na2 * nb2, na2 * nb2))
                     elif (a, b) == (1, 2):
                         segs.append(_seg(("v", self.off[src]), na2 * nb2, H, dimt, na2 * nb2))
@@ -172,7 +174,8 @@ class TrimerHvPlan:
                         # spectator 1: (-1)^(n_1 dq), n_1 its electron-count parity, dq the parity of
                         # the charge moved between fragments 0 and 2
                         odd = (self.n_elec[1] - t[1]) % 2 == 1 and (t[0] - ca2) % 2 == 1
-                        self.orders.add((1, 0, 2))
+                        self.orders_v.add((1, 0, 2))
+                        self.orders_w.add((1, 0, 2))
                         segs.append(_seg(("v102", self.off[src]), na2 * nb2, H, dimt, na2 * nb2,
                                          alpha=-1.0 if odd else 1.0))
                 if not segs:
@@ -191,7 +194,7 @@ class TrimerHvPlan:
     def _trimers(self, avail):
         """Three-stage products of every trimer charge block (build_H.py:103-188)."""
         ns, N = self.ns, self.Ns
-        P_off, T1_off, T2_off, R2_off = {}, {}, {}, {}
+        P_off, T1_off, T2_off, R3_off = {}, {}, {}, {}
         out_tasks = {}
         self.integral_keys = set()          # (kind, order) of every W matrix the stage-1 tasks read
         self.n_trimer_blocks = 0
@@ -205,7 +208,9 @@ class TrimerHvPlan:
                 if not all(avail(order[k], ops[k], ci[order[k]], cj[order[k]]) for k in range(3)):
                     continue
                 self.n_trimer_blocks += 1
-                self.orders.add(order)
+                out_order = (x, z, y)
+                self.orders_v.add(order)
+                self.orders_w.add(out_order)
                 nx, nxp = ns[x][ci[x]], ns[x][cj[x]]
                 ny, nyp = ns[y][ci[y]], ns[y][cj[y]]
                 nz, nzp = ns[z][ci[z]], ns[z][cj[z]]
@@ -221,37 +226,45 @@ class TrimerHvPlan:
                         segs.append(_seg((("eye", nx), 0), 1, (("Uq", order), 0), 1, 1, sA=nx))
                     self.build_tasks.append(_task(nxp, Ny * Nz, ("Pt", P_off[pkey]), nx * Ny * Nz, segs, mode=0,
                                                   batch=nx, sC=Ny * Nz))
-                # R2 as [y][r][y'] (per build)
-                rkey = (y, ops[1], ci[y], cj[y])
-                if rkey not in R2_off:
-                    R2_off[rkey] = self._alloc("R2t", ny * Ny * nyp)
-                    self.permutes.append(((("rho",) + rkey, 0), (ny, nyp, Ny), (0, 2, 1), ("R2t", R2_off[rkey])))
-                # A: T1[x'][y'][z][s] = sum_z' v[x',y',z'] R3[z,z',s]
-                t1key = (order, cj, z, ops[2], ci[z])
+                # R3 as [z][s][z'] (per build)
+                rkey = (z, ops[2], ci[z], cj[z])
+                if rkey not in R3_off:
+                    R3_off[rkey] = self._alloc("R3t", nz * Nz * nzp)
+                    self.permutes.append(((("rho",) + rkey, 0), (nz, nzp, Nz), (0, 2, 1), ("R3t", R3_off[rkey])))
+                # A: T1[(x' y')][(z s)] = sum_z' v_xyz[(x' y')][z'] R3t[(z s)][z']
+                t1key = (order, cj, rkey)
                 if t1key not in T1_off:
                     T1_off[t1key] = self._alloc("T1", nxp * nyp * nz * Nz)
-                    self.launches[0].append(_task(
-                        nxp * nyp, Nz, ("T1", T1_off[t1key]), nz * Nz,
-                        [_seg((_vname(order), self.off[cj]), nzp, (("rho", z, ops[2], ci[z], cj[z]), 0), Nz, nzp,
-                              flags=2, sB=nzp * Nz)], mode=0, batch=nz, sC=Nz))
+                    task = _task(nxp * nyp, nz * Nz, ("T1", T1_off[t1key]), nz * Nz,
+                                 [_seg((_vname(order), self.off[cj]), nzp, ("R3t", R3_off[rkey]), nzp, nzp)], mode=0)
+                    task["role"] = "A"
+                    self.launches[0].append(task)
                 # B: T2[x][r][y'][z] = sum_x' sum_s Pt[x'][x][r][s] T1[x'][y'][z][s]
-                t2key = (pkey, t1key)
+                s2 = -1.0 if (self.n_elec[1] - ci[1]) % 2 else 1.0
+                s3 = -1.0 if (self.n_elec[2] - ci[2]) % 2 else 1.0
+                alpha = (4.0 if kind == "tex" else 2.0) * _phase(kind, order, s2, s3)
+                t2key = (pkey, t1key)            # one charge block: (ci[x], ci[z], cj) fix ci[y]
                 if t2key not in T2_off:
                     T2_off[t2key] = self._alloc("T2", nx * Ny * nyp * nz)
                     p0, q0 = P_off[pkey], T1_off[t1key]
                     segs = [_seg(("Pt", p0 + xp * nx * Ny * Nz), Nz, ("T1", q0 + xp * nyp * nz * Nz), Nz, Nz)
                             for xp in range(nxp)]
-                    self.launches[1].append(_task(nx * Ny, nyp * nz, ("T2", T2_off[t2key]), nyp * nz, segs, mode=0))
-                # C: w[x][y][z] += a sum_(r,y') R2t[y][r][y'] T2[x][r][y'][z]
-                s2 = -1.0 if (self.n_elec[1] - ci[1]) % 2 else 1.0
-                s3 = -1.0 if (self.n_elec[2] - ci[2]) % 2 else 1.0
-                alpha = (4.0 if kind == "tex" else 2.0) * _phase(kind, order, s2, s3)
-                okey = (order, ci)
+                    task = _task(nx * Ny, nyp * nz, ("T2", T2_off[t2key]), nyp * nz, segs, mode=0)
+                    task["role"] = "B"
+                    self.launches[1].append(task)
+                    # T2p[x][z][y'][r] = a T2[x][r][y'][z] (per product): the K-contiguous operand of
+                    # stage C with the block's factor and phase folded in
+                    self.mid_permutes.append((("T2", T2_off[t2key]), (nx, Ny, nyp, nz), (0, 3, 2, 1),
+                                              ("T2p", T2_off[t2key]), alpha))
+                    self.sizes["T2p"] = self.sizes["T2"]
+                # C: w_xzy[(x z)][y] += sum_(y',r) T2p[(x z)][(y' r)] R2[y][(y' r)]
+                okey = (out_order, ci)
                 if okey not in out_tasks:
-                    out_tasks[okey] = _task(ny, nz, (_wname(order), self.off[ci]), nz, [], batch=nx, sC=ny * nz)
+                    out_tasks[okey] = _task(nx * nz, ny, (_wname(out_order), self.off[ci]), ny, [])
+                    out_tasks[okey]["role"] = "C"
                     self.launches[2].append(out_tasks[okey])
-                out_tasks[okey]["segs"].append(_seg(("R2t", R2_off[rkey]), Ny * nyp, ("T2", T2_off[t2key]), nz,
-                                                    Ny * nyp, alpha=alpha, flags=2, sB=Ny * nyp * nz))
+                out_tasks[okey]["segs"].append(_seg(("T2p", T2_off[t2key]), nyp * Ny,
+                                                    (("rho", y, ops[1], ci[y], cj[y]), 0), nyp * Ny, nyp * Ny))
 
     # ---------------------------------------------------------------------------------
     def permutation(self, order):
@@ -374,48 +387,49 @@ class XRTrimerHamiltonian:
         self.W = {k: w.contiguous().reshape(-1) for k, w in W.items()}
         self.Uq = {k: u.contiguous().reshape(-1) for k, u in Uq.items()}
         self.eyes = {}
-        self._perm_idx = {o: torch.as_tensor(plan.permutation(o), device=dev)
-                          for o in sorted(plan.orders) if o != IDENTITY}
-        self._permutes = [(self._resolve(src), shape, ax, self._resolve(dst)) for src, shape, ax, dst in plan.permutes]
-        # stage B (2 n^4 N^2 FLOPs per trimer block, nearly all of a product) on the tensor cores
-        # for the split forms: Pt slices split once per build, T1 slices once per product; the
-        # small stages and the pair terms then run with FP32 products and FP64 sums
+        self._gather = {o: torch.as_tensor(plan.permutation(o), device=dev) for o in sorted(plan.orders_v - {IDENTITY})}
+        self._scatter = {o: torch.as_tensor(plan.permutation(o), device=dev) for o in sorted(plan.orders_w - {IDENTITY})}
+        self._permutes = [(self._resolve(src), shape, ax, self._resolve(dst), 1.0)
+                          for src, shape, ax, dst in plan.permutes]
+        self._mid_permutes = [(self._resolve(src), shape, ax, self._resolve(dst), a)
+                              for src, shape, ax, dst, a in plan.mid_permutes]
+        # split forms: the pair terms and the three trimer stages on the tensor cores, each role
+        # with its own split registry (a vector block is an operand of several shapes); operands
+        # that change per product (vector blocks, T1, T2p) are split per product, the rest once
+        # per build; the monomer terms and the per-build stage keep FP32 products / FP64 sums
         self.tc = hv_precision in ("bf16x3", "tf32x3")
         simt = "fp32" if self.tc else hv_precision
+        tc_roles = ("pair", "A", "B", "C") if self.tc else ()
         self.stage1 = self._grouped(plan.build_tasks, simt)
-        pair_tasks = [t for t in plan.launches[0] if t.get("role") == "pair"] if self.tc else []
-        self.stages = [self._grouped([t for t in L if not (self.tc and t.get("role") == "pair")], simt)
-                       for L in plan.launches]
-        self.pairs_tc = None
+        self.simt = [self._grouped([t for t in L if t.get("role") not in tc_roles], simt) for L in plan.launches]
+        self.tcs = [[] for _ in plan.launches]
+        self.stage_b = self.simt[1]
         if self.tc:
             from .gemm import SplitRegistry, TCGroupedGemm
-            # pair terms: H2 sub-blocks split once per build, the vector blocks once per product
-            self.reg_pairs = SplitRegistry(hv_precision, dev)
-            tcp = TCGroupedGemm(self.reg_pairs)
-            for t in pair_tasks:
-                assert t["batch"] == 1 and all(sg["flags"] == 0 for sg in t["segs"])
-                segs, groups = [], []
-                for sg in t["segs"]:
-                    segs.append((self._resolve(sg["A"]), sg["lda"], self._resolve(sg["B"]), sg["ldb"], sg["K"],
-                                 sg["alpha"]))
-                    groups.append(tuple("H2" if isinstance(r[0], tuple) else "vec" for r in (sg["A"], sg["B"])))
-                tcp.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=1, groups=groups)
-            self.reg_pairs.upload()
-            self.pairs_tc = tcp.finalize()
-            if autotune:
-                self.pairs_tc.autotune()
-            self.reg = SplitRegistry(hv_precision, dev)
-            tcg = TCGroupedGemm(self.reg)
-            for t in plan.launches[1]:
-                assert t["batch"] == 1 and all(sg["flags"] == 0 for sg in t["segs"])
-                segs = [(self._resolve(sg["A"]), sg["lda"], self._resolve(sg["B"]), sg["ldb"], sg["K"], sg["alpha"])
-                        for sg in t["segs"]]
-                tcg.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"],
-                        groups=[("Pt", "T1")] * len(segs))
-            self.reg.upload()
-            self.stages[1] = tcg.finalize()
-            if autotune:
-                self.stages[1].autotune()
+            per_product = ("v", "T1", "T2p")
+            for k, L in enumerate(plan.launches):
+                for role in tc_roles:
+                    tasks = [t for t in L if t.get("role") == role]
+                    if not tasks:
+                        continue
+                    reg = SplitRegistry(hv_precision, dev)
+                    g = TCGroupedGemm(reg)
+                    for t in tasks:
+                        assert t["batch"] == 1 and all(sg["flags"] == 0 for sg in t["segs"])
+                        segs, groups = [], []
+                        for sg in t["segs"]:
+                            segs.append((self._resolve(sg["A"]), sg["lda"], self._resolve(sg["B"]), sg["ldb"], sg["K"],
+                                         sg["alpha"]))
+                            groups.append(tuple("product" if isinstance(r[0], str) and r[0].startswith(per_product)
+                                                else "build" for r in (sg["A"], sg["B"])))
+                        g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], groups=groups)
+                    reg.upload()
+                    g.finalize()
+                    if autotune:
+                        g.autotune()
+                    self.tcs[k].append((reg, g))
+                    if role == "B":
+                        self.stage_b = g
         self.flops_apply = plan.flops_apply
         self.dim = plan.dim
 
@@ -467,13 +481,21 @@ class XRTrimerHamiltonian:
             self.set_coeffs(coeffs)
         for pl in self.plans:
             pl.launch()
-        for src, shape, ax, dst in self._permutes:
-            n = int(np.prod(shape))
-            dst[:n].view(shape[ax[0]], shape[ax[1]], shape[ax[2]]).copy_(src[:n].view(shape).permute(*ax))
+        self._run_permutes(self._permutes)
         self.stage1.run()
-        if self.tc:
-            self.reg.split("Pt")
-            self.reg_pairs.split("H2")
+        for phase in self.tcs:
+            for reg, _g in phase:
+                reg.split("build")
+
+    @staticmethod
+    def _run_permutes(ops):
+        for src, shape, ax, dst, scale in ops:
+            n = int(np.prod(shape))
+            out = dst[:n].view(*[shape[a] for a in ax])
+            if scale == 1.0:
+                out.copy_(src[:n].view(shape).permute(*ax))
+            else:
+                torch.mul(src[:n].view(shape).permute(*ax), scale, out=out)
 
     def apply(self, x, out=None):
         """out = H x (device vectors of length self.dim, block layout); returns out."""
@@ -481,17 +503,18 @@ class XRTrimerHamiltonian:
         if x.data_ptr() != v.data_ptr():
             v.copy_(x)
         w.zero_()
-        for o, idx in self._perm_idx.items():
+        for o in self._scatter:
             self.bufs[_wname(o)].zero_()
+        for o, idx in self._gather.items():
             torch.index_select(v, 0, idx, out=self.bufs[_vname(o)])
-        self.stages[0].run()
-        if self.tc:
-            self.reg_pairs.split("vec")
-            self.pairs_tc.run()
-            self.reg.split("T1")
-        self.stages[1].run()
-        self.stages[2].run()
-        for o, idx in self._perm_idx.items():
+        for k in range(3):
+            if k == 2:
+                self._run_permutes(self._mid_permutes)
+            self.simt[k].run()
+            for reg, g in self.tcs[k]:
+                reg.split("product")
+                g.run()
+        for o, idx in self._scatter.items():
             w.index_add_(0, idx, self.bufs[_wname(o)])
         if out is not None and out.data_ptr() != w.data_ptr():
             out.copy_(w)
@@ -502,9 +525,9 @@ class XRTrimerHamiltonian:
         """Raise if a bounded device wait of a tensor-core launch timed out (syncs)."""
         for pl in self.plans:
             pl.check_status()
-        if self.tc:
-            self.stages[1].check()
-            self.pairs_tc.check()
+        for phase in self.tcs:
+            for _reg, g in phase:
+                g.check()
 
     def product_index(self):
         """(device int64 index, product-space dimension): element e of a block-layout vector is

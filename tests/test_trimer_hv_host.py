@@ -88,11 +88,16 @@ class _Interpreter:
         for t in plan.build_tasks:
             _run_task(self._resolve, t)
         for src, shape, ax, dst in plan.permutes:
-            s_arr, s0 = self._resolve(src)
-            d_arr, d0 = self._resolve(dst)
-            n = int(np.prod(shape))
-            d_arr[d0:d0 + n] = s_arr[s0:s0 + n].reshape(shape).transpose(ax).ravel()
-        self.perm = {o: plan.permutation(o) for o in plan.orders if o != (0, 1, 2)}
+            self._permute(src, shape, ax, dst, 1.0)
+        self.gather = {o: plan.permutation(o) for o in plan.orders_v if o != (0, 1, 2)}
+        self.scatter = {o: plan.permutation(o) for o in plan.orders_w if o != (0, 1, 2)}
+
+    def _permute(self, src, shape, ax, dst, scale):
+        s_arr, s0 = self._resolve(src)
+        d_arr, d0 = self._resolve(dst)
+        n = int(np.prod(shape))
+        assert s0 + n <= s_arr.size and d0 + n <= d_arr.size
+        d_arr[d0:d0 + n] = scale * s_arr[s0:s0 + n].reshape(shape).transpose(ax).ravel()
 
     def _resolve(self, ref):
         key, off = ref
@@ -108,13 +113,16 @@ class _Interpreter:
         for k in b:
             if k.startswith("w"):
                 b[k][:] = 0.0
-        for o, idx in self.perm.items():
+        for o, idx in self.gather.items():
             b["v%d%d%d" % o][:] = v[idx]
-        for L in self.plan.launches:
+        for k, L in enumerate(self.plan.launches):
+            if k == 2:
+                for src, shape, ax, dst, scale in self.plan.mid_permutes:
+                    self._permute(src, shape, ax, dst, scale)
             for t in L:
                 _run_task(self._resolve, t)
         w = b["w"].copy()
-        for o, idx in self.perm.items():
+        for o, idx in self.scatter.items():
             w[idx] += b["w%d%d%d" % o]
         return w
 
