@@ -13,7 +13,8 @@ energy/gradient copied back every step.
   python bench.py --config 2 ...         (trimer: pair builds + matrix-free H x v Lanczos ground state)
 
 Multi-GPU: the path does not shard (one dimer), so N>1 runs N independent replicas
-(one per rank, launched by torchrun); value = total iterations / max time over ranks.
+(one per rank, launched by torchrun); value = max time over ranks / iterations of all ranks
+(replica_aggregate).
 """
 import argparse
 import json
@@ -261,6 +262,20 @@ def dominant_kernel_roofline(it, config, reps=20):
                 traffic=DENSITY_ADJ_TRAFFIC_BYTES.get(config))
 
 
+def replica_aggregate(total_ms, e2e_ms, steps, world, device):
+    """Whole-job figures of N independent replicas: every rank ran `steps` iterations of its
+    own copy of the workload; the job's time is the slowest rank's (max over ranks), so the
+    job's seconds per iteration are that time over the iterations of all ranks.  Returns
+    (max total ms, max e2e ms, job s/iter, job e2e s/iter)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    mx, me = float(t[0]), float(t[1])
+    return mx, me, mx / 1e3 / (steps * world), me / 1e3 / (steps * world)
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -317,16 +332,13 @@ def run_ours(args):
         e2e_ms.append(t0.elapsed_time(t1))
     e2e_total = sum(e2e_ms)
 
-    tens = torch.tensor([total_ms, e2e_total], device="cuda")
-    if world > 1:
-        dist.all_reduce(tens, op=dist.ReduceOp.MAX)
-    total_ms, e2e_total = float(tens[0]), float(tens[1])
+    total_ms, e2e_total, s_per_iter, e2e_s_per_iter = replica_aggregate(total_ms, e2e_total, args.steps, world,
+                                                                        "cuda")
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    s_per_iter = total_ms / 1e3 / args.steps
     peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
     dk = dominant_kernel_roofline(it, args.config)
@@ -371,7 +383,7 @@ def run_ours(args):
                    "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{world}",
                    "step": "one steepest-descent state-optimizer iteration: densities + XR-H build + FP64 Lanczos "
                            "ground state + adjoint state and orbital gradients + Loewdin step"},
-        "e2e": {"value": e2e_total / 1e3 / args.steps, "unit": "s/iter", "h2d_bytes_per_step": it.h2d_bytes,
+        "e2e": {"value": e2e_s_per_iter, "unit": "s/iter", "h2d_bytes_per_step": it.h2d_bytes,
                 "d2h_bytes_per_step": it.d2h_bytes},
         "gpu_launches": launches, "gpu_launches_per_iteration": per_iter, "roofline": roofline, "clocks": clocks,
         "energies": energies[:3], "flops_per_build": it.opt.plan.flops, "variants": variants,
@@ -416,6 +428,8 @@ def run_trimer(args):
     from qodeapplications_gb300.densities import FragmentSpace
     from qodeapplications_gb300.hamiltonian import DeviceIntegrals
     from qodeapplications_gb300.trimer_hv import XRTrimerHamiltonian
+    if int(os.environ.get("RANK", "0")) != 0:
+        return                       # one trimer on one GPU: under torchrun rank 0 alone runs it
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     c = dict(CONFIGS[2])
     if args.states:
