@@ -332,6 +332,8 @@ class XRDimerPlan:
     convention: 'hermitian' (diagram phases of hermitian-XRCC) or 'general' (the sign
               convention of general-XRCC/build_H.py:68, charge-transfer blocks differ by
               the gauge (-1)^(n_i1 + n_j0)).
+    builders: two DensityBuilder objects shared with other plans (built by their owner;
+              launch(build_densities=False)), or None for the plan's own.
 
     The inputs are the persistent coefficient buffers self.coeffs[m][charge]
     (n_states x n_conf); launch() enqueues the whole build on the current stream without
@@ -340,7 +342,7 @@ class XRDimerPlan:
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
                  convention="hermitian", layout="product", dens_precision=None, sigma_precision=None,
-                 autotune=True):
+                 autotune=True, builders=None):
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
         self.ints = ints
@@ -367,6 +369,10 @@ class XRDimerPlan:
             # near FP32 accuracy; 3 x BF16 (16-bit) would cost about 1e-5 relative per element
             self.builders = [IntermediateDensityBuilder(spaces[m], self.n_states[m], precision="tf32x3",
                                                         autotune=autotune) for m in (0, 1)]
+        elif builders is not None:
+            # density builders shared with other plans (the pairs of a larger system): the
+            # owner builds them once per iteration and calls launch(build_densities=False)
+            self.builders = list(builders)
         else:
             self.builders = [DensityBuilder(spaces[m], self.n_states[m], precision=self.dens_precision)
                              for m in (0, 1)]
@@ -656,10 +662,12 @@ class XRDimerPlan:
             for c in self.charges[m]:
                 self.coeffs[m][c].copy_(coeffs[m][c], non_blocking=True)
 
-    def launch(self):
-        """Enqueue the whole build (densities, sigma, precontractions, final blocks)."""
+    def launch(self, build_densities=True):
+        """Enqueue the whole build (densities, sigma, precontractions, final blocks); with
+        build_densities=False the density builders are taken as already built."""
         for m in (0, 1):
-            self.builders[m].build(self.coeffs[m])
+            if build_densities:
+                self.builders[m].build(self.coeffs[m])
         self.sigma_batch.run()
         for m in (0, 1):
             for c, sg in self.sigma[m].items():

@@ -357,18 +357,25 @@ class XRTrimerHamiltonian:
 
     def __init__(self, spaces, n_states, charges, ints, precision="fp64", hv_precision="fp64", total_charge=None,
                  autotune=True):
+        from .densities import DensityBuilder
         from .hamiltonian import XRDimerPlan
         dev = spaces[0].device
         self.device = dev
         self.charges = [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
+        # one density builder per fragment, shared by the two pair plans that hold it (FP32
+        # products on the split-precision paths, as XRDimerPlan chooses for its own)
+        dens_precision = "fp32" if precision in ("bf16x3", "tf32x3") else "fp64"
+        self.builders = [DensityBuilder(spaces[f], self.n_states[f], precision=dens_precision) for f in range(3)]
         self.plans = [XRDimerPlan([spaces[a], spaces[b]], [self.n_states[a], self.n_states[b]],
                                   [self.charges[a], self.charges[b]], _PairIntegrals(ints, (a, b)), output="split",
-                                  precision=precision, convention="general", layout="sector", autotune=autotune)
+                                  precision=precision, convention="general", layout="sector", autotune=autotune,
+                                  builders=[self.builders[a], self.builders[b]])
                       for a, b in PAIRS]
-        # each fragment's densities and monomer blocks from one pair plan that holds it
+        # each fragment's coefficient buffers and monomer blocks from one pair plan that holds it
         holder = {0: (0, 0), 1: (0, 1), 2: (1, 1)}
-        self.rho = [self.plans[p].builders[k].rho for p, k in (holder[f] for f in range(3))]
+        self.rho = [b.rho for b in self.builders]
+        self.coeffs = [self.plans[p].coeffs[k] for p, k in (holder[f] for f in range(3))]
         self.H1blk = [self.plans[p].H1blk[k] for p, k in (holder[f] for f in range(3))]
 
         def avail(f, op, bc, kc):
@@ -479,8 +486,10 @@ class XRTrimerHamiltonian:
         """Enqueue the pair builds and the per-build trimer stage (no host synchronisation)."""
         if coeffs is not None:
             self.set_coeffs(coeffs)
+        for b, z in zip(self.builders, self.coeffs):
+            b.build(z)
         for pl in self.plans:
-            pl.launch()
+            pl.launch(build_densities=False)
         self._run_permutes(self._permutes)
         self.stage1.run()
         for phase in self.tcs:
