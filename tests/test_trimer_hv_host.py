@@ -205,3 +205,28 @@ def test_plan_sector_ground_state_is_fci():
     G = G[O.popcount(G) == 6]
     E_fci = np.linalg.eigvalsh(O.fci_hamiltonian(ints.h, ints.Vfull, G))
     np.testing.assert_allclose(np.linalg.eigvalsh(H)[:5], E_fci[:5], atol=1e-11)
+
+
+def test_plan_uneven_state_counts_and_charge_order():
+    """Charge blocks of different sizes (3, 2 and 1 states for charges 0, +1, -1, in the
+    general-XRCC order with the reference charge first) on all three fragments."""
+    charges = (0, +1, -1)
+    counts = {0: 3, +1: 2, -1: 1}
+    sysd = S.make_system(n_frag=3, n_orb=3, n_states=3, charges=charges, n_elec_ref=4, seed=77)
+    ints = O.FragInts(sysd["h"], sysd["V"], sysd["Ns"])
+    dens = []
+    for m in range(3):
+        secs = {c: O.Sector(sysd["states"][m][c][0][:counts[c]], sysd["states"][m][c][1]) for c in charges}
+        dens.append(O.build_densities(secs, 3, 0, 4))
+    ns = [dict(counts)] * 3
+    for tc in (None, 0):
+        plan = TrimerHvPlan([list(charges)] * 3, ns, [4] * 3, ints.Ns,
+                            lambda f, op, bc, kc: (bc, kc) in dens[f].get(op, {}), tc)
+        Hfull = O.general_xr_H_full(dens, ints, 4, list(charges), 3)
+        idx, D = plan.product_index()
+        it = _Interpreter(plan, dens, ints)
+        v = np.random.default_rng(9).normal(size=plan.dim)
+        vp = np.zeros(D)
+        vp[idx] = v
+        ref = (Hfull @ vp)[idx]
+        assert np.abs(it.apply(v) - ref).max() <= 1e-12 * np.abs(ref).max()
