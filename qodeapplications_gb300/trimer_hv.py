@@ -84,7 +84,7 @@ class TrimerHvPlan:
     total_charge: None for the whole product space, or one total charge (H conserves it)
 
     Buffers are named: 'v', 'w' (the vectors), 'vXYZ'/'wXYZ' (permuted copies for fragment
-    order XYZ), 'Pt', 'R2t', 'T1', 'T2' (intermediates, sizes in self.sizes) and external
+    order XYZ), 'Pt', 'R3t', 'T1', 'T2', 'T2p' (intermediates, sizes in self.sizes) and external
     keys ('rho', f, op, bc, kc), ('H1', f, c), ('H2', pair, t), ('W', kind, order),
     ('Uq', order), ('eye', n).  A reference is (buffer, element offset)."""
 
@@ -93,7 +93,7 @@ class TrimerHvPlan:
         self.ns = [dict(n) for n in n_states]
         self.n_elec = list(n_elec)
         self.Ns = list(Ns)
-        ns, N = self.ns, self.Ns
+        ns = self.ns
         triples = [(a, b, c) for a in self.charges[0] for b in self.charges[1] for c in self.charges[2]]
         if total_charge is not None:
             triples = [t for t in triples if sum(t) == total_charge]
