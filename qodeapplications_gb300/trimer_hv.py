@@ -383,6 +383,8 @@ class XRTrimerHamiltonian:
 
         plan = TrimerHvPlan(self.charges, self.n_states, [sp.n_elec_ref for sp in spaces], [sp.N for sp in spaces],
                             avail, total_charge)
+        if plan.dim == 0:
+            raise ValueError(f"no product state has total charge {total_charge}")
         self.plan = plan
         for p, lay in enumerate(plan.pair_layout):
             for t, (base, dimt) in lay.items():

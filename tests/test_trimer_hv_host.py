@@ -230,3 +230,12 @@ def test_plan_uneven_state_counts_and_charge_order():
         vp[idx] = v
         ref = (Hfull @ vp)[idx]
         assert np.abs(it.apply(v) - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_plan_empty_sector_has_no_work():
+    """A total charge that no charge triple reaches gives an empty plan (the device class
+    then refuses it with ValueError before any product)."""
+    plan = TrimerHvPlan([[1, 0, -1]] * 3, [{1: 2, 0: 2, -1: 2}] * 3, [4] * 3, [6] * 3,
+                        lambda f, op, bc, kc: True, total_charge=5)
+    assert plan.dim == 0 and plan.triples == [] and all(not L for L in plan.launches)
+    assert plan.flops_apply == 0.0 and not plan.build_tasks
