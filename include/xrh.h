@@ -145,7 +145,8 @@ int xrh_coeff_stage(const xrh_coeff_task* tasks_dev, int n_tasks, int64_t total_
  * (K * n_b * n_k <= 1048576 doubles, else XRH_ERR_CAPACITY) and writes rho_dev directly in
  * the (n_b, n_k, K) layout.  Arguments are those of xrh_density_accumulate.  It calls no
  * cudaMalloc/cudaFree.  The first call on a device looks up that device's address of the
- * array (cudaGetSymbolAddress) and must therefore happen before any stream capture.  All
+ * array (cudaGetSymbolAddress) and must therefore happen before any stream capture; first
+ * calls from several host threads at once are safe (each stores the same address).  All
  * calls share the array: calls that overlap on the GPU (other streams, other host threads)
  * race and must be serialised by the caller.  Every GPU that loads the library keeps the
  * 8 MiB until the process exits. */

@@ -8,10 +8,12 @@
 #
 # Flags follow the reference's own loader: qode.util.PyC.import_C(name, flags="-O2")
 # (general-XRCC/build_H.py:20, general-XRCC/build_density_tensors.py:23-24).
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# The reference tree is the first argument, else $XRH_REFERENCE_ROOT, else /root/reference.
+# Without the sources (e.g. on a machine that has only this repository) it exits 0 and keeps
+# any prebuilt oracle/_ref.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${XRH_REFERENCE_ROOT:-/root/reference}}"
 SRC="$REF/general-XRCC"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/density_tensors.c" ]; then

@@ -10,6 +10,8 @@
 //       build_density_tensors.py:122-133, H_contractions.c:61-78).
 #include "xrh_common.cuh"
 
+#include <atomic>
+
 namespace {
 
 constexpr int kAccThreads = 256;
@@ -394,7 +396,9 @@ extern "C" int xrh_mirror_density(int na, int nb, int N, int L, const double* sr
 namespace {
 constexpr int64_t kNoAllocScratchDoubles = 1LL << 20;          // 8 MiB of FP64
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
-double* g_noalloc_scratch_addr[256] = {};                      // device address per device ordinal
+// device address of the array per device ordinal; a first call from two host threads at once
+// looks the address up twice and stores the same value, so relaxed atomics suffice
+std::atomic<double*> g_noalloc_scratch_addr[256] = {};
 }  // namespace
 
 extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t* idx_ptr_dev, const int32_t* P_dev,
@@ -410,7 +414,7 @@ extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t
         return XRH_ERR_CUDA;
     }
     if (dev < 0 || dev >= 256) return XRH_ERR_CAPACITY;
-    double* scratch = g_noalloc_scratch_addr[dev];
+    double* scratch = g_noalloc_scratch_addr[dev].load(std::memory_order_relaxed);
     if (!scratch) {
         // once per device, with that device current: the host-side name of the array is not a
         // device address, so ask the runtime for this device's address of it
@@ -419,7 +423,7 @@ extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t
             xrh_set_last_cuda_error((int)e);
             return XRH_ERR_CUDA;
         }
-        g_noalloc_scratch_addr[dev] = scratch;
+        g_noalloc_scratch_addr[dev].store(scratch, std::memory_order_relaxed);
     }
     // the accumulate kernel overwrites every scratch element it uses: nothing to clear
     int st = xrh_density_accumulate(precision, K, idx_ptr_dev, P_dev, Q_dev, sign_dev, zbT_dev, n_b, zkT_dev, n_k,

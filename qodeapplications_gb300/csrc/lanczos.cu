@@ -14,6 +14,26 @@
 
 #include "xrh_common.cuh"
 
+#include <mutex>
+
+namespace {
+// Host-side launch state of the Lanczos loops, one record per device ordinal: function
+// attributes (the raised dynamic shared-memory limits, the non-portable cluster size) are
+// per device, and so is the cluster shape chosen for a sector.  One mutex guards all records
+// (the first eager call of a shape takes it; later calls only read under it).
+constexpr int kLzMaxDevices = 64;
+struct LzChoice { int n, m, max_ctas, nb, h_smem; size_t smem; bool ok; };
+struct LzDeviceState {
+    size_t coop_smem_set = 48 * 1024;
+    size_t cluster_smem_set = 48 * 1024;
+    int nonportable = -1;
+    LzChoice cache[32];
+    int n_cache = 0;
+};
+std::mutex g_lz_mutex;
+LzDeviceState g_lz_state[kLzMaxDevices];
+}  // namespace
+
 namespace {
 
 __global__ void __launch_bounds__(256) gemv_rows_kernel(int64_t rows, int64_t cols, const double* __restrict__ A,
@@ -674,14 +694,18 @@ extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t l
     if (base > (size_t)smem_optin) return XRH_ERR_CAPACITY;
     const int stage_v = base + sizeof(double) * (size_t)n <= (size_t)smem_optin ? 1 : 0;
     const size_t smem = base + (stage_v ? sizeof(double) * (size_t)n : 0);
-    // raise the kernel's dynamic shared-memory limit once per larger size (set before any
-    // capture by the first, eager call)
-    static size_t smem_set = 48 * 1024;
-    if (smem > smem_set) {
-        if (cudaFuncSetAttribute(lanczos_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return XRH_ERR_CUDA;
-        smem_set = smem;
+    // raise the kernel's dynamic shared-memory limit on this device once per larger size (set
+    // before any capture by the first, eager call)
+    if (dev < 0 || dev >= kLzMaxDevices) return XRH_ERR_CAPACITY;
+    {
+        std::lock_guard<std::mutex> lock(g_lz_mutex);
+        size_t& smem_set = g_lz_state[dev].coop_smem_set;
+        if (smem > smem_set) {
+            if (cudaFuncSetAttribute(lanczos_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+                return XRH_ERR_CUDA;
+            smem_set = smem;
+        }
     }
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_coop_kernel, LC_THREADS, smem) != cudaSuccess)
         return XRH_ERR_CUDA;
@@ -714,31 +738,32 @@ static size_t lanczos_cluster_smem(int n, int m, int nb, int h_smem, int smem_op
 
 // Cluster size (16 CTAs when the part schedules such clusters with the needed shared memory,
 // else 8), H in shared memory or not, and the shared memory per CTA for an n x n sector and m
-// steps.  Decided once per shape (on the first, eager call) and cached, so no occupancy query
-// runs inside a stream capture.  Returns false when no cluster takes the sector.
+// steps on the current device.  Decided once per (device, shape) on the first, eager call and
+// cached, so no occupancy query runs inside a stream capture.  Returns false when no cluster
+// takes the sector.
 static bool lanczos_cluster_choice(int n, int m, int max_ctas, int& nb, int& h_smem, size_t& smem) {
-    struct Choice { int n, m, max_ctas, nb, h_smem; size_t smem; bool ok; };
-    static Choice cache[32];
-    static int n_cache = 0;
-    for (int i = 0; i < n_cache; ++i)
-        if (cache[i].n == n && cache[i].m == m && cache[i].max_ctas == max_ctas) {
-            nb = cache[i].nb;
-            h_smem = cache[i].h_smem;
-            smem = cache[i].smem;
-            return cache[i].ok;
-        }
     int dev = 0, smem_optin = 0;
-    bool ok = false;
     nb = 0;
     h_smem = 0;
     smem = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
-        static int nonportable = -1;
-        if (nonportable < 0)
-            nonportable = cudaFuncSetAttribute(lanczos_cluster_kernel,
-                                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess ? 1 : 0;
-        static size_t smem_set = 48 * 1024;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kLzMaxDevices) return false;
+    std::lock_guard<std::mutex> lock(g_lz_mutex);
+    LzDeviceState& st = g_lz_state[dev];
+    for (int i = 0; i < st.n_cache; ++i)
+        if (st.cache[i].n == n && st.cache[i].m == m && st.cache[i].max_ctas == max_ctas) {
+            nb = st.cache[i].nb;
+            h_smem = st.cache[i].h_smem;
+            smem = st.cache[i].smem;
+            return st.cache[i].ok;
+        }
+    bool ok = false;
+    if (cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
+        if (st.nonportable < 0)
+            st.nonportable = cudaFuncSetAttribute(lanczos_cluster_kernel,
+                                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess
+                                 ? 1
+                                 : 0;
+        const int nonportable = st.nonportable;
         const int top = (nonportable ? 16 : 8) < max_ctas || max_ctas <= 0 ? (nonportable ? 16 : 8) : max_ctas;
         for (int want = top; !ok && want >= 1; want = want > 8 ? 8 : want / 2) {
             nb = want < n ? want : n;
@@ -749,11 +774,11 @@ static bool lanczos_cluster_choice(int n, int m, int max_ctas, int& nb, int& h_s
                 smem = lanczos_cluster_smem(n, m, nb, 0, smem_optin);
             }
             if (!smem) continue;
-            if (smem > smem_set) {
+            if (smem > st.cluster_smem_set) {
                 if (cudaFuncSetAttribute(lanczos_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem) != cudaSuccess)
                     continue;
-                smem_set = smem;
+                st.cluster_smem_set = smem;
             }
             cudaLaunchConfig_t cfg = {};
             cudaLaunchAttribute attr[1];
@@ -771,7 +796,7 @@ static bool lanczos_cluster_choice(int n, int m, int max_ctas, int& nb, int& h_s
         }
         cudaGetLastError();
     }
-    if (n_cache < 32) cache[n_cache++] = Choice{n, m, max_ctas, nb, h_smem, smem, ok};
+    if (st.n_cache < 32) st.cache[st.n_cache++] = LzChoice{n, m, max_ctas, nb, h_smem, smem, ok};
     return ok;
 }
 

@@ -144,6 +144,28 @@ class Lanczos:
         resid = abs(b[cut - 1] * Y[cut - 1, 0]) if cut == m else 0.0
         return w[:k], resid
 
+    def ritz(self, k=5):
+        """Host part (after a sync): the lowest k Ritz values, their tridiagonal eigenvectors
+        (cut x k) and the residual norm estimate of each."""
+        from scipy.linalg import eigh_tridiagonal
+        self.solve(1)
+        m, cut = self.m, self._cut
+        a = self._host[:m].numpy()[:cut].copy()
+        b = self._host[m:2 * m].numpy()[:cut].copy()
+        w, Y = eigh_tridiagonal(a, b[:cut - 1])
+        k = min(k, cut)
+        resid = np.abs(b[cut - 1] * Y[cut - 1, :k]) if cut == m else np.zeros(k)
+        return w[:k], Y[:, :k], resid
+
+    def ritz_vector(self, y, out):
+        """out = V^T y for a tridiagonal eigenvector y (length <= m), on the device."""
+        yy = np.zeros(self.m + 1)
+        yy[:len(y)] = y
+        self.y.copy_(torch.from_numpy(yy))
+        out.zero_()
+        call("xrh_gemv_cols", self.m, self.n, ptr(self.V), self.n, ptr(self.y), 1.0, ptr(out), stream_ptr())
+        return out
+
     def ground_vector(self):
         """Ritz vector of the lowest eigenvalue (device, normalised)."""
         y = np.zeros(self.m + 1)
@@ -162,3 +184,27 @@ def lowest_eigenpairs_lanczos(H, k=5, m=96):
     torch.cuda.current_stream().synchronize()
     w, resid = lz.solve(k)
     return w, lz.ground_vector(), resid
+
+
+def lowest_eigenpairs(H, k=5, tol=1e-10, m=None):
+    """Lowest k eigenvalues (numpy) and eigenvectors (device, n x k) of a symmetric FP64
+    matrix on the device by this library's Lanczos loop: the Krylov depth doubles until every
+    one of the k Ritz pairs has a residual below tol (relative to max(1, |w|)) or the depth
+    reaches n, where the Krylov space is the whole space."""
+    n = int(H.shape[0])
+    H = H.contiguous()
+    m = min(n, max(120, 8 * k) if m is None else int(m))
+    while True:
+        lz = Lanczos(n, m=m, device=H.device)
+        lz.krylov(H)
+        lz.stage_to_host()
+        torch.cuda.current_stream().synchronize()
+        w, Y, resid = lz.ritz(k)
+        if m >= n or np.all(resid <= tol * np.maximum(1.0, np.abs(w))):
+            break
+        m = min(n, 2 * m)
+    vecs = torch.zeros((n, len(w)), dtype=torch.float64, device=H.device)
+    tmp = torch.zeros(n, dtype=torch.float64, device=H.device)
+    for i in range(len(w)):
+        vecs[:, i].copy_(lz.ritz_vector(Y[:, i], tmp))
+    return w, vecs

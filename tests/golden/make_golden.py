@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference tree (default /root/reference) after
-`oracle/build_ref.sh` has compiled its C kernels:
+Run on a machine that has the reference tree after `oracle/build_ref.sh` has compiled its
+C kernels; the tree is the first argument, else $XRH_REFERENCE_ROOT, else /root/reference:
 
     python tests/golden/make_golden.py [REFERENCE_ROOT]
 
@@ -260,7 +260,7 @@ def trimer_elements(ref_root, n_el=300):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
+    root = args[0] if args else os.environ.get("XRH_REFERENCE_ROOT", "/root/reference")
     if "--trimer" in sys.argv:
         trimer_elements(root)
     else:
