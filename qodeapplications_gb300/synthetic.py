@@ -122,6 +122,27 @@ def make_system(n_frag=2, n_orb=9, n_states=10, charges=(+1, 0, -1), n_elec_ref=
                 charges=tuple(charges), Ns=[2 * n_orb] * n_frag, h=h, V=V, states=states)
 
 
+def spin_block_one_electron(h_sp, frag_sizes):
+    """A spatial one-electron matrix spin-blocked like spin_orbital_integrals' h."""
+    sidx = np.array(spin_orbital_spatial_index(frag_sizes))
+    spin = np.concatenate([np.repeat([0, 1], nf) for nf in frag_sizes])
+    return h_sp[np.ix_(sidx, sidx)] * (spin[:, None] == spin[None, :])
+
+
+def make_nuclear_potentials(n_frag, n_orb, scale=0.05, seed=4321):
+    """Seeded fragment nuclear potentials U[k] (supersystem spin orbitals, symmetric spatial
+    entries N(0, scale), spin-blocked), for inputs with U != 0: the integrals are then
+    T = h - sum_k U[k] and U (the reference's fragment-blocked T and U,
+    hermitian-XRCC/get_ints.py:116-155), with the total one-electron operator h unchanged."""
+    rng = np.random.default_rng(seed)
+    n = n_frag * n_orb
+    out = []
+    for _k in range(n_frag):
+        a = rng.normal(0.0, scale, size=(n, n))
+        out.append(spin_block_one_electron(np.triu(a) + np.triu(a, 1).T, [n_orb] * n_frag))
+    return np.array(out)
+
+
 def spin_orbital_spatial_index(frag_sizes):
     """Spatial orbital of every spin orbital (alpha block then beta block per fragment)."""
     out, off = [], 0
