@@ -8,9 +8,12 @@ rotations) when the adjoint is enabled.  `value` is device-resident (inputs in H
 `e2e` goes through the same public API with the states in pinned host memory and the
 energy/gradient copied back every step.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|3] [--precision P]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3|1] [--precision P]
   python bench.py --impl reference ...   (the FP64 CPU oracle on the host cores)
   python bench.py --config 2 ...         (trimer: pair builds + matrix-free H x v Lanczos ground state)
+
+The default workload is the dimer 2 x 14 spatial orbitals / 60 states per charge sector
+(build + state and orbital gradient + step); --config 1 is the 2 x 9 / 10-state dimer.
 
 Multi-GPU: the path does not shard (one dimer), so N>1 runs N independent replicas
 (one per rank, launched by torchrun); value = max time over ranks / iterations of all ranks
@@ -43,10 +46,10 @@ METRIC = "XR-H build+grad s/iter vs plain FP64 GPU, at |dE|<=1e-6 Eh vs FP64 ora
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
+    p.add_argument("--config", type=int, default=3, choices=sorted(CONFIGS))
     p.add_argument("--precision", default="tf32x3")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-variants", action="store_true")
@@ -64,25 +67,126 @@ def make_system(cfg):
 # CPU oracle step (reference arm and cpu_baseline)
 # ------------------------------------------------------------------------------------------
 
-def oracle_step(sysd):
+def _oracle():
     sys.path.insert(0, os.path.join(HERE, "oracle"))
-    import numpy as np
     import xr_oracle as O
+    return O
+
+
+def oracle_step(sysd):
+    """One full FP64 build with the NumPy oracle (the reference's algorithm and contraction
+    order): densities of both fragments (ccaa included, as build_density_tensors.py:122-133
+    builds them), the order-0 XR-H (get_xr_result.py:86-132), the dense eigensolve
+    (mains/workflow.py:229).  Returns (E0, seconds of densities, seconds of H, seconds of
+    the eigensolve)."""
+    import numpy as np
+    O = _oracle()
     charges = list(sysd["charges"])
     ints = O.FragInts(sysd["h"], sysd["V"], sysd["Ns"])
+    t0 = time.perf_counter()
     dens = [O.build_densities({c: O.Sector(*sysd["states"][m][c]) for c in charges}, sysd["n_orb"],
                               sysd["n_core"], sysd["n_elec_ref"]) for m in range(2)]
+    t1 = time.perf_counter()
     H1, H2 = O.get_xr_H0(ints, dens, [charges, charges])
     H = O.full_H(H1, H2)
-    w, v = np.linalg.eigh(H)
-    return float(w[0])
+    t2 = time.perf_counter()
+    w = np.linalg.eigvalsh(H)
+    t3 = time.perf_counter()
+    return float(w[0]), t1 - t0, t2 - t1, t3 - t2
+
+
+def _einsum_rate(n_rows, K, N, reps=2):
+    """FP64 GFLOP/s of the host BLAS on one precontraction-shaped product (n_rows x K) @ (K x N),
+    the dominant contraction shape of the reference's H build (precontract.py:75)."""
+    import numpy as np
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((n_rows, K))
+    B = rng.standard_normal((K, N))
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        A @ B
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return 2.0 * n_rows * K * N / best / 1e9
+
+
+def oracle_sampled_iteration(sysd, h_flops, budget_s=20.0):
+    """Extrapolated FP64 CPU seconds of one build of the reference's algorithm at a size where
+    a full CPU run takes hours (the 2 x 14 / 60-state dimer), from a bounded sample:
+
+    * densities (the dominant CPU cost): every (op, bra charge, ket charge) block the reference
+      builds (build_density_tensors.py:57-160, ccaa included) is built by the oracle for a
+      random subset of the ket configurations (the work is a sum over ket configurations, so
+      it scales with their number) and two bra-state counts (it is linear in them); the time
+      is extrapolated to all configurations and all states, for both fragments;
+    * H: the algorithmic FLOPs of the order-0 build (precontractions, final contractions, and
+      the n^2 N^4 monomer_2e contraction of every stored ccaa block) divided by the host BLAS
+      rate on a precontraction-shaped product;
+    * the dense eigensolve of the full product-basis H (mains/workflow.py:229): symmetric
+      eigvalsh timed at a smaller dimension and scaled by n^3 (a lower bound of the reference's
+      general scipy.linalg.eig).
+    The gradient is not included (the reference's costs two more H builds with determinant
+    densities, state_gradients.py:170-185): the figure is a lower bound of a CPU iteration."""
+    import numpy as np
+    O = _oracle()
+    rng = np.random.default_rng(5)
+    charges = list(sysd["charges"])
+    n_orb, n_core = sysd["n_orb"], sysd["n_core"]
+    N = 2 * n_orb
+    st = sysd["states"][0]
+    blocks = [(op, bc, kc) for bc in charges for kc in charges for op in O.OPS_FOR_DCHG.get(bc - kc, ())]
+    per_block_budget = budget_s / len(blocks)
+    dens_s, detail = 0.0, {}
+    for (op, bc, kc) in blocks:
+        zb, mb = st[bc]
+        zk, mk = st[kc]
+        n_b = zb.shape[0]
+        frac = min(1.0, {1: 0.2, 2: 0.1, 3: 0.03, 4: 0.004}[len(op)])
+        n_sub = max(8, int(frac * len(mk)))
+        sub = np.sort(rng.choice(len(mk), size=min(n_sub, len(mk)), replace=False))
+        nbs = (1, 2) if len(op) == 4 else (2, 4)
+        ts = []
+        for nb in nbs:
+            t0 = time.perf_counter()
+            O.transition_density(op, zb[:nb], mb, zk[:, sub], mk[sub], N, n_orb, n_core)
+            ts.append(time.perf_counter() - t0)
+        slope = max(0.0, (ts[1] - ts[0]) / (nbs[1] - nbs[0]))
+        t_full = (ts[0] + slope * (n_b - nbs[0])) * len(mk) / len(sub)
+        detail[f"{op}({bc},{kc})"] = round(t_full, 3)
+        dens_s += t_full
+        if sum(ts) > per_block_budget:
+            per_block_budget = max(0.5, per_block_budget * 0.8)
+    dens_s *= 2                            # both fragments have the same sizes
+    # monomer_2e on every stored ccaa block: n_b n_k N^4 multiply-adds per charge, both fragments
+    n = {c: st[c][0].shape[0] for c in charges}
+    mono_flops = 2 * sum(2.0 * n[c] * n[c] * N ** 4 for c in charges)
+    rate = _einsum_rate(n[charges[0]] ** 2, N * N, N * N)
+    h_s = (h_flops + mono_flops) / (rate * 1e9)
+    # dense eigensolve of the whole product-basis H
+    dim = sum(n.values()) ** 2
+    m_s = 2000
+    A = rng.standard_normal((m_s, m_s))
+    A = A + A.T
+    t0 = time.perf_counter()
+    np.linalg.eigvalsh(A)
+    eig_s = (time.perf_counter() - t0) * (dim / m_s) ** 3
+    return dict(total=dens_s + h_s + eig_s, densities=dens_s, h_build=h_s, eigensolve=eig_s,
+                blas_gflops=rate, density_blocks_fragment0_s=detail)
 
 
 def time_oracle(sysd, budget_s=30.0):
     t0 = time.perf_counter()
-    e = oracle_step(sysd)
+    e, td, th, te = oracle_step(sysd)
     dt = time.perf_counter() - t0
-    return dt, e
+    return dt, e, dict(densities=td, h_build=th, eigensolve=te)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
 
 
 # ------------------------------------------------------------------------------------------
@@ -195,10 +299,43 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
     return sum(ms) / 1e3 / steps, Es, it
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel (the FP32 density adjoint of
-# one fragment), from one ncu capture of the bench command (profiles/); None where no capture
-# exists for the workload
-DENSITY_ADJ_TRAFFIC_BYTES = {1: 26_176_896}
+# DRAM bytes (read + write) per launch of the dominant kernel, from ncu captures of the bench
+# command (the summaries are in profiles/); None where no capture of the current kernel exists
+DENSITY_ADJ_TRAFFIC = {}
+
+
+def measure_peaks():
+    """Throughput of the arithmetic pipes the SIMT kernels use, measured live like the HBM and
+    BF16 figures of MEASURED_PEAKS.json: the best of 3 CUDA-event-timed torch.matmul calls
+    (cuBLAS) per type -- FP64 (4096^3), FP32 with IEEE products (8192^3, the CUDA-core FMA
+    rate) and TF32 tensor-core (8192^3).  No clock or power setting is touched."""
+    import torch
+    out = {}
+    prev = torch.get_float32_matmul_precision()
+    for name, dtype, n, prec in (("fp64_tflops", torch.float64, 4096, None),
+                                 ("fp32_simt_tflops", torch.float32, 8192, "highest"),
+                                 ("tf32_tflops", torch.float32, 8192, "high")):
+        if prec:
+            torch.set_float32_matmul_precision(prec)
+        a = torch.randn(n, n, dtype=dtype, device="cuda")
+        b = torch.randn(n, n, dtype=dtype, device="cuda")
+        a @ b
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b
+    torch.set_float32_matmul_precision(prev)
+    torch.cuda.empty_cache()
+    out["how"] = "torch.matmul (cuBLAS), best of 3, CUDA events: fp64 4096^3, fp32 IEEE 8192^3, tf32 8192^3"
+    return out
 
 
 def density_adjoint_work(adj, m):
@@ -259,7 +396,7 @@ def dominant_kernel_roofline(it, config, reps=20):
     fl = sum(w[1] for w in work) / len(work)
     kname = ("density_adjoint_units_kernel" if name.endswith("units") else "density_adjoint_f32_grouped_kernel")
     return dict(name=f"{kname} (FP32 density adjoint, one launch per fragment)", ms=ms, bytes=by, flops=fl,
-                traffic=DENSITY_ADJ_TRAFFIC_BYTES.get(config))
+                kernel=kname, traffic=DENSITY_ADJ_TRAFFIC.get((config, kname)))
 
 
 def replica_aggregate(total_ms, e2e_ms, steps, world, device):
@@ -334,6 +471,8 @@ def run_ours(args):
 
     total_ms, e2e_total, s_per_iter, e2e_s_per_iter = replica_aggregate(total_ms, e2e_total, args.steps, world,
                                                                         "cuda")
+    h2d_bytes, d2h_bytes = it.h2d_bytes, it.d2h_bytes
+    residual_last, flops_per_build = it.opt.residual, it.opt.plan.flops
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -341,39 +480,67 @@ def run_ours(args):
 
     peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+    live = measure_peaks()
     dk = dominant_kernel_roofline(it, args.config)
     if dk is not None:
         hbm = float(peaks.get("hbm_gbs", 6800.0))
-        achieved = dk["bytes"] / (dk["ms"] * 1e-3) / 1e9
-        roofline = {"bound": "hbm", "kernel": dk["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                    "frac": achieved / hbm, "traffic": dk["traffic"], "launch_ms": dk["ms"],
+        gbs = dk["bytes"] / (dk["ms"] * 1e-3) / 1e9
+        tflops = dk["flops"] / (dk["ms"] * 1e-3) / 1e12
+        roofline = {"bound": "fp32 (CUDA-core FMA)", "kernel": dk["name"], "achieved": tflops,
+                    "peak": live["fp32_simt_tflops"], "unit": "TFLOP/s", "frac": tflops / live["fp32_simt_tflops"],
+                    "traffic": dk["traffic"], "launch_ms": dk["ms"],
                     "algorithmic_bytes_per_launch": dk["bytes"], "flops_per_launch": dk["flops"],
-                    "fp32_tflops_achieved": dk["flops"] / (dk["ms"] * 1e-3) / 1e12,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy) of measured"
-                    if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
-                    "note": "sparse outer-product accumulation over coupling lists on the CUDA cores (FP32 FMA, "
-                            "coefficient rows gathered from L2): neither HBM- nor tensor-bound; the FP32 rate is "
-                            "given beside the HBM fraction"}
+                    "peak_source": "fp32 IEEE cuBLAS GEMM measured in this run (of measured)",
+                    "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm, "frac": gbs / hbm,
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                            else "fallback 6.8 TB/s (of fallback)"},
+                    "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel in a "
+                                       "capture of the bench command (profiles/)") if dk["traffic"] else
+                                      "null: no ncu capture of the current kernel build at this workload",
+                    "note": "sparse outer products over coupling lists (4 n_b n_k FLOPs and 9 bytes per coupling; "
+                            "coefficient rows gathered from L2): bound by the FP32 pipe, not by HBM or the tensor "
+                            "cores; the HBM fraction is given beside it"}
     else:
         roofline = None
 
     variants = {}
     if not args.no_variants and world == 1:
+        fp64_steps = 3 if args.config == 3 else max(2, args.steps // 2)
         for prec in ("fp64", "bf16x3", "tf32x3"):
             if prec == args.precision:
                 variants[prec] = {"s_per_iter": s_per_iter, "E_first": energies[0]}
                 continue
-            v, Es, _ = time_variant(sysd, prec, max(2, args.steps // 2), args.warmup, l2_flush)
+            v, Es, _ = time_variant(sysd, prec, fp64_steps if prec == "fp64" else max(2, args.steps // 2),
+                                    args.warmup, l2_flush)
             variants[prec] = {"s_per_iter": v}
-        # accuracy at identical states: one build per variant from the initial states
+        del it
+        torch.cuda.empty_cache()
+        it = None
+        # accuracy at identical states: converged ground state of every variant from the initial states
         variants["accuracy"] = accuracy_check(sysd)
     cpu = None
-    if not args.no_cpu_baseline and world == 1 and args.config == 1:
-        dt, e_cpu = time_oracle(sysd)
-        cpu = {"value": dt, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full iteration (densities + H + dense eigensolve, no gradient) of the same workload "
-                         "with the NumPy FP64 oracle, BLAS threads = all cores",
-               "E0": e_cpu}
+    if not args.no_cpu_baseline and world == 1:
+        if args.config == 1:
+            dt, e_cpu, parts = time_oracle(sysd)
+            cpu = {"value": dt, "unit": "s/iter", "cores": cpu_threads(), "kind": "port",
+                   "sample": "one full iteration (densities + H + dense eigensolve, no gradient) of the same "
+                             "workload with the NumPy FP64 oracle, BLAS threads = all cores",
+                   "parts_s": parts, "E0": e_cpu}
+            acc = variants.get("accuracy")
+            if acc:
+                for prec, rec in acc.items():
+                    rec["dE0_vs_oracle"] = abs(rec["E0"] - e_cpu)
+        else:
+            smp = oracle_sampled_iteration(sysd, h_flops_of(sysd, args.config))
+            cpu = {"value": smp["total"], "unit": "s/iter", "cores": cpu_threads(), "kind": "port",
+                   "extrapolated": True,
+                   "sample": "NumPy FP64 oracle (the reference's algorithm) on a bounded sample, extrapolated: every "
+                             "density block of one fragment on a random subset of ket configurations and 1-2 / 2-4 "
+                             "bra states (linear in both), H build = its algorithmic FLOPs at the measured host BLAS "
+                             "rate, dense eigensolve scaled by n^3 from n = 2000; no gradient (a lower bound)",
+                   "parts_s": {k: smp[k] for k in ("densities", "h_build", "eigensolve")},
+                   "blas_gflops": smp["blas_gflops"]}
+    plan_info = h_entries_of(sysd, args.config)
     line = {
         "metric": METRIC, "value": s_per_iter, "unit": "s/iter", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": False,
@@ -383,10 +550,13 @@ def run_ours(args):
                    "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{world}",
                    "step": "one steepest-descent state-optimizer iteration: densities + XR-H build + FP64 Lanczos "
                            "ground state + adjoint state and orbital gradients + Loewdin step"},
-        "e2e": {"value": e2e_s_per_iter, "unit": "s/iter", "h2d_bytes_per_step": it.h2d_bytes,
-                "d2h_bytes_per_step": it.d2h_bytes},
+        "e2e": {"value": e2e_s_per_iter, "unit": "s/iter", "h2d_bytes_per_step": h2d_bytes,
+                "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches, "gpu_launches_per_iteration": per_iter, "roofline": roofline, "clocks": clocks,
-        "energies": energies[:3], "flops_per_build": it.opt.plan.flops, "variants": variants,
+        "h_entries_per_build": plan_info["entries"],
+        "h_entries_per_s": plan_info["entries"] / s_per_iter,
+        "energies": energies[:3], "lanczos_residual_last": residual_last, "flops_per_build": flops_per_build,
+        "peaks_measured": live, "variants": variants,
     }
     if "fp64" in variants and args.precision != "fp64":
         line["speedup_vs_fp64_gpu"] = variants["fp64"]["s_per_iter"] / s_per_iter
@@ -397,21 +567,94 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def h_entries_of(sysd, config):
+    """Entries of the XR-H one build forms: the blocks of every total-charge sector (the
+    blocks between different total charges vanish and are never formed)."""
+    n = [{c: sysd["states"][m][c][0].shape[0] for c in sysd["charges"]} for m in range(2)]
+    sectors = {}
+    for c0, a in n[0].items():
+        for c1, b in n[1].items():
+            sectors[c0 + c1] = sectors.get(c0 + c1, 0) + a * b
+    return {"entries": float(sum(d * d for d in sectors.values())), "sector_dims": sectors}
+
+
+def h_flops_of(sysd, config=None):
+    """Algorithmic FLOPs of one order-0 dimer H build in the reference's contraction order
+    (host arithmetic only): for every charge block with equal total charges, every order-0
+    label and every catalog permutation that the block's charge changes admit
+    (diagrams/S{T,U,V}_diagrams.py), the precontraction once per cache key
+    (precontract.py:80,86: label, fragments, charge pair) and the final contraction, each
+    2 x the product of the extents of its indices; plus t00 / u000 (2 n^2 N^2 per monomer
+    block).  The v0000 monomer term is counted with the density builds (monomer_2e)."""
+    chg = list(sysd["charges"])
+    n = [{c: sysd["states"][m][c][0].shape[0] for c in chg} for m in range(2)]
+    N = 2 * sysd["n_orb"]
+    # (Dchgs, permutations, precontraction index extents (beyond i, j), final extents (beyond ijkl))
+    cat = {"t01": ((-1, +1), ((0, 1), (1, 0)), 2, 1), "u001": ((-1, +1), ((0, 1), (1, 0)), 2, 1),
+           "u101": ((-1, +1), ((0, 1), (1, 0)), 2, 1), "u100": ((0, 0), ((0, 1), (1, 0)), 2, None),
+           "v0101": ((0, 0), ((0, 1),), 4, 2), "v0001": ((-1, +1), ((0, 1), (1, 0)), 4, 1),
+           "v0100": ((+1, -1), ((0, 1), (1, 0)), 4, 1), "v0011": ((-2, +2), ((0, 1), (1, 0)), 4, 2)}
+    flops, seen = 0.0, set()
+    for ci0 in chg:
+        for ci1 in chg:
+            for cj0 in chg:
+                for cj1 in chg:
+                    if ci0 + ci1 != cj0 + cj1:
+                        continue
+                    pairs = ((ci0, cj0), (ci1, cj1))
+                    for lab, (dch, perms, pre_ext, fin_ext) in cat.items():
+                        for perm in perms:
+                            pc = tuple(pairs[k] for k in perm)
+                            if not all(pc[k][0] - pc[k][1] == dch[k] for k in range(2)):
+                                continue
+                            A, B = perm
+                            nai, naj = n[A][pc[0][0]], n[A][pc[0][1]]
+                            nbi, nbj = n[B][pc[1][0]], n[B][pc[1][1]]
+                            key = (lab, A, pc[0])
+                            if key not in seen:
+                                seen.add(key)
+                                flops += 2.0 * nai * naj * N ** pre_ext
+                            if fin_ext is not None:
+                                flops += 2.0 * nai * naj * nbi * nbj * N ** fin_ext
+    for m in range(2):
+        for c in chg:
+            flops += 2 * 2.0 * n[m][c] ** 2 * N ** 2          # t00 and u000
+    return flops
+
+
 def accuracy_check(sysd):
-    """|E0(variant) - E0(fp64)| and max|H(variant) - H(fp64)| for the initial states."""
+    """Every variant against FP64 at the initial states, with converged eigenpairs (restarted
+    Lanczos to a residual of 1e-9): |dE0|, max |dH| over the sector matrices, and the relative
+    errors of the tangent state gradient and of dE/dkappa."""
     import torch
-    from qodeapplications_gb300.iteration import XRStateOptimizer
+    from qodeapplications_gb300 import synthetic as S
+    from qodeapplications_gb300.autograd import XRDimerEnergy
+    from qodeapplications_gb300.gradients import tangent_project
+    chg = list(sysd["charges"])
     out, ref = {}, None
+    sidx = S.spin_orbital_spatial_index([sysd["n_orb"]] * 2)
     for prec in ("fp64", "bf16x3", "tf32x3"):
-        opt = XRStateOptimizer(sysd, precision=prec, orbital_gradient=False, use_graphs=False)
-        E = opt.iterate()
-        H = {t: sec["H"].clone() for t, sec in opt.plan.sectors.items()}
+        eng = XRDimerEnergy.from_system(sysd, precision=prec, tol=1e-9)
+        h = torch.as_tensor(sysd["h"], device="cuda")
+        V = torch.as_tensor(sysd["V"], device="cuda")
+        z = [{c: torch.as_tensor(sysd["states"][m][c][0], device="cuda") for c in chg} for m in range(2)]
+        E = float(eng(h, V, z))
+        eng.adj.launch(eng.d_product)
+        g = eng.adj.state_gradient()
+        gt = torch.cat([tangent_project(g[m][c], z[m][c]).reshape(-1) for m in range(2) for c in chg])
+        T = h.contiguous()
+        kg = eng.adj.orbital_gradient(T, torch.zeros((2,) + T.shape, dtype=torch.float64, device="cuda"),
+                                      V.contiguous(), sidx).clone()
+        Hs = {t: sec["H"].clone() for t, sec in eng.plan.sectors.items()}
+        rec = {"E0": E, "lanczos_residual": eng.residual}
         if ref is None:
-            ref = (E, H)
-            continue
-        out[prec] = {"dE0": abs(E - ref[0]),
-                     "max_dH": max(float((H[t] - ref[1][t]).abs().max()) for t in H)}
-        del opt
+            ref = (E, Hs, gt.clone(), kg)
+        else:
+            rec.update(dE0=abs(E - ref[0]), max_dH=max(float((Hs[t] - ref[1][t]).abs().max()) for t in Hs),
+                       state_grad_rel=float((gt - ref[2]).norm() / ref[2].norm()),
+                       orbital_grad_rel=float((kg - ref[3]).norm() / ref[3].norm()))
+        out[prec] = rec
+        del eng, Hs
         torch.cuda.empty_cache()
     return out
 
@@ -555,20 +798,33 @@ def run_reference(args):
                           "H, 1.7 M x 1.7 M at this size (23 TB in FP64); no CPU run of it is possible"}))
         return
     sysd = make_system(args.config)
-    times = []
+    times, extra = [], {}
     n_timed = min(args.steps, 2)      # each oracle iteration takes tens of seconds: keep the run to minutes
     for _ in range(n_timed):
-        dt, e = time_oracle(sysd)
+        if args.config == 1:
+            dt, e, parts = time_oracle(sysd)
+            extra = {"E0": e, "parts_s": parts}
+            sample = (f"{n_timed} full iteration(s) of the workload (densities + H + dense eigensolve, no "
+                      "gradient) with the NumPy FP64 oracle (restatement of the reference; the reference's own "
+                      "Python path needs Qode)")
+        else:
+            smp = oracle_sampled_iteration(sysd, h_flops_of(sysd))
+            dt = smp["total"]
+            extra = {"extrapolated": True, "parts_s": {k: smp[k] for k in ("densities", "h_build", "eigensolve")},
+                     "blas_gflops": smp["blas_gflops"]}
+            sample = (f"{n_timed} bounded sample(s) of the workload with the NumPy FP64 oracle, extrapolated to the "
+                      "full size: every density block on a random subset of ket configurations and 1-4 bra states, "
+                      "H build = its algorithmic FLOPs at the measured host BLAS rate, dense eigensolve scaled by "
+                      "n^3; no gradient (a lower bound of a reference iteration)")
         times.append(dt)
     v = sum(times) / len(times)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded system)",
             "config": {"workload": CONFIGS[args.config]["name"], "step": "densities + H build + FP64 eigensolve"},
-            "cpu_baseline": {"value": v, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{n_timed} full iteration(s) of the workload with the NumPy FP64 oracle "
-                                       "(restatement of the reference; the reference's own Python path needs Qode)"},
-            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}, "E0": e}
+            "cpu_baseline": dict({"value": v, "unit": "s/iter", "cores": cpu_threads(), "kind": "port",
+                                  "sample": sample}, **extra),
+            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
