@@ -216,6 +216,9 @@ class SigmaBatch:
     def __init__(self, items, device):
         self.items = items
         self.tc = bool(items) and items[0][0].tc
+        if not items:
+            self.reg = None
+            return
         self.scatter = _lib.PairLaunch([(sg.pl, sg.off_dev, sg.stride_dev, zT, sg.D, sg.n) for sg, zT in items],
                                        False, device)
         self.gather = _lib.PairLaunch([(sg.pl, sg.off_dev, sg.stride_dev, sg.E, sg.sigmaT, sg.n)
@@ -334,6 +337,10 @@ class XRDimerPlan:
               the gauge (-1)^(n_i1 + n_j0)).
     builders: two DensityBuilder objects shared with other plans (built by their owner;
               launch(build_densities=False)), or None for the plan's own.
+    monomer_2e: how the monomer two-electron term v0000 is formed: 'sigma' (the default:
+              sigma vectors through (n-2)-electron pair intermediates, rho^ccaa never
+              stored), 'ccaa' (a stored rho^ccaa block per charge, contracted with V as
+              SV_1mer_0.py:24 does; for densities handed in by a caller) or 'none'.
 
     The inputs are the persistent coefficient buffers self.coeffs[m][charge]
     (n_states x n_conf); launch() enqueues the whole build on the current stream without
@@ -342,7 +349,10 @@ class XRDimerPlan:
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
                  convention="hermitian", layout="product", dens_precision=None, sigma_precision=None,
-                 autotune=True, builders=None):
+                 autotune=True, builders=None, monomer_2e="sigma"):
+        if monomer_2e not in ("sigma", "ccaa", "none"):
+            raise ValueError("monomer_2e must be 'sigma', 'ccaa' or 'none'")
+        self.monomer_2e = monomer_2e
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
         self.ints = ints
@@ -451,18 +461,23 @@ class XRDimerPlan:
                     continue
                 n = ns[m][c]
                 ca = rho[m]["ca"][(c, c)]
-                sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m),
-                                      precision=_lib.PRECISIONS[self.sigma_precision], own_gemm=False)
-                self.sigma[m][c] = sg
-                nconf = spaces[m].n_conf[c]
-                zrow = self.coeffs[m][c]
+                if monomer_2e == "sigma":
+                    sg = SigmaTwoElectron(spaces[m], c, n, ints.V(m, m, m, m),
+                                          precision=_lib.PRECISIONS[self.sigma_precision], own_gemm=False)
+                    self.sigma[m][c] = sg
+                    nconf = spaces[m].n_conf[c]
+                    zrow = self.coeffs[m][c]
                 targets_h1 = [self.H1blk[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
                 targets_du = [self.DU[m][c]] + ([self.FULLD[m][c]] if output == "full" else [])
                 for tgt in targets_h1:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("hmm", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))
-                    mono.append((n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n,
-                                 _splitk(nconf, target=128, cap=512)))
+                    if monomer_2e == "sigma":
+                        mono.append((n, n, [(zrow, nconf, sg.sigmaT, nconf, nconf, 1.0)], tgt, n,
+                                     _splitk(nconf, target=128, cap=512)))
+                    elif monomer_2e == "ccaa":
+                        mono.append((n * n, 1, [(rho[m]["ccaa"][(c, c)], N[m] ** 4, W[("vmmmm", m)], N[m] ** 4,
+                                                 N[m] ** 4, 1.0)], tgt, 1, _splitk(N[m] ** 4)))
                 for tgt in targets_du:
                     mono.append((n * n, 1, [(ca, N[m] ** 2, W[("u100", m)], N[m] ** 2, N[m] ** 2, 1.0)], tgt, 1,
                                  _splitk(N[m] ** 2)))
@@ -641,6 +656,9 @@ class XRDimerPlan:
             W[("cc", m)] = ints.V(m, m, o, o).permute(3, 2, 0, 1).reshape(N[o] ** 2, N[m] ** 2).contiguous()
             W[("hmm", m)] = (ints.T(m, m) + ints.U(m, m, m)).reshape(1, N[m] ** 2).contiguous()
             W[("u100", m)] = ints.U(o, m, m).reshape(1, N[m] ** 2).contiguous()
+            if getattr(self, "monomer_2e", "sigma") == "ccaa":
+                # v0000 on a stored rho^ccaa[i, j, p, q, s, r]: the weights V_pqrs in (p, q, s, r) order
+                W[("vmmmm", m)] = ints.V(m, m, m, m).permute(0, 1, 3, 2).reshape(1, N[m] ** 4).contiguous()
         return W
 
     def set_integrals(self, ints):
@@ -673,7 +691,7 @@ class XRDimerPlan:
             for c, sg in self.sigma[m].items():
                 if sg.pl is None:
                     sg.run_sigma(self.builders[m].zT[c])
-        self.arena.buf.zero_()
+        _lib.zero_(self.arena.buf)
         s = stream_ptr()
         if self.mono_gemv_tasks is not None:
             gtd, n_g, rows8 = self.mono_gemv_tasks
@@ -727,7 +745,8 @@ class XRDimerPlan:
         self.sigma_batch.check()
 
 
-def lowest_eigenpairs(H, k=5):
-    """Lowest k eigenvalues/vectors of the symmetric excitonic H in FP64 on the GPU."""
-    w, v = torch.linalg.eigh(0.5 * (H + H.t()))
-    return w[:k], v[:, :k]
+def lowest_eigenpairs(H, k=5, tol=1e-10):
+    """Lowest k eigenvalues (numpy) and eigenvectors (device) of the symmetric excitonic H
+    in FP64 on the GPU, by this library's Lanczos loop (eigen.lowest_eigenpairs)."""
+    from .eigen import lowest_eigenpairs as _lanczos_pairs
+    return _lanczos_pairs(H, k=k, tol=tol)
