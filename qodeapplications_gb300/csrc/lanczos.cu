@@ -275,8 +275,9 @@ __global__ void __launch_bounds__(256) gemv_rows_grouped_kernel(const xrh_gemv_t
 // sums are reduced by warps in a fixed order, identical in every CTA, so all CTAs hold the same
 // coefficients and results do not depend on scheduling.  V is written by every CTA and read
 // by all, so its global reads bypass L1 (ld.global.cg).  Barrier k waits until a counter
-// reaches (k+1) * gridDim.x; a wait that exceeds LC_WAIT_LIMIT polls sets XRH_ERR_TIMEOUT in
-// *status and the CTA returns.
+// reaches (k+1) * gridDim.x; a wait that exceeds wait_limit polls (LC_WAIT_LIMIT unless the
+// caller of xrh_lanczos_coop_bounded gives another) sets XRH_ERR_TIMEOUT in *status and the CTA
+// returns; every later barrier of the other CTAs then returns too.
 constexpr int LC_THREADS = 256;
 constexpr int LC_WARPS = LC_THREADS / 32;
 constexpr int LC_MAX_CTAS = 256;
@@ -290,7 +291,8 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
 }
 
 // Returns false (all threads of the CTA) when the wait gave up or another CTA already failed.
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, int32_t* status) {
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, int32_t* status,
+                                             long long wait_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -299,7 +301,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int t
         atomicAdd(count, 1u);
         long long it = 0;
         while (ld_acquire_u32(count) < target) {
-            if (++it > LC_WAIT_LIMIT) { ok = 0; break; }
+            if (++it > wait_limit) { ok = 0; break; }
             __nanosleep(20);
         }
         if (!ok) atomicExch(status, XRH_ERR_TIMEOUT);
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
                                                                 double* __restrict__ V, double* __restrict__ alpha,
                                                                 double* __restrict__ beta, double* __restrict__ part,
                                                                 unsigned int* count, int32_t* status, int rows_max,
-                                                                int stage_v) {
+                                                                int stage_v, long long wait_limit) {
     extern __shared__ double sm[];
     const unsigned int nb = gridDim.x, b = blockIdx.x;
     const int64_t r0 = (int64_t)b * n / nb, r1 = (int64_t)(b + 1) * n / nb;
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
         V[r0 + r] = x;
         Vs[r] = x;
     }
-    if (!grid_barrier(count, ++bar * nb, status)) return;
+    if (!grid_barrier(count, ++bar * nb, status, wait_limit)) return;
     for (int j = 0; j < m; ++j) {
         const double* vj = V + (int64_t)j * n;
         if (stage_v) {
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
                 if (lane == 0) pp[(int64_t)i * nb + b] = s;
             }
-            if (!grid_barrier(count, ++bar * nb, status)) return;
+            if (!grid_barrier(count, ++bar * nb, status, wait_limit)) return;
             reduce_partials(pp, nb, cnt, c);
             __syncthreads();
             a += c[j];
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
             alpha[j] = a;
             beta[j] = bj;
         }
-        if (!grid_barrier(count, ++bar * nb, status)) return;
+        if (!grid_barrier(count, ++bar * nb, status, wait_limit)) return;
     }
 }
 
@@ -675,10 +677,10 @@ extern "C" int64_t xrh_lanczos_coop_work(int m) {
     return (int64_t)LC_MAX_CTAS * 2 * (int64_t)(m + 2) + 2;
 }
 
-extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
-                                double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
-                                int64_t work_len, int32_t* status_dev, void* stream) {
-    if (n <= 0 || m <= 0 || ld < n) return XRH_ERR_ARG;
+static int lanczos_coop_launch(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                               double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                               int64_t work_len, int32_t* status_dev, long long wait_limit, void* stream) {
+    if (n <= 0 || m <= 0 || ld < n || wait_limit < 0) return XRH_ERR_ARG;
     if (!H_dev || !v0_dev || !V_dev || !alpha_dev || !beta_dev || !work_dev || !status_dev) return XRH_ERR_ARG;
     if (work_len < xrh_lanczos_coop_work(m)) return XRH_ERR_CAPACITY;
     int dev = 0, sms = 0, per_sm = 0, smem_optin = 0;
@@ -716,8 +718,10 @@ extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t l
     if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return XRH_ERR_CUDA;
     int64_t n_arg = n, ld_arg = ld;
     int m_arg = m, rows_arg = (int)rows_max, stage_arg = stage_v;
-    void* args[] = {&n_arg, &m_arg, (void*)&H_dev, &ld_arg, (void*)&v0_dev, (void*)&V_dev, (void*)&alpha_dev,
-                    (void*)&beta_dev, (void*)&part, (void*)&count, (void*)&status_dev, &rows_arg, &stage_arg};
+    long long limit_arg = wait_limit;
+    void* args[] = {&n_arg,         &m_arg,       (void*)&H_dev, &ld_arg,           (void*)&v0_dev,
+                    (void*)&V_dev,  (void*)&alpha_dev, (void*)&beta_dev, (void*)&part, (void*)&count,
+                    (void*)&status_dev, &rows_arg, &stage_arg,  &limit_arg};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_coop_kernel, dim3((unsigned)nb),
                                                       dim3(LC_THREADS), args, smem, s);
     if (e != cudaSuccess) {
@@ -725,6 +729,20 @@ extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t l
         return XRH_ERR_CUDA;
     }
     return XRH_OK;
+}
+
+extern "C" int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                                double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                                int64_t work_len, int32_t* status_dev, void* stream) {
+    return lanczos_coop_launch(n, m, H_dev, ld, v0_dev, V_dev, alpha_dev, beta_dev, work_dev, work_len, status_dev,
+                               LC_WAIT_LIMIT, stream);
+}
+
+extern "C" int xrh_lanczos_coop_bounded(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                                        double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                                        int64_t work_len, int32_t* status_dev, int64_t max_polls, void* stream) {
+    return lanczos_coop_launch(n, m, H_dev, ld, v0_dev, V_dev, alpha_dev, beta_dev, work_dev, work_len, status_dev,
+                               (long long)max_polls, stream);
 }
 
 // Shared memory (bytes) of the cluster loop for a given split; 0 when it does not fit.
