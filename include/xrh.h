@@ -79,9 +79,11 @@ int xrh_density_accumulate(int precision, int64_t K, const int64_t* idx_ptr_dev,
 
 /* FP32 variant of xrh_density_accumulate for the split-precision paths: coefficients given
  * pre-converted to FP32 as zb32 [n_bra_conf, round_up(n_b,4)] and zk32 [n_ket_conf,
- * round_up(n_k,4)] (rows padded with zeros, 16-byte aligned); FP32 products and chunk sums,
- * FP64 running sums.  splits > 1 divides the couplings of every operator index over that
- * many CTAs and ADDS to rhoT_dev, which must then be zeroed by the caller. */
+ * round_up(n_k,4)] (rows padded with zeros, 16-byte aligned); FP32 products and stage sums,
+ * running sums as FP32 (hi, lo) pairs.  The couplings of every operator index must come
+ * positive signs first (the order FragmentSpace builds): the kernel multiplies each sign range
+ * with a uniform sign.  splits > 1 divides the couplings of every operator index over that
+ * many CTAs and ADDS to rhoT_dev, which must then be zeroed by the caller.  n_b, n_k <= 1024. */
 int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* idx_ptr_dev, const int32_t* P_dev,
                                const int32_t* Q_dev, const int8_t* sign_dev, const float* zb32_dev, int n_b,
                                const float* zk32_dev, int n_k, double* rhoT_dev, void* stream);
@@ -319,6 +321,14 @@ int64_t xrh_lanczos_coop_work(int m);
 int xrh_lanczos_coop(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
                      double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
                      int64_t work_len, int32_t* status_dev, void* stream);
+/* xrh_lanczos_coop with the grid barriers' wait bound given by the caller: a CTA that has
+ * polled max_polls times without the others arriving writes XRH_ERR_TIMEOUT to *status_dev
+ * and returns, and the other CTAs return at their next barrier (max_polls = 0: a CTA gives
+ * up unless every other CTA has already arrived, so any launch of two or more CTAs reports
+ * XRH_ERR_TIMEOUT; for tests of the failure path).  No reference counterpart. */
+int xrh_lanczos_coop_bounded(int64_t n, int m, const double* H_dev, int64_t ld, const double* v0_dev,
+                             double* V_dev, double* alpha_dev, double* beta_dev, double* work_dev,
+                             int64_t work_len, int32_t* status_dev, int64_t max_polls, void* stream);
 
 /* The optimizer's state update for every (fragment, charge) block at once; replaces the
  * per-fragment NumPy step of StateSpaceOptimizer/state_solver.py:207-453 (tangent
@@ -600,6 +610,78 @@ int xrh_tc_encode_map(int precision, const void* base_dev, int64_t rows, int64_t
 int xrh_gemm_tc_grouped(int precision, const xrh_tc_task* tasks_dev, int n_tasks, int64_t total_tiles,
                         const xrh_tc_segment* segs_dev, const void* maps_dev, int32_t* status_dev,
                         void* stream);
+
+/* Small dense FP64 matrices of the orbital transformation (n <= 64, row-major, one CTA each;
+ * XRH_ERR_CAPACITY above):
+ *   xrh_inverse_small: Ainv = A^-1 by Gauss-Jordan with partial pivoting; *status_dev = 0, or 1
+ *       for a pivot below 1e-300 (Ainv then undefined).  Replaces the overlap inverse of the
+ *       biorthogonalisation, direct_Sinv (hermitian-XRCC/get_ints.py:62-66).
+ *   xrh_expm_small: E = exp(A) by scaling and squaring with a degree-16 Taylor polynomial: the
+ *       orbital rotation R = exp(kappa) (no reference counterpart: the reference's orbital
+ *       solver rotates with the first-order I + s x, StateSpaceOptimizer/orbital_solver.py:431).
+ *   xrh_spin_block: out[a, b] = in[sidx[a], sidx[b]] if spin[a] == spin[b] else 0, the
+ *       spin-orbital form of a spatial matrix (no reference counterpart: qode's
+ *       spin_orb_integrals, hermitian-XRCC/get_ints.py:134-135, does this on the host). */
+int xrh_inverse_small(int n, const double* A_dev, int64_t lda, double* Ainv_dev, int64_t ldi,
+                      int32_t* status_dev, void* stream);
+int xrh_expm_small(int n, const double* A_dev, int64_t lda, double* E_dev, int64_t lde, void* stream);
+int xrh_spin_block(int n_so, const int32_t* sidx_dev, const int8_t* spin_dev, const double* in_dev, int64_t ldin,
+                   double* out_dev, int64_t ldout, void* stream);
+/* out[i, j] = in[idx[i], idx[j]], i, j < n: a principal submatrix (the alpha-alpha block of
+ * a spin-orbital overlap before its inverse; no reference counterpart). */
+int xrh_gather_submatrix(int n, const int32_t* idx_dev, const double* in_dev, int64_t ldin, double* out_dev,
+                         int64_t ldout, void* stream);
+
+/* Helpers of the device-resident optimizer iteration (no reference counterpart; they keep
+ * PyTorch and library kernels out of the captured iteration):
+ *   xrh_zero: cudaMemsetAsync of bytes at ptr_dev;
+ *   xrh_index_move: dst[idx[i]] = src[i] (gather = 0) or dst[i] = src[idx[i]] (gather = 1),
+ *       i < n (a scatter's indices distinct);
+ *   xrh_spin_sum_antisym: out[a, b] = sum_k (G[s_k(a), s_k(b)] - G[s_k(b), s_k(a)]) with
+ *       s_k(a) = so[k * n_sp + a] the spin orbital of spatial orbital a in spin block k: the
+ *       antisymmetric spatial orbital gradient from the spin-orbital one;
+ *   xrh_small_mm_grouped: C = alpha A B + beta I for n x n row-major FP64 blocks, n <= 64, task
+ *       t owning CTAs [cta_begin, cta_begin + ceil(n / 4)) (sorted, total_ctas the sum) -- the
+ *       Newton-Schulz steps of the Loewdin orthonormalisation of every state block at once. */
+typedef struct {
+    const double* A;
+    const double* B;
+    double* C;
+    int32_t n, reserved;
+    double alpha, beta;
+    int64_t cta_begin;
+} xrh_small_mm_task;   /* 56 bytes */
+int xrh_zero(void* ptr_dev, int64_t bytes, void* stream);
+int xrh_index_move(int64_t n, const int64_t* idx_dev, const double* src_dev, double* dst_dev, int gather,
+                   void* stream);
+int xrh_spin_sum_antisym(int n_sp, int n_spin, const int32_t* so_dev, const double* G_dev, int64_t ldg,
+                         double* out_dev, void* stream);
+int xrh_small_mm_grouped(const xrh_small_mm_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
+
+/* Reordering of the three-fragment vectors of the matrix-free H x v (no reference
+ * counterpart: the reference forms the dense product-basis H, general-XRCC/hamiltonian.py:18-80):
+ *   xrh_permute_grouped: task t writes dst[e] = scale * src[sum_k i_k src_stride[k]] for the
+ *       row-major multi-index (i_0 .. i_{ndim-1}) of element e over dst_shape (ndim <= 6),
+ *       e < n_elems; its elements are [elem_begin, elem_begin + n_elems) of the launch (tasks
+ *       sorted by elem_begin, total_elems the sum);
+ *   xrh_gather_sum: dst[j] = (accumulate ? dst[j] : 0) + sum_t src_t[idx_t[j]], t < n_terms <= 8,
+ *       j < n, added in term order (deterministic; no atomics). */
+typedef struct {
+    const double* src;
+    double* dst;
+    int64_t dst_shape[6];
+    int64_t src_stride[6];
+    int32_t ndim, reserved;
+    double scale;
+    int64_t elem_begin, n_elems;
+} xrh_permute_task;   /* 144 bytes */
+int xrh_permute_grouped(const xrh_permute_task* tasks_dev, int n_tasks, int64_t total_elems, void* stream);
+typedef struct {
+    const double* src[8];
+    const int64_t* idx[8];
+    int32_t n_terms, reserved;
+} xrh_gather_terms;   /* 136 bytes, passed by host pointer (the kernel receives a copy) */
+int xrh_gather_sum(int64_t n, const xrh_gather_terms* terms, double* dst_dev, int accumulate, void* stream);
 
 #ifdef __cplusplus
 }

@@ -35,6 +35,7 @@ _SIGS = {
     "xrh_lanczos_cluster": (_i32, [_i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _vp]),
     "xrh_lanczos_cluster_fits": (_i32, [_i32, _i32, _i32]),
     "xrh_lanczos_coop": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "xrh_lanczos_coop_bounded": (_i32, [_i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
     "xrh_state_ctas": (_i32, [_i64]),
     "xrh_abt_ctas": (_i32, [_i64]),
     "xrh_split_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp]),
@@ -79,6 +80,16 @@ _SIGS = {
     "xrh_split_operand": (_i32, [_i32, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),
     "xrh_tc_encode_map": (_i32, [_i32, _vp, _i64, _i64, _i32, _vp]),
     "xrh_gemm_tc_grouped": (_i32, [_i32, _vp, _i32, _i64, _vp, _vp, _vp, _vp]),
+    "xrh_inverse_small": (_i32, [_i32, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "xrh_expm_small": (_i32, [_i32, _vp, _i64, _vp, _i64, _vp]),
+    "xrh_spin_block": (_i32, [_i32, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "xrh_gather_submatrix": (_i32, [_i32, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "xrh_zero": (_i32, [_vp, _i64, _vp]),
+    "xrh_index_move": (_i32, [_i64, _vp, _vp, _vp, _i32, _vp]),
+    "xrh_spin_sum_antisym": (_i32, [_i32, _i32, _vp, _vp, _i64, _vp, _vp]),
+    "xrh_small_mm_grouped": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_permute_grouped": (_i32, [_vp, _i32, _i64, _vp]),
+    "xrh_gather_sum": (_i32, [_i64, _vp, _vp, _i32, _vp]),
 }
 _OPTIONAL = {}
 
@@ -118,7 +129,7 @@ class LaunchCounter:
     except the host-only ones below launches one kernel of this library (those in `multi` the
     number given)."""
     multi = {"xrh_orbital_terms": 2, "xrh_gemv_rows_split": 2, "xrh_lanczos_normalize_split": 2}
-    host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems",
+    host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems", "xrh_zero",
                  "xrh_tc_encode_map", "xrh_state_ctas", "xrh_abt_ctas", "xrh_lanczos_coop_work",
                  "xrh_lanczos_cluster_fits", "xrh_gemv_split_work"}
     count = 0
@@ -208,6 +219,17 @@ STATE_TASK_DTYPE = np.dtype([("gT", np.uint64), ("gT32", np.uint64), ("z", np.ui
                              ("S", np.uint64), ("M", np.uint64), ("K", np.int64), ("n", np.int32),
                              ("reserved", np.int32), ("cta_begin", np.int64)])
 assert STATE_TASK_DTYPE.itemsize == 80
+SMALL_MM_TASK_DTYPE = np.dtype([("A", np.uint64), ("B", np.uint64), ("C", np.uint64), ("n", np.int32),
+                                ("reserved", np.int32), ("alpha", np.float64), ("beta", np.float64),
+                                ("cta_begin", np.int64)])
+assert SMALL_MM_TASK_DTYPE.itemsize == 56
+PERMUTE_TASK_DTYPE = np.dtype([("src", np.uint64), ("dst", np.uint64), ("dst_shape", np.int64, 6),
+                               ("src_stride", np.int64, 6), ("ndim", np.int32), ("reserved", np.int32),
+                               ("scale", np.float64), ("elem_begin", np.int64), ("n_elems", np.int64)])
+assert PERMUTE_TASK_DTYPE.itemsize == 144
+GATHER_TERMS_DTYPE = np.dtype([("src", np.uint64, 8), ("idx", np.uint64, 8), ("n_terms", np.int32),
+                               ("reserved", np.int32)])
+assert GATHER_TERMS_DTYPE.itemsize == 136
 TASK_DTYPE = np.dtype([("M", np.int64), ("N", np.int64), ("seg_begin", np.int64), ("seg_count", np.int64),
                        ("mode", np.int64), ("splitk", np.int64), ("tile_begin", np.int64), ("C", np.uint64),
                        ("ldc", np.int64), ("rowA", np.uint64), ("colA", np.uint64), ("rowB", np.uint64),
@@ -288,3 +310,10 @@ class PairLaunch:
     def run(self, stream=None):
         if self.n:
             call("xrh_pair_grouped", self.gather, ptr(self.dev), self.n, self.max_total, stream_ptr(stream))
+
+
+def zero_(t):
+    """t[...] = 0 by cudaMemsetAsync on the current stream (no kernel; a memset node inside a
+    captured graph)."""
+    call("xrh_zero", ptr(t), t.numel() * t.element_size(), stream_ptr())
+    return t

@@ -42,3 +42,6 @@ static_assert(sizeof(xrh_split_task) == 64, "xrh_split_task layout is part of th
 static_assert(sizeof(xrh_dens_unit) == 16, "xrh_dens_unit layout is part of the ABI");
 static_assert(sizeof(xrh_state_task) == 80, "xrh_state_task layout is part of the ABI");
 static_assert(sizeof(xrh_tc_task) == 144, "xrh_tc_task layout is part of the ABI");
+static_assert(sizeof(xrh_small_mm_task) == 56, "xrh_small_mm_task layout is part of the ABI");
+static_assert(sizeof(xrh_permute_task) == 144, "xrh_permute_task layout is part of the ABI");
+static_assert(sizeof(xrh_gather_terms) == 136, "xrh_gather_terms layout is part of the ABI");

@@ -90,20 +90,43 @@ __device__ __forceinline__ void atomic_add4(float* dst, const float (&v)[4], int
     }
 }
 
+// Couplings per stage of the FP32 adjoint: the work items of a stage, (C/4) x (n_k/4 + n_b/4)
+// register tiles, about one per thread (C a multiple of 4, 4..128), so a stage keeps every
+// thread busy for any state count, and the staging buffers hold about 4 x 256 x 4 floats.
+__host__ __device__ __forceinline__ int adj_chunk(int nbp, int nkp) {
+    int c = 4 * (kAdjThreads / ((nbp >> 2) + (nkp >> 2)));
+    return c < 4 ? 4 : (c > 128 ? 128 : c);
+}
+
+// Shared memory (bytes) of the FP32 adjoint for the largest n_b, n_k of a launch: G in both
+// orientations plus two stages of gathered rows (at most 2 x 4096 floats, see adj_chunk).
+static size_t adj_f32_smem(int max_nb, int max_nk) {
+    const int nbp = (max_nb + 3) & ~3, nkp = (max_nk + 3) & ~3;
+    size_t stage = 0;
+    for (int b = 4; b <= nbp; b += 4)           // the largest C (nbp' + nkp') over the smaller tasks
+        for (int k = 4; k <= nkp; k += 4) {
+            const size_t v = (size_t)adj_chunk(b, k) * (b + k);
+            stage = v > stage ? v : stage;
+        }
+    return sizeof(float) * (2 * (size_t)nbp * nkp + 2 * stage);
+}
+
+// One CTA per operator index.  G[idx] is staged in shared memory in both orientations; the
+// couplings are streamed in stages of C (adj_chunk): the coefficient rows of stage k+1 are
+// gathered with cp.async while stage k is multiplied, with ONE barrier per stage (the buffer a
+// gather overwrites was read in the stage before that barrier).  Signs, P and Q of a work item
+// come from global memory (L1) when its results go out, so no index array sits in shared
+// memory between barriers.
 __device__ __forceinline__ void density_adjoint_f32_body(
     int64_t idx, const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
     const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT, unsigned char* smem_raw) {
-    // coefficient rows come pre-converted to FP32 and padded to nbp/nkp (16-byte rows), so the
-    // z rows of a chunk are gathered with cp.async into a double-buffered ring while the
-    // previous chunk is multiplied
     const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
+    const int C = adj_chunk(nbp, nkp);
     float* g = reinterpret_cast<float*>(smem_raw);          // [nbp][nkp]
     float* gt = g + nbp * nkp;                              // [nkp][nbp]
-    float* zb_s = gt + nkp * nbp;                           // [2][chunk][nbp]
-    float* zk_s = zb_s + 2 * kAdjChunk * nbp;               // [2][chunk][nkp]
-    __shared__ int sP[2][kAdjChunk], sQ[2][kAdjChunk];
-    __shared__ float sS[2][kAdjChunk];
+    float* zb_s = gt + nkp * nbp;                           // [2][C][nbp]
+    float* zk_s = zb_s + 2 * C * nbp;                       // [2][C][nkp]
     const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
     if (c_begin == c_end) return;
     const double* gi = gT + idx * (int64_t)nb * nk;
@@ -113,123 +136,81 @@ __device__ __forceinline__ void density_adjoint_f32_body(
         g[t] = v;
         gt[j * nbp + i] = v;
     }
-    const int n_chunks = (int)((c_end - c_begin + kAdjChunk - 1) / kAdjChunk);
+    const int n_chunks = (int)((c_end - c_begin + C - 1) / C);
     const int gb = nbp / 4, gk = nkp / 4;
-    auto load_idx = [&](int k, int buf) {
-        const int64_t c0 = c_begin + (int64_t)k * kAdjChunk;
-        for (int t = threadIdx.x; t < kAdjChunk; t += blockDim.x) {
-            const int64_t c = c0 + t;
-            const bool ok = c < c_end;
-            sP[buf][t] = ok ? P[c] : -1;
-            sQ[buf][t] = ok ? Q[c] : -1;
-            sS[buf][t] = ok ? (sgn[c] < 0 ? -1.f : 1.f) : 0.f;
-        }
-    };
-    auto stage = [&](int buf) {
-        float* zbb = zb_s + buf * kAdjChunk * nbp;
-        float* zkb = zk_s + buf * kAdjChunk * nkp;
-        for (int x = threadIdx.x; x < kAdjChunk * gb; x += blockDim.x) {
+    auto stage = [&](int k, int buf) {
+        const int64_t c0 = c_begin + (int64_t)k * C;
+        float* zbb = zb_s + buf * C * nbp;
+        float* zkb = zk_s + buf * C * nkp;
+        for (int x = threadIdx.x; x < C * gb; x += blockDim.x) {
             const int c = x / gb, part = x - c * gb;
-            const int p = sP[buf][c];
-            if (p >= 0) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)p * nbp + part * 4);
+            const int64_t cc = c0 + c;
+            if (cc < c_end) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)__ldg(P + cc) * nbp + part * 4);
             else *reinterpret_cast<float4*>(zbb + c * nbp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        for (int x = threadIdx.x; x < kAdjChunk * gk; x += blockDim.x) {
+        for (int x = threadIdx.x; x < C * gk; x += blockDim.x) {
             const int c = x / gk, part = x - c * gk;
-            const int q = sQ[buf][c];
-            if (q >= 0) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)q * nkp + part * 4);
+            const int64_t cc = c0 + c;
+            if (cc < c_end) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)__ldg(Q + cc) * nkp + part * 4);
             else *reinterpret_cast<float4*>(zkb + c * nkp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         cp_async_commit();
     };
     const int tj = nkp / 4, ti = nbp / 4;
-    const int ket_tiles = (kAdjChunk / 4) * tj, bra_tiles = (kAdjChunk / 4) * ti;
-    __syncthreads();
-    load_idx(0, 0);
-    __syncthreads();
-    stage(0);
+    const int ket_tiles = (C / 4) * tj, bra_tiles = (C / 4) * ti;
+    stage(0, 0);
     for (int k = 0; k < n_chunks; ++k) {
         const int buf = k & 1;
-        __syncthreads();                             // chunk k-1 (buffer buf ^ 1) fully consumed
-        if (k + 1 < n_chunks) load_idx(k + 1, buf ^ 1);
-        __syncthreads();                             // indices of k+1 visible
-        if (k + 1 < n_chunks) {
-            stage(buf ^ 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-        const float* zbb = zb_s + buf * kAdjChunk * nbp;
-        const float* zkb = zk_s + buf * kAdjChunk * nkp;
+        cp_async_wait<0>();                          // this thread's gathers of stage k landed
+        __syncthreads();                             // everyone's landed; stage k-1 fully consumed
+        if (k + 1 < n_chunks) stage(k + 1, buf ^ 1); // in flight while stage k is multiplied
+        const int64_t c0 = c_begin + (int64_t)k * C;
+        const float* zbb = zb_s + buf * C * nbp;
+        const float* zkb = zk_s + buf * C * nkp;
         for (int w = threadIdx.x; w < ket_tiles + bra_tiles; w += blockDim.x) {
             float acc[4][4] = {};
-            if (w < ket_tiles) {            // U[c, J] = s_c sum_I zb[c, I] G[I, J]
-                const int c4 = (w / tj) * 4, j4 = (w % tj) * 4;
-                // 4 x 4 blocks of both operands per step (rows padded with zeros to nbp)
-                for (int I = 0; I < nbp; I += 4) {
-                    float4 a[4], b[4];
+            const bool ket = w < ket_tiles;
+            const int wl = ket ? w : w - ket_tiles;
+            const int tw = ket ? tj : ti;
+            const int c4 = (wl / tw) * 4, o4 = (wl % tw) * 4;
+            // ket: U[c, J] = sum_I zb[c, I] G[I, J]   bra: W[c, I] = sum_J zk[c, J] G^T[J, I]
+            const float* A = ket ? zbb : zkb;
+            const float* B = ket ? g : gt;
+            const int la = ket ? nbp : nkp, lb = ket ? nkp : nbp;
+            for (int K0 = 0; K0 < la; K0 += 4) {
+                float4 a[4], b[4];
 #pragma unroll
-                    for (int x = 0; x < 4; ++x) a[x] = *reinterpret_cast<const float4*>(zbb + (c4 + x) * nbp + I);
+                for (int x = 0; x < 4; ++x) a[x] = *reinterpret_cast<const float4*>(A + (c4 + x) * la + K0);
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) b[i] = *reinterpret_cast<const float4*>(g + (I + i) * nkp + j4);
+                for (int i = 0; i < 4; ++i) b[i] = *reinterpret_cast<const float4*>(B + (K0 + i) * lb + o4);
 #pragma unroll
-                    for (int x = 0; x < 4; ++x) {
-                        const float av[4] = {a[x].x, a[x].y, a[x].z, a[x].w};
+                for (int x = 0; x < 4; ++x) {
+                    const float av[4] = {a[x].x, a[x].y, a[x].z, a[x].w};
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            acc[x][0] = fmaf(av[i], b[i].x, acc[x][0]);
-                            acc[x][1] = fmaf(av[i], b[i].y, acc[x][1]);
-                            acc[x][2] = fmaf(av[i], b[i].z, acc[x][2]);
-                            acc[x][3] = fmaf(av[i], b[i].w, acc[x][3]);
-                        }
+                    for (int i = 0; i < 4; ++i) {
+                        acc[x][0] = fmaf(av[i], b[i].x, acc[x][0]);
+                        acc[x][1] = fmaf(av[i], b[i].y, acc[x][1]);
+                        acc[x][2] = fmaf(av[i], b[i].z, acc[x][2]);
+                        acc[x][3] = fmaf(av[i], b[i].w, acc[x][3]);
                     }
                 }
-                const int valid = nk - j4 < 4 ? nk - j4 : 4;
-                for (int x = 0; x < 4; ++x) {
-                    const int q = sQ[buf][c4 + x];
-                    if (q < 0) continue;
-                    const float sc = sS[buf][c4 + x];
+            }
+            const int n_out = ket ? nk : nb;
+            const int valid = n_out - o4 < 4 ? n_out - o4 : 4;
+            for (int x = 0; x < 4; ++x) {
+                const int64_t cc = c0 + c4 + x;
+                if (cc >= c_end) break;
+                const float sc = __ldg(sgn + cc) < 0 ? -1.f : 1.f;
 #pragma unroll
-                    for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
-                    atomic_add4(gzkT + (int64_t)q * nk + j4, acc[x], valid);
-                }
-            } else {                        // W[c, I] = s_c sum_J G[I, J] zk[c, J]
-                const int wb = w - ket_tiles;
-                const int c4 = (wb / ti) * 4, i4 = (wb % ti) * 4;
-                for (int J = 0; J < nkp; J += 4) {
-                    float4 a[4], b[4];
-#pragma unroll
-                    for (int x = 0; x < 4; ++x) a[x] = *reinterpret_cast<const float4*>(zkb + (c4 + x) * nkp + J);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) b[j] = *reinterpret_cast<const float4*>(gt + (J + j) * nbp + i4);
-#pragma unroll
-                    for (int x = 0; x < 4; ++x) {
-                        const float av[4] = {a[x].x, a[x].y, a[x].z, a[x].w};
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            acc[x][0] = fmaf(av[j], b[j].x, acc[x][0]);
-                            acc[x][1] = fmaf(av[j], b[j].y, acc[x][1]);
-                            acc[x][2] = fmaf(av[j], b[j].z, acc[x][2]);
-                            acc[x][3] = fmaf(av[j], b[j].w, acc[x][3]);
-                        }
-                    }
-                }
-                const int valid = nb - i4 < 4 ? nb - i4 : 4;
-                for (int x = 0; x < 4; ++x) {
-                    const int p = sP[buf][c4 + x];
-                    if (p < 0) continue;
-                    const float sc = sS[buf][c4 + x];
-#pragma unroll
-                    for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
-                    atomic_add4(gzbT + (int64_t)p * nb + i4, acc[x], valid);
-                }
+                for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
+                float* dst = ket ? gzkT + (int64_t)__ldg(Q + cc) * nk + o4 : gzbT + (int64_t)__ldg(P + cc) * nb + o4;
+                atomic_add4(dst, acc[x], valid);
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
+__global__ void __launch_bounds__(kAdjThreads, 3) density_adjoint_f32_kernel(
     const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
     const double* __restrict__ gT, float* __restrict__ gzbT, float* __restrict__ gzkT) {
@@ -238,7 +219,7 @@ __global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_kernel(
 }
 
 // Every block of a task table in one launch (one CTA per operator index).
-__global__ void __launch_bounds__(kAdjThreads) density_adjoint_f32_grouped_kernel(
+__global__ void __launch_bounds__(kAdjThreads, 3) density_adjoint_f32_grouped_kernel(
     const xrh_dens_adj_task* __restrict__ tasks, int n_tasks) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int lo = 0, hi = n_tasks - 1;
@@ -429,8 +410,8 @@ extern "C" int xrh_density_adjoint_f32_grouped(const xrh_dens_adj_task* tasks_de
     if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
     if (!tasks_dev) return XRH_ERR_ARG;
     if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
-    const int nbp = (max_nb + 3) & ~3, nkp = (max_nk + 3) & ~3;
-    const size_t smem = sizeof(float) * (2 * (size_t)nbp * nkp + 2 * (size_t)kAdjChunk * (nbp + nkp));
+    if (max_nb > 1024 || max_nk > 1024) return XRH_ERR_CAPACITY;
+    const size_t smem = adj_f32_smem(max_nb, max_nk);
     if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(density_adjoint_f32_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -479,8 +460,8 @@ extern "C" int xrh_density_adjoint(int precision, int64_t K, const int64_t* idx_
             reinterpret_cast<const double*>(zkT_dev), n_k, gT_dev, reinterpret_cast<double*>(gzbT_dev),
             reinterpret_cast<double*>(gzkT_dev));
     } else if (precision == XRH_FP32) {
-        const int nbp = (n_b + 3) & ~3, nkp = (n_k + 3) & ~3;
-        const size_t smem32 = sizeof(float) * (2 * (size_t)nbp * nkp + 2 * (size_t)kAdjChunk * (nbp + nkp));
+        if (n_b > 1024 || n_k > 1024) return XRH_ERR_CAPACITY;
+        const size_t smem32 = adj_f32_smem(n_b, n_k);
         if (smem32 > 200 * 1024) return XRH_ERR_CAPACITY;
         cudaFuncSetAttribute(density_adjoint_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
         if ((reinterpret_cast<uintptr_t>(zbT_dev) & 15) || (reinterpret_cast<uintptr_t>(zkT_dev) & 15)) return XRH_ERR_ARG;

@@ -443,22 +443,40 @@ extern "C" int xrh_density_build_noalloc(int precision, int64_t K, const int64_t
 namespace {
 
 
-constexpr int kF32Chunk = 64;
+constexpr int kF32StageFloats = 8192;            // one stage of gathered rows: at most 32 KB
 
-// One operator index (and one split of its couplings) per CTA: a 4 x 4 register tile of the
-// n_b x n_k block per thread over a double-buffered ring of gathered coefficient rows.  FP32
-// chunk sums are folded into FP32 (hi, lo) pairs by TwoSum and fl32(hi + lo) is written: the
-// FP64 pipe, a small fraction of the FP32 rate on this part, stays idle.
+// Thread groups of the FP32 forward: a block of n_b x n_k has T = (n_b/4)(n_k/4) register
+// tiles; when T < kAccThreads, G = kAccThreads / T groups of T threads share a stage, each
+// group taking every G-th coupling, and their sums are combined at the end.
+__host__ __device__ __forceinline__ int f32_groups(int nbp, int nkp) {
+    const int T = (nbp >> 2) * (nkp >> 2);
+    return T >= kAccThreads ? 1 : kAccThreads / T;
+}
+// Couplings per stage: 64 per group, as many as fit kF32StageFloats.
+__host__ __device__ __forceinline__ int f32_chunk(int nbp, int nkp) {
+    int c = 64 * f32_groups(nbp, nkp);
+    const int cap = kF32StageFloats / (nbp + nkp);
+    return c < cap ? c : (cap < 4 ? 4 : cap);
+}
+
+// One operator index (and one split of its couplings) per CTA: 4 x 4 register tiles of the
+// n_b x n_k block over a double-buffered ring of gathered FP32 coefficient rows, ONE barrier
+// per stage (the rows of stage k+1 are gathered with cp.async while stage k is multiplied).
+// The coupling list of an index is ordered positive signs first (FragmentSpace), so the
+// stages cover the positive range, then the negative one, and a stage multiplies with a
+// uniform sign (the FFMA negates its operand for free).  FP32 stage sums are folded into
+// FP32 (hi, lo) pairs by TwoSum and fl32(hi + lo) is written: the FP64 pipe, a small
+// fraction of the FP32 rate on this part, stays idle.
 __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const int64_t* __restrict__ idx_ptr,
                                                  const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
                                                  const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb,
                                                  const float* __restrict__ zk32, int nk, double* __restrict__ rhoT,
                                                  int splits, unsigned char* smem_raw) {
     const int nbp = (nb + 3) & ~3, nkp = (nk + 3) & ~3;
-    float* zb_s = reinterpret_cast<float*>(smem_raw);               // [2][chunk][nbp]
-    float* zk_s = zb_s + 2 * kF32Chunk * nbp;                        // [2][chunk][nkp]
-    __shared__ int sP[2][kF32Chunk], sQ[2][kF32Chunk];
-    __shared__ float sS[2][kF32Chunk];
+    const int G = f32_groups(nbp, nkp), C = f32_chunk(nbp, nkp);
+    float* zb_s = reinterpret_cast<float*>(smem_raw);               // [2][C][nbp]
+    float* zk_s = zb_s + 2 * C * nbp;                                // [2][C][nkp]
+    __shared__ int64_t s_split;
     const int64_t cb0 = idx_ptr[idx], ce0 = idx_ptr[idx + 1];
     const int64_t len = ce0 - cb0;
     const int64_t per = (len + splits - 1) / splits;
@@ -471,39 +489,54 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
             for (int o = threadIdx.x; o < nb * nk; o += blockDim.x) out[o] = 0.0;
         return;
     }
-    const int n_chunks = (int)((c_end - c_begin + kF32Chunk - 1) / kF32Chunk);
-    const int gb = nbp / 4, gk = nkp / 4;       // 16-byte granules per row
-    auto load_idx = [&](int k, int buf) {
-        const int64_t c0 = c_begin + (int64_t)k * kF32Chunk;
-        for (int t = threadIdx.x; t < kF32Chunk; t += blockDim.x) {
-            const int64_t c = c0 + t;
-            const bool ok = c < c_end;
-            sP[buf][t] = ok ? P[c] : -1;
-            sQ[buf][t] = ok ? Q[c] : -1;
-            sS[buf][t] = ok ? (sgn[c] < 0 ? -1.f : 1.f) : 0.f;
+    if (threadIdx.x == 0) {                       // first negative coupling (signs sorted + then -)
+        int64_t lo = c_begin, hi = c_end;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (__ldg(sgn + mid) < 0) hi = mid; else lo = mid + 1;
+        }
+        s_split = lo;
+    }
+    __syncthreads();
+    const int64_t c_split = s_split;
+    const int n_pos = (int)((c_split - c_begin + C - 1) / C);
+    const int n_chunks = n_pos + (int)((c_end - c_split + C - 1) / C);
+    const int gb = nbp / 4, gk = nkp / 4;
+    auto range = [&](int k, int64_t& c0, int64_t& ce) {
+        if (k < n_pos) {
+            c0 = c_begin + (int64_t)k * C;
+            ce = c_split;
+        } else {
+            c0 = c_split + (int64_t)(k - n_pos) * C;
+            ce = c_end;
         }
     };
-    auto stage = [&](int buf) {
-        float* zbb = zb_s + buf * kF32Chunk * nbp;
-        float* zkb = zk_s + buf * kF32Chunk * nkp;
-        for (int g = threadIdx.x; g < kF32Chunk * gb; g += blockDim.x) {
-            const int c = g / gb, part = g - c * gb;
-            const int p = sP[buf][c];
-            if (p >= 0) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)p * nbp + part * 4);
+    auto stage = [&](int k, int buf) {
+        int64_t c0, ce;
+        range(k, c0, ce);
+        float* zbb = zb_s + buf * C * nbp;
+        float* zkb = zk_s + buf * C * nkp;
+        for (int x = threadIdx.x; x < C * gb; x += blockDim.x) {
+            const int c = x / gb, part = x - c * gb;
+            const int64_t cc = c0 + c;
+            if (cc < ce) cp_async16(zbb + c * nbp + part * 4, zb32 + (int64_t)__ldg(P + cc) * nbp + part * 4);
             else *reinterpret_cast<float4*>(zbb + c * nbp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        for (int g = threadIdx.x; g < kF32Chunk * gk; g += blockDim.x) {
-            const int c = g / gk, part = g - c * gk;
-            const int q = sQ[buf][c];
-            if (q >= 0) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)q * nkp + part * 4);
+        for (int x = threadIdx.x; x < C * gk; x += blockDim.x) {
+            const int c = x / gk, part = x - c * gk;
+            const int64_t cc = c0 + c;
+            if (cc < ce) cp_async16(zkb + c * nkp + part * 4, zk32 + (int64_t)__ldg(Q + cc) * nkp + part * 4);
             else *reinterpret_cast<float4*>(zkb + c * nkp + part * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         cp_async_commit();
     };
 
+    const int active_threads = G * (n_tiles < kAccThreads ? n_tiles : kAccThreads);
     for (int t0 = 0; t0 < n_tiles; t0 += kAccThreads) {
-        const int t = t0 + threadIdx.x;
-        const bool active = t < n_tiles;
+        const bool grouped = G > 1;
+        const int t = grouped ? (int)threadIdx.x % n_tiles : t0 + (int)threadIdx.x;
+        const int grp = grouped ? (int)threadIdx.x / n_tiles : 0;
+        const bool active = (int)threadIdx.x < active_threads && t < n_tiles;
         const int i0 = active ? (t / tiles_j) * 4 : 0, j0 = active ? (t % tiles_j) * 4 : 0;
         float acc[4][4], acc_lo[4][4];          // running sums as FP32 (hi, lo) pairs (TwoSum)
 #pragma unroll
@@ -513,37 +546,41 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
                 acc[a][b] = 0.f;
                 acc_lo[a][b] = 0.f;
             }
-        __syncthreads();
-        load_idx(0, 0);
-        __syncthreads();
-        stage(0);
+        __syncthreads();                             // the ring is free (previous round done)
+        stage(0, 0);
         for (int k = 0; k < n_chunks; ++k) {
             const int buf = k & 1;
-            __syncthreads();                         // chunk k-1 (buffer buf ^ 1) fully consumed
-            if (k + 1 < n_chunks) load_idx(k + 1, buf ^ 1);
-            __syncthreads();                         // indices of k+1 visible
-            if (k + 1 < n_chunks) {
-                stage(buf ^ 1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            __syncthreads();                         // gathers of chunk k visible to every thread
+            cp_async_wait<0>();
+            __syncthreads();                         // stage k visible, stage k-1 consumed
+            if (k + 1 < n_chunks) stage(k + 1, buf ^ 1);
             if (active) {
-                const float* zbb = zb_s + buf * kF32Chunk * nbp;
-                const float* zkb = zk_s + buf * kF32Chunk * nkp;
+                const float* zbb = zb_s + buf * C * nbp;
+                const float* zkb = zk_s + buf * C * nkp;
                 float part[4][4] = {};
+                if (k < n_pos) {
 #pragma unroll 4
-                for (int c = 0; c < kF32Chunk; ++c) {
-                    const float s = sS[buf][c];
-                    const float4 va = *reinterpret_cast<const float4*>(zbb + c * nbp + i0);
-                    const float4 vb = *reinterpret_cast<const float4*>(zkb + c * nkp + j0);
-                    const float av[4] = {s * va.x, s * va.y, s * va.z, s * va.w};
-                    const float bv[4] = {vb.x, vb.y, vb.z, vb.w};
+                    for (int c = grp; c < C; c += G) {
+                        const float4 va = *reinterpret_cast<const float4*>(zbb + c * nbp + i0);
+                        const float4 vb = *reinterpret_cast<const float4*>(zkb + c * nkp + j0);
+                        const float av[4] = {va.x, va.y, va.z, va.w};
+                        const float bv[4] = {vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
-                    for (int a = 0; a < 4; ++a)
+                        for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int b = 0; b < 4; ++b) part[a][b] = fmaf(av[a], bv[b], part[a][b]);
+                            for (int b = 0; b < 4; ++b) part[a][b] = fmaf(av[a], bv[b], part[a][b]);
+                    }
+                } else {
+#pragma unroll 4
+                    for (int c = grp; c < C; c += G) {
+                        const float4 va = *reinterpret_cast<const float4*>(zbb + c * nbp + i0);
+                        const float4 vb = *reinterpret_cast<const float4*>(zkb + c * nkp + j0);
+                        const float av[4] = {va.x, va.y, va.z, va.w};
+                        const float bv[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+                        for (int a = 0; a < 4; ++a)
+#pragma unroll
+                            for (int b = 0; b < 4; ++b) part[a][b] = fmaf(-av[a], bv[b], part[a][b]);
+                    }
                 }
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
@@ -556,7 +593,37 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
                     }
             }
         }
-        if (active) {
+        if (grouped) {
+            // combine the groups' (hi, lo) sums through the (now idle) ring, in group order
+            __syncthreads();
+            float* red = zb_s;                       // [G][n_tiles][32]: hi 16, lo 16
+            if (active) {
+                float* r = red + ((int64_t)grp * n_tiles + t) * 32;
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) {
+                        r[a * 4 + b] = acc[a][b];
+                        r[16 + a * 4 + b] = acc_lo[a][b];
+                    }
+            }
+            __syncthreads();
+            if (active && grp == 0) {
+                for (int q = 1; q < G; ++q) {
+                    const float* r = red + ((int64_t)q * n_tiles + t) * 32;
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            float sum, err;
+                            xrh_two_sum(acc[a][b], r[a * 4 + b], sum, err);
+                            acc[a][b] = sum;
+                            acc_lo[a][b] += err + r[16 + a * 4 + b];
+                        }
+                }
+            }
+        }
+        if (active && grp == 0) {
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -568,10 +635,27 @@ __device__ __forceinline__ void density_f32_body(int64_t idx, int split, const i
                     else atomicAdd(o, v);
                 }
         }
+        if (grouped) break;                          // every tile was covered by the groups
     }
 }
 
-__global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
+// Shared memory (bytes) of the FP32 forward for the largest n_b, n_k of a launch: two stages
+// of gathered rows, and the group reduction that reuses them.
+static size_t f32_smem(int max_nb, int max_nk) {
+    const int nbp = (max_nb + 3) & ~3, nkp = (max_nk + 3) & ~3;
+    size_t need = 0;
+    for (int b = 4; b <= nbp; b += 4)
+        for (int k = 4; k <= nkp; k += 4) {
+            const size_t ring = 2 * (size_t)f32_chunk(b, k) * (b + k);
+            const int T = (b / 4) * (k / 4);
+            const size_t red = T < kAccThreads ? (size_t)f32_groups(b, k) * T * 32 : 0;
+            const size_t v = ring > red ? ring : red;
+            need = v > need ? v : need;
+        }
+    return sizeof(float) * need;
+}
+
+__global__ void __launch_bounds__(kAccThreads, 3) density_acc_f32_kernel(
     const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
     double* __restrict__ rhoT, int splits) {
@@ -580,7 +664,7 @@ __global__ void __launch_bounds__(kAccThreads) density_acc_f32_kernel(
 }
 
 // Every block of a task table in one launch: CTA -> task by binary search on cta_begin.
-__global__ void __launch_bounds__(kAccThreads) density_acc_f32_grouped_kernel(const xrh_dens_task* __restrict__ tasks,
+__global__ void __launch_bounds__(kAccThreads, 3) density_acc_f32_grouped_kernel(const xrh_dens_task* __restrict__ tasks,
                                                                               int n_tasks) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int lo = 0, hi = n_tasks - 1;
@@ -771,7 +855,8 @@ extern "C" int xrh_density_accumulate_f32_grouped(const xrh_dens_task* tasks_dev
     if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
     if (!tasks_dev) return XRH_ERR_ARG;
     if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
-    const size_t smem = sizeof(float) * 2 * (size_t)kF32Chunk * (size_t)(((max_nb + 3) & ~3) + ((max_nk + 3) & ~3));
+    if (max_nb > 1024 || max_nk > 1024) return XRH_ERR_CAPACITY;
+    const size_t smem = f32_smem(max_nb, max_nk);
     if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(density_acc_f32_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -789,7 +874,8 @@ extern "C" int xrh_density_accumulate_f32(int64_t K, int splits, const int64_t* 
         return XRH_ERR_ARG;
     if (K > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     if ((reinterpret_cast<uintptr_t>(zb32_dev) & 15) || (reinterpret_cast<uintptr_t>(zk32_dev) & 15)) return XRH_ERR_ARG;
-    const size_t smem = sizeof(float) * 2 * (size_t)kF32Chunk * (size_t)(((n_b + 3) & ~3) + ((n_k + 3) & ~3));
+    if (n_b > 1024 || n_k > 1024) return XRH_ERR_CAPACITY;
+    const size_t smem = f32_smem(n_b, n_k);
     if (smem > 200 * 1024) return XRH_ERR_CAPACITY;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(density_acc_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -135,8 +135,10 @@ class FragmentSpace:
                  ptr(self.sorted_masks[bc]), ptr(self.sorted_pos[bc]), n_bra, ptr(offsets), ptr(idx), ptr(P),
                  ptr(Q), ptr(sign), s)
         idx, P, Q, sign = idx[:total], P[:total], Q[:total], sign[:total]
-        # stable sort by operator index (Q order kept inside an index: deterministic sums)
-        order = torch.argsort(idx.to(torch.int64) * (max(n_ket, 1)) + Q.to(torch.int64))
+        # sort by operator index, inside an index positive signs first (the FP32 density kernel
+        # multiplies each sign range with a uniform sign), then by Q: deterministic sums
+        nk = max(n_ket, 1)
+        order = torch.argsort((idx.to(torch.int64) * 2 + (sign < 0).to(torch.int64)) * nk + Q.to(torch.int64))
         idx, P, Q, sign = idx[order].contiguous(), P[order].contiguous(), Q[order].contiguous(), sign[order].contiguous()
         idx_ptr = torch.zeros(K + 1, dtype=torch.int64, device=self.device)
         if total:
@@ -404,13 +406,13 @@ class DensityBuilder:
         self._stage_coefficients(coeffs, bra_coeffs, s)
         if self.f32:
             for t in self._zero_first:
-                t.zero_()
+                _lib.zero_(t)
             if self._n_dens_tasks:
                 call("xrh_density_accumulate_f32_grouped", ptr(self._dens_tasks), self._n_dens_tasks,
                      self._dens_ctas, self._max_nb, self._max_nk, s)
             if self._n_units:
                 if self._unit_zero is not None:
-                    self._unit_zero.zero_()
+                    _lib.zero_(self._unit_zero)
                 call("xrh_density_accumulate_f32_units", ptr(self._unit_tasks), self._n_unit_tasks, ptr(self._units),
                      self._n_units, self._max_n, s)
         if not self.f32:
