@@ -16,6 +16,7 @@ one-CTA loop and "steps" six launches per step, kept as cross-checks.
 import numpy as np
 import torch
 
+from . import _lib
 from ._lib import call, ptr, stream_ptr
 
 SMALL_SECTOR = 2048
@@ -162,7 +163,7 @@ class Lanczos:
         yy = np.zeros(self.m + 1)
         yy[:len(y)] = y
         self.y.copy_(torch.from_numpy(yy))
-        out.zero_()
+        _lib.zero_(out)
         call("xrh_gemv_cols", self.m, self.n, ptr(self.V), self.n, ptr(self.y), 1.0, ptr(out), stream_ptr())
         return out
 
@@ -171,7 +172,7 @@ class Lanczos:
         y = np.zeros(self.m + 1)
         y[:self._cut] = self._ritz
         self.y.copy_(torch.from_numpy(y))
-        self.vec.zero_()
+        _lib.zero_(self.vec)
         call("xrh_gemv_cols", self.m, self.n, ptr(self.V), self.n, ptr(self.y), 1.0, ptr(self.vec), stream_ptr())
         return self.vec
 

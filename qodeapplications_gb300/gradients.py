@@ -476,12 +476,12 @@ class XRDimerAdjoint:
         s = stream_ptr()
         if d is not None:
             self.d.copy_(d)
-        self.arena.buf.zero_()
+        _lib.zero_(self.arena.buf)
         if self.prec32:
             for m in (0, 1):
                 for t in self.gz32[m].values():
-                    t.zero_()
-                self.Gamma32[m].zero_()
+                    _lib.zero_(t)
+                _lib.zero_(self.Gamma32[m])
         self.L1.run()
         self.L2.run()
         self.launch_L3()
@@ -625,7 +625,7 @@ class XRDimerAdjoint:
                 self._integral_gradients_into(dT, dU, dV)
                 Ga = dV - dV.permute(1, 0, 2, 3) - dV.permute(0, 1, 3, 2) + dV.permute(1, 0, 3, 2)
                 torch.add(Ga, Ga.permute(2, 3, 0, 1), out=b["B"])
-            Gso.zero_()
+            _lib.zero_(Gso)
             # the one-body terms T dT^T + T^T dT + sum_k U_k dU_k^T + U_k^T dU_k (dU_k = dT) in
             # one launch
             tab, n_tab, ctas = b["one_body"]
@@ -645,14 +645,12 @@ class XRDimerAdjoint:
             Gso += 4.0 * (V.reshape(t, -1) @ Gbar.reshape(t, -1).t())
         key = (tuple(spatial_index), T.device)
         if key not in self._spatial_cache:     # built on first use, outside any graph capture
-            n_sp = int(max(spatial_index)) + 1
-            Pm = torch.zeros((t, n_sp), dtype=torch.float64, device=T.device)
-            Pm[torch.arange(t, device=T.device), torch.as_tensor(np.asarray(spatial_index), device=T.device)] = 1.0
-            self._spatial_cache[key] = (Pm, _same_spin(t, spatial_index, T.device))
-        Pm, same = self._spatial_cache[key]
-        # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs
-        Gsp = Pm.t() @ (Gso * same) @ Pm
-        return Gsp - Gsp.t()
+            self._spatial_cache[key] = _spin_blocks(spatial_index, T.device)
+        so, n_sp, n_spin, out = self._spatial_cache[key]
+        # a spatial rotation acts on both spins alike: sum the same-spin spin-orbital pairs of
+        # every spatial pair, antisymmetrised (xrh_spin_sum_antisym)
+        call("xrh_spin_sum_antisym", n_sp, n_spin, ptr(so), ptr(Gso), Gso.shape[1], ptr(out), stream_ptr())
+        return out
 
 
 def _one_body_table(pairs, device):
@@ -669,6 +667,22 @@ def _one_body_table(pairs, device):
             e["cta_begin"], e["flags"] = cta, flags
             cta += int(_lib.lib().xrh_abt_ctas(t))
     return torch.from_numpy(tab.view(np.uint8).copy()).to(device), len(tab), cta
+
+
+def _spin_blocks(spatial_index, device):
+    """so[k, a] = the spin orbital of spatial orbital a in spin block k (alpha, beta), with the
+    output buffer of the spatial gradient."""
+    n_sp = int(max(spatial_index)) + 1
+    so = np.full((2, n_sp), -1, dtype=np.int32)
+    seen = {}
+    for i, sp in enumerate(spatial_index):
+        k = seen.get(sp, 0)
+        so[k, sp] = i
+        seen[sp] = k + 1
+    if (so < 0).any():
+        raise ValueError("every spatial orbital needs an alpha and a beta spin orbital")
+    out = torch.zeros((n_sp, n_sp), dtype=torch.float64, device=device)
+    return torch.from_numpy(so.reshape(-1).copy()).to(device), n_sp, 2, out
 
 
 def _same_spin(t, spatial_index, device):

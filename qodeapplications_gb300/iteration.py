@@ -29,27 +29,65 @@ from .hamiltonian import DeviceIntegrals, XRDimerPlan
 from .synthetic import spin_orbital_spatial_index
 
 
-def _inv_sqrt_newton_schulz(S, iters=6):
-    """S^-1/2 for symmetric positive definite S close to the identity (coupled Newton-Schulz);
-    S may be a batch (..., n, n)."""
-    n = S.shape[-1]
-    I = torch.eye(n, dtype=S.dtype, device=S.device).expand_as(S)
-    Y, Z = S.clone(), I.clone()
-    for _ in range(iters):
-        T = 0.5 * (3.0 * I - Z @ Y)
-        Y = Y @ T
-        Z = T @ Z
-    return Z
-
-
 NS_ITERS = 6
+
+
+class NewtonSchulzGrouped:
+    """M_i = S_i^-1/2 for every state block i (n <= 64) by coupled Newton-Schulz iterations
+    (Y_0 = S, Z_0 = I; T = (3 I - Z Y) / 2, Y <- Y T, Z <- T Z; Z -> S^-1/2) in FP64, two
+    xrh_small_mm_grouped launches per iteration over all blocks.  The task tables are built
+    once over persistent buffers, so run() can be captured in a CUDA graph."""
+
+    def __init__(self, S_views, M_views, iters, device):
+        f64 = dict(dtype=torch.float64, device=device)
+        self.keep = []
+        per = []
+        for S, M in zip(S_views, M_views):
+            n = S.shape[0]
+            if n > 64:
+                raise ValueError("Newton-Schulz blocks are limited to 64 states")
+            b = dict(n=n, S=S, M=M, Y=[torch.empty((n, n), **f64) for _ in range(2)],
+                     Z=[torch.empty((n, n), **f64) for _ in range(2)], T=torch.empty((n, n), **f64),
+                     I=torch.eye(n, **f64))
+            self.keep.append(b)
+            per.append(b)
+        self.launches = []
+        for it in range(iters):
+            first, last = it == 0, it == iters - 1
+            a_tasks, b_tasks = [], []
+            for b in per:
+                Yin = b["S"] if first else b["Y"][(it - 1) % 2]
+                Zin = b["I"] if first else b["Z"][(it - 1) % 2]
+                Zout = b["M"] if last else b["Z"][it % 2]
+                a_tasks.append((Zin, Yin, b["T"], b["n"], -0.5, 1.5))
+                if not last:
+                    b_tasks.append((Yin, b["T"], b["Y"][it % 2], b["n"], 1.0, 0.0))
+                b_tasks.append((b["T"], Zin, Zout, b["n"], 1.0, 0.0))
+            self.launches.append(self._table(a_tasks, device))
+            self.launches.append(self._table(b_tasks, device))
+
+    @staticmethod
+    def _table(tasks, device):
+        tab = np.zeros(len(tasks), dtype=_lib.SMALL_MM_TASK_DTYPE)
+        cta = 0
+        for i, (A, B, C, n, alpha, beta) in enumerate(tasks):
+            e = tab[i]
+            e["A"], e["B"], e["C"], e["n"], e["alpha"], e["beta"], e["cta_begin"] = (
+                A.data_ptr(), B.data_ptr(), C.data_ptr(), n, alpha, beta, cta)
+            cta += (n + 3) // 4
+        return torch.from_numpy(tab.view(np.uint8).copy()).to(device), len(tab), cta
+
+    def run(self):
+        s = stream_ptr()
+        for tab, n_t, ctas in self.launches:
+            call("xrh_small_mm_grouped", ptr(tab), n_t, ctas, s)
 
 
 class StateStepper:
     """The state update z <- (z' z'^T)^-1/2 z', z' = z - step * (tangent part of dE/dz), over
     every (fragment, charge) block in grouped FP64 launches: G = g z^T, the tangent step with
     its squared norm, S = z' z'^T, M = S^-1/2 (Newton-Schulz; one CTA per block for n <= 32,
-    batched torch matmuls above), z = M z'.  coeffs[i] is the n x K state block (updated in
+    NewtonSchulzGrouped above), z = M z'.  coeffs[i] is the n x K state block (updated in
     place); grads[i] = (gT, gT32) with dE/dz = (gT + gT32)^T, gT32 None or FP32, both K x n.
     All buffers are persistent, so launch() may be captured in a CUDA graph."""
 
@@ -94,26 +132,20 @@ class StateStepper:
         self.n_tasks = nb
         self.tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
         self.small_ns = max(ns) <= 32
-        by_n = {}
-        for i, n in enumerate(ns):
-            by_n.setdefault(n, []).append(i)
-        self.by_n = by_n
+        self.ns_grouped = None if self.small_ns else NewtonSchulzGrouped(self.S_views, self.M_views, NS_ITERS, dev)
 
     def launch(self):
         """One step on the current stream; returns the squared tangent-gradient norm (device)."""
         s = stream_ptr()
         tp = ptr(self.tasks)
-        self.zeroed.zero_()
+        _lib.zero_(self.zeroed)
         call("xrh_gram_grouped", tp, self.n_tasks, self.total_ctas, 0, s)
         call("xrh_tangent_step", tp, self.n_tasks, self.total_ctas, self.step, ptr(self.sq), s)
         call("xrh_gram_grouped", tp, self.n_tasks, self.total_ctas, 1, s)
         if self.small_ns:
             call("xrh_inv_sqrt_small", tp, self.n_tasks, NS_ITERS, s)
         else:
-            for n, ids in self.by_n.items():
-                Z = _inv_sqrt_newton_schulz(torch.stack([self.S_views[i] for i in ids]), NS_ITERS)
-                for k, i in enumerate(ids):
-                    self.M_views[i].copy_(Z[k])
+            self.ns_grouped.run()
         call("xrh_left_multiply", tp, self.n_tasks, self.total_ctas, s)
         return self.sq[0]
 
@@ -168,8 +200,7 @@ class XRStateOptimizer:
     def _backward(self, t, warm):
         lz = (self.lz_warm if warm else self.lz)[t]
         d = lz.ground_vector()
-        self.d_product.zero_()
-        self.d_product.index_copy_(0, self.plan.sectors[t]["rows"], d)
+        self._scatter_ground(t, d)
         # the warm start of the next iteration
         self.lz_warm[t].v0.copy_(d)
         self.adj.launch(self.d_product)
@@ -253,16 +284,20 @@ class XRStateOptimizer:
     def _backward_graphed(self, t):
         lz = self.lz_warm[t]
         d = lz.vec
-        d.zero_()
-        from ._lib import call, ptr, stream_ptr
+        _lib.zero_(d)
         call("xrh_gemv_cols", lz.m, lz.n, ptr(lz.V), lz.n, ptr(lz.y), 1.0, ptr(d), stream_ptr())
-        self.d_product.zero_()
-        self.d_product.index_copy_(0, self.plan.sectors[t]["rows"], d)
+        self._scatter_ground(t, d)
         lz.v0.copy_(d)
         self.adj.launch(self.d_product)
         self._gsq = self.stepper.launch()
         if self.orbital:
             self.kappa_grad = self.adj.orbital_gradient(self.T, self.U, self.V, self.sidx)
+
+    def _scatter_ground(self, t, d):
+        """d_product (product order, zero outside sector t) from the sector's ground vector."""
+        rows = self.plan.sectors[t]["rows"]
+        _lib.zero_(self.d_product)
+        call("xrh_index_move", rows.numel(), ptr(rows), ptr(d), ptr(self.d_product), 0, stream_ptr())
 
     @property
     def gradient_norm(self):
