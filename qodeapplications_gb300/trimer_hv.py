@@ -38,6 +38,8 @@ xrh_gemm_task / xrh_gemm_segment contract of include/xrh.h.
 import numpy as np
 import torch
 
+from . import _lib
+from ._lib import call, ptr, stream_ptr
 from .gemm import GroupedGemm
 from .trimer import _case, _phase
 
@@ -322,6 +324,29 @@ def trimer_integral_matrices(V, U, order_kinds, Ns):
     return W, Uq
 
 
+def permute_tasks(ops):
+    """xrh_permute_task records (host) for ops = [(src address, shape, ax, dst address,
+    scale)]: dst = scale * src.reshape(shape).transpose(ax), row-major.  Returns (table,
+    total elements)."""
+    tab = np.zeros(len(ops), dtype=_lib.PERMUTE_TASK_DTYPE)
+    begin = 0
+    for i, (src, shape, ax, dst, scale) in enumerate(ops):
+        if len(shape) > 6:
+            raise ValueError("permutes of more than 6 indices")
+        n = int(np.prod(shape))
+        strides = np.ones(len(shape), dtype=np.int64)
+        for k in range(len(shape) - 2, -1, -1):
+            strides[k] = strides[k + 1] * shape[k + 1]
+        e = tab[i]
+        e["src"], e["dst"], e["ndim"], e["scale"] = src, dst, len(shape), float(scale)
+        for k, a in enumerate(ax):
+            e["dst_shape"][k] = shape[a]
+            e["src_stride"][k] = strides[a]
+        e["elem_begin"], e["n_elems"] = begin, n
+        begin += n
+    return tab, begin
+
+
 class _PairIntegrals:
     """The integral accessors of fragments (a, b) of a larger system, numbered (0, 1)."""
 
@@ -397,11 +422,25 @@ class XRTrimerHamiltonian:
         self.Uq = {k: u.contiguous().reshape(-1) for k, u in Uq.items()}
         self.eyes = {}
         self._gather = {o: torch.as_tensor(plan.permutation(o), device=dev) for o in sorted(plan.orders_v - {IDENTITY})}
-        self._scatter = {o: torch.as_tensor(plan.permutation(o), device=dev) for o in sorted(plan.orders_w - {IDENTITY})}
-        self._permutes = [(self._resolve(src), shape, ax, self._resolve(dst), 1.0)
-                          for src, shape, ax, dst in plan.permutes]
-        self._mid_permutes = [(self._resolve(src), shape, ax, self._resolve(dst), a)
-                              for src, shape, ax, dst, a in plan.mid_permutes]
+        # w += w_order[inverse permutation]: every permuted accumulator returns in one gather-sum
+        self._scatter = {}
+        for o in sorted(plan.orders_w - {IDENTITY}):
+            idx = plan.permutation(o)
+            inv = np.empty_like(idx)
+            inv[idx] = np.arange(len(idx))
+            self._scatter[o] = torch.as_tensor(inv, device=dev)
+        if len(self._scatter) > 8:
+            raise ValueError("more than 8 permuted accumulators")
+        terms = np.zeros(1, dtype=_lib.GATHER_TERMS_DTYPE)
+        for t, (o, inv) in enumerate(self._scatter.items()):
+            terms[0]["src"][t] = self.bufs[_wname(o)].data_ptr()
+            terms[0]["idx"][t] = inv.data_ptr()
+        terms[0]["n_terms"] = len(self._scatter)
+        self._scatter_terms = terms
+        self._permutes = self._permute_table([(self._resolve(src), shape, ax, self._resolve(dst), 1.0)
+                                              for src, shape, ax, dst in plan.permutes])
+        self._mid_permutes = self._permute_table([(self._resolve(src), shape, ax, self._resolve(dst), a)
+                                                  for src, shape, ax, dst, a in plan.mid_permutes])
         # split forms: the pair terms and the three trimer stages on the tensor cores, each role
         # with its own split registry (a vector block is an operand of several shapes); operands
         # that change per product (vector blocks, T1, T2p) are split per product, the rest once
@@ -498,26 +537,30 @@ class XRTrimerHamiltonian:
             for reg, _g in phase:
                 reg.split("build")
 
+    def _permute_table(self, ops):
+        """xrh_permute_grouped task table: dst = scale * src.view(shape).permute(ax)."""
+        tab, total = permute_tasks([(src.data_ptr(), shape, ax, dst.data_ptr(), scale)
+                                    for src, shape, ax, dst, scale in ops])
+        dev_tab = torch.from_numpy(tab.view(np.uint8).copy()).to(self.device) if len(ops) else None
+        return (dev_tab, len(ops), total)
+
     @staticmethod
-    def _run_permutes(ops):
-        for src, shape, ax, dst, scale in ops:
-            n = int(np.prod(shape))
-            out = dst[:n].view(*[shape[a] for a in ax])
-            if scale == 1.0:
-                out.copy_(src[:n].view(shape).permute(*ax))
-            else:
-                torch.mul(src[:n].view(shape).permute(*ax), scale, out=out)
+    def _run_permutes(table):
+        tab, n_t, total = table
+        if n_t:
+            call("xrh_permute_grouped", ptr(tab), n_t, total, stream_ptr())
 
     def apply(self, x, out=None):
         """out = H x (device vectors of length self.dim, block layout); returns out."""
         v, w = self.bufs["v"], self.bufs["w"]
+        s = stream_ptr()
         if x.data_ptr() != v.data_ptr():
             v.copy_(x)
-        w.zero_()
+        _lib.zero_(w)
         for o in self._scatter:
-            self.bufs[_wname(o)].zero_()
+            _lib.zero_(self.bufs[_wname(o)])
         for o, idx in self._gather.items():
-            torch.index_select(v, 0, idx, out=self.bufs[_vname(o)])
+            call("xrh_index_move", idx.numel(), ptr(idx), ptr(v), ptr(self.bufs[_vname(o)]), 1, s)
         for k in range(3):
             if k == 2:
                 self._run_permutes(self._mid_permutes)
@@ -525,8 +568,8 @@ class XRTrimerHamiltonian:
             for reg, g in self.tcs[k]:
                 reg.split("product")
                 g.run()
-        for o, idx in self._scatter.items():
-            w.index_add_(0, idx, self.bufs[_wname(o)])
+        if self._scatter:
+            call("xrh_gather_sum", self.dim, self._scatter_terms.ctypes.data, ptr(w), 1, s)
         if out is not None and out.data_ptr() != w.data_ptr():
             out.copy_(w)
             return out
@@ -546,15 +589,45 @@ class XRTrimerHamiltonian:
         idx, dim = self.plan.product_index()
         return torch.as_tensor(idx, device=self.device), dim
 
-    def lowest(self, k=1, m=60, seed=7):
+    def lowest(self, k=1, m=60, seed=7, tol=None, max_restarts=30, graph=False):
         """Lowest k eigenvalues (FP64 Lanczos on the matrix-free product) and the residual
-        estimate of the lowest; the ground-state vector is self.lanczos.ground_vector()."""
+        estimate of the lowest; the ground-state vector is self.lanczos.ground_vector().
+        tol: restart the Krylov loop from the current ground Ritz vector until the residual
+        of the lowest pair is below tol * max(1, |E0|) (None: one loop of m steps).
+        graph: replay the m-step Krylov loop (products and Gram-Schmidt) as one CUDA graph,
+        captured on the first call."""
         from .eigen import Lanczos
         if getattr(self, "lanczos", None) is None or self.lanczos.m != min(m, self.dim):
             self.lanczos = Lanczos(self.dim, m=m, device=self.device, seed=seed, mode="steps")
+            self._krylov_graph = None
         lz = self.lanczos
-        lz.krylov_operator(lambda x, y: self.apply(x, y))
-        lz.stage_to_host()
-        torch.cuda.current_stream().synchronize()
-        return lz.solve(k)
 
+        def krylov():
+            lz.krylov_operator(lambda x, y: self.apply(x, y))
+
+        if graph and self._krylov_graph is None:
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            v0 = lz.v0.clone()
+            with torch.cuda.stream(s):          # warm the allocator outside the capture
+                krylov()
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                krylov()
+            lz.v0.copy_(v0)
+            self._krylov_graph = g
+        w = resid = None
+        for _ in range(max_restarts if tol is not None else 1):
+            if graph:
+                self._krylov_graph.replay()
+            else:
+                krylov()
+            lz.stage_to_host()
+            torch.cuda.current_stream().synchronize()
+            w, resid = lz.solve(k)
+            if tol is None or resid <= tol * max(1.0, abs(float(w[0]))):
+                break
+            lz.v0.copy_(lz.ground_vector())
+        return w, resid

@@ -239,3 +239,25 @@ def test_plan_empty_sector_has_no_work():
                         lambda f, op, bc, kc: True, total_charge=5)
     assert plan.dim == 0 and plan.triples == [] and all(not L for L in plan.launches)
     assert plan.flops_apply == 0.0 and not plan.build_tasks
+
+
+def test_permute_task_records_match_numpy_transpose():
+    """The xrh_permute_grouped records (dst shape, source strides) reproduce
+    numpy.transpose when the kernel's index walk is replayed on the host."""
+    from qodeapplications_gb300.trimer_hv import permute_tasks
+    rng = np.random.default_rng(2)
+    cases = [((3, 4, 5), (2, 0, 1), 1.0), ((2, 3, 4, 5), (1, 3, 0, 2), -0.5), ((6, 7), (1, 0), 2.0),
+             ((2, 2, 3, 2, 3, 2), (5, 4, 3, 2, 1, 0), 1.0)]
+    srcs = [rng.standard_normal(int(np.prod(sh))) for sh, _, _ in cases]
+    tab, total = permute_tasks([(i, sh, ax, i, sc) for i, (sh, ax, sc) in enumerate(cases)])
+    assert total == sum(int(np.prod(sh)) for sh, _, _ in cases)
+    for rec, (sh, ax, sc), src in zip(tab, cases, srcs):
+        out = np.empty(int(rec["n_elems"]))
+        for e in range(int(rec["n_elems"])):
+            r, off = e, 0
+            for k in range(int(rec["ndim"]) - 1, -1, -1):
+                d = int(rec["dst_shape"][k])
+                off += (r % d) * int(rec["src_stride"][k])
+                r //= d
+            out[e] = rec["scale"] * src[off]
+        np.testing.assert_array_equal(out, sc * src.reshape(sh).transpose(ax).ravel())
