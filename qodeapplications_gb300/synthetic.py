@@ -122,6 +122,71 @@ def make_system(n_frag=2, n_orb=9, n_states=10, charges=(+1, 0, -1), n_elec_ref=
                 charges=tuple(charges), Ns=[2 * n_orb] * n_frag, h=h, V=V, states=states)
 
 
+class ChainIntegralSource:
+    """The integrals of make_system (same seed, same random stream for h and the Cholesky
+    vectors L^K) for chains and rings too large for the supersystem V: fragment blocks are
+    formed on request, with the accessors of the reference's fragment-blocked integral
+    structs (hermitian-XRCC/get_ints.py:116-155): T[m, n], U[k, m, n] (zero), V[m, n, o, p],
+    S[m, n] (identity), each spin-blocked (alpha then beta inside a fragment) and V
+    antisymmetrised as in spin_orbital_integrals."""
+
+    def __init__(self, n_frag, n_orb, n_chol=40, seed=1234):
+        rng = np.random.default_rng(seed)
+        n = n_frag * n_orb
+        a = rng.normal(0.0, 0.1, size=(n, n))
+        self.h_sp = np.triu(a) + np.triu(a, 1).T
+        L = rng.normal(0.0, 0.05, size=(n_chol, n, n))
+        self.L = 0.5 * (L + L.transpose(0, 2, 1))
+        self.rng = rng                      # continues with the states, as in make_system
+        self.n_frag, self.n_orb = n_frag, n_orb
+        sp = np.tile(np.arange(n_orb), 2)
+        self._sp = [m * n_orb + sp for m in range(n_frag)]
+        self._spin = np.repeat([0, 1], n_orb)
+        outer = self
+
+        class _Acc:
+            def __init__(self, fn):
+                self.fn = fn
+
+            def __getitem__(self, key):
+                return self.fn(*(key if isinstance(key, tuple) else (key,)))
+
+        self.T = _Acc(self._T)
+        self.U = _Acc(lambda k, m, n: np.zeros((2 * n_orb, 2 * n_orb)))
+        self.V = _Acc(self._V)
+        self.S = _Acc(lambda m, n: np.eye(2 * n_orb) if m == n else np.zeros((2 * n_orb, 2 * n_orb)))
+        self._cache = {}
+        del outer
+
+    def _T(self, m, n):
+        a, b = self._sp[m], self._sp[n]
+        return self.h_sp[np.ix_(a, b)] * (self._spin[:, None] == self._spin[None, :])
+
+    def _eri(self, a, b, c, d):
+        """(ab|cd) for spatial index arrays."""
+        return np.einsum("kab,kcd->abcd", self.L[:, a][:, :, b], self.L[:, c][:, :, d], optimize=True)
+
+    def _V(self, m, n, o, p):
+        key = (m, n, o, p)
+        if key not in self._cache:
+            sa, sb, sc, sd = self._sp[m], self._sp[n], self._sp[o], self._sp[p]
+            sp = self._spin
+            d = (sp[:, None] == sp[None, :]).astype(float)
+            # <ab|cd> = (ac|bd) delta(s_a, s_c) delta(s_b, s_d)
+            phys = self._eri(sa, sc, sb, sd).transpose(0, 2, 1, 3) * d[:, None, :, None] * d[None, :, None, :]
+            # <ab|dc> = (ad|bc) delta(s_a, s_d) delta(s_b, s_c), indexed [a, b, c, d]
+            physx = self._eri(sa, sd, sb, sc).transpose(0, 2, 3, 1) * d[:, None, None, :] * d[None, :, :, None]
+            self._cache[key] = 0.25 * (phys - physx)
+        return self._cache[key]
+
+    def make_states(self, charges, n_states, n_elec_ref=4, n_core=0):
+        """states[m][chg] = (coeffs, masks) from the continued random stream (make_system's)."""
+        out = []
+        for _m in range(self.n_frag):
+            out.append({c: make_states(self.rng, self.n_orb, n_core, n_elec_ref - c, n_states) for c in charges})
+        return out
+
+
 def spin_block_one_electron(h_sp, frag_sizes):
     """A spatial one-electron matrix spin-blocked like spin_orbital_integrals' h."""
     sidx = np.array(spin_orbital_spatial_index(frag_sizes))
