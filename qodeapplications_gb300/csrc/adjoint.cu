@@ -103,9 +103,9 @@ __host__ __device__ __forceinline__ int adj_chunk(int nbp, int nkp) {
 static size_t adj_f32_smem(int max_nb, int max_nk) {
     const int nbp = (max_nb + 3) & ~3, nkp = (max_nk + 3) & ~3;
     size_t stage = 0;
-    for (int b = 4; b <= nbp; b += 4)           // the largest C (nbp' + nkp') over the smaller tasks
+    for (int b = 4; b <= nbp; b += 4)           // the largest C (nbp' + nkp' + 3) over the smaller tasks
         for (int k = 4; k <= nkp; k += 4) {
-            const size_t v = (size_t)adj_chunk(b, k) * (b + k);
+            const size_t v = (size_t)adj_chunk(b, k) * (b + k + 3);
             stage = v > stage ? v : stage;
         }
     return sizeof(float) * (2 * (size_t)nbp * nkp + 2 * stage);
@@ -114,9 +114,9 @@ static size_t adj_f32_smem(int max_nb, int max_nk) {
 // One CTA per operator index.  G[idx] is staged in shared memory in both orientations; the
 // couplings are streamed in stages of C (adj_chunk): the coefficient rows of stage k+1 are
 // gathered with cp.async while stage k is multiplied, with ONE barrier per stage (the buffer a
-// gather overwrites was read in the stage before that barrier).  Signs, P and Q of a work item
-// come from global memory (L1) when its results go out, so no index array sits in shared
-// memory between barriers.
+// gather overwrites was read in the stage before that barrier).  The stage's P, Q and signs are
+// written to shared memory beside its rows (same double buffer), for the atomics that send a
+// work item's results out.
 __device__ __forceinline__ void density_adjoint_f32_body(
     int64_t idx, const int64_t* __restrict__ idx_ptr, const int32_t* __restrict__ P, const int32_t* __restrict__ Q,
     const int8_t* __restrict__ sgn, const float* __restrict__ zb32, int nb, const float* __restrict__ zk32, int nk,
@@ -127,6 +127,8 @@ __device__ __forceinline__ void density_adjoint_f32_body(
     float* gt = g + nbp * nkp;                              // [nkp][nbp]
     float* zb_s = gt + nkp * nbp;                           // [2][C][nbp]
     float* zk_s = zb_s + 2 * C * nbp;                       // [2][C][nkp]
+    int* sPQ = reinterpret_cast<int*>(zk_s + 2 * C * nkp);  // [2][C][2]: P, Q (-1 past the end)
+    float* sS = reinterpret_cast<float*>(sPQ + 4 * C);      // [2][C]: signs
     const int64_t c_begin = idx_ptr[idx], c_end = idx_ptr[idx + 1];
     if (c_begin == c_end) return;
     const double* gi = gT + idx * (int64_t)nb * nk;
@@ -142,6 +144,13 @@ __device__ __forceinline__ void density_adjoint_f32_body(
         const int64_t c0 = c_begin + (int64_t)k * C;
         float* zbb = zb_s + buf * C * nbp;
         float* zkb = zk_s + buf * C * nkp;
+        for (int c = threadIdx.x; c < C; c += blockDim.x) {    // indices of the stage, for its atomics
+            const int64_t cc = c0 + c;
+            const bool in = cc < c_end;
+            sPQ[(buf * C + c) * 2] = in ? __ldg(P + cc) : -1;
+            sPQ[(buf * C + c) * 2 + 1] = in ? __ldg(Q + cc) : -1;
+            sS[buf * C + c] = in ? (__ldg(sgn + cc) < 0 ? -1.f : 1.f) : 0.f;
+        }
         for (int x = threadIdx.x; x < C * gb; x += blockDim.x) {
             const int c = x / gb, part = x - c * gb;
             const int64_t cc = c0 + c;
@@ -164,7 +173,6 @@ __device__ __forceinline__ void density_adjoint_f32_body(
         cp_async_wait<0>();                          // this thread's gathers of stage k landed
         __syncthreads();                             // everyone's landed; stage k-1 fully consumed
         if (k + 1 < n_chunks) stage(k + 1, buf ^ 1); // in flight while stage k is multiplied
-        const int64_t c0 = c_begin + (int64_t)k * C;
         const float* zbb = zb_s + buf * C * nbp;
         const float* zkb = zk_s + buf * C * nkp;
         for (int w = threadIdx.x; w < ket_tiles + bra_tiles; w += blockDim.x) {
@@ -198,12 +206,12 @@ __device__ __forceinline__ void density_adjoint_f32_body(
             const int n_out = ket ? nk : nb;
             const int valid = n_out - o4 < 4 ? n_out - o4 : 4;
             for (int x = 0; x < 4; ++x) {
-                const int64_t cc = c0 + c4 + x;
-                if (cc >= c_end) break;
-                const float sc = __ldg(sgn + cc) < 0 ? -1.f : 1.f;
+                const int row = sPQ[(buf * C + c4 + x) * 2 + (ket ? 1 : 0)];
+                if (row < 0) break;
+                const float sc = sS[buf * C + c4 + x];
 #pragma unroll
                 for (int y = 0; y < 4; ++y) acc[x][y] *= sc;
-                float* dst = ket ? gzkT + (int64_t)__ldg(Q + cc) * nk + o4 : gzbT + (int64_t)__ldg(P + cc) * nb + o4;
+                float* dst = ket ? gzkT + (int64_t)row * nk + o4 : gzbT + (int64_t)row * nb + o4;
                 atomic_add4(dst, acc[x], valid);
             }
         }
