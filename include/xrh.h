@@ -635,8 +635,12 @@ int xrh_gather_submatrix(int n, const int32_t* idx_dev, const double* in_dev, in
 /* Helpers of the device-resident optimizer iteration (no reference counterpart; they keep
  * PyTorch and library kernels out of the captured iteration):
  *   xrh_zero: cudaMemsetAsync of bytes at ptr_dev;
- *   xrh_index_move: dst[idx[i]] = src[i] (gather = 0) or dst[i] = src[idx[i]] (gather = 1),
- *       i < n (a scatter's indices distinct);
+ *   xrh_index_move: dst[idx[i]] = src[i] (gather = 0, indices distinct), dst[i] = src[idx[i]]
+ *       (gather = 1) or dst[idx[i]] += src[i] (gather = 2, FP64 atomic adds: repeated indices
+ *       allowed), i < n;
+ *   xrh_f64_to_f32: dst[i] = (float)src[i], i < n (round to nearest);
+ *   xrh_add_mixed: y[i] += alpha * (x64[i] + x32[i]) with either input NULL for zero (the two
+ *       precision parts of a state gradient summed into an FP64 total);
  *   xrh_spin_sum_antisym: out[a, b] = sum_k (G[s_k(a), s_k(b)] - G[s_k(b), s_k(a)]) with
  *       s_k(a) = so[k * n_sp + a] the spin orbital of spatial orbital a in spin block k: the
  *       antisymmetric spatial orbital gradient from the spin-orbital one;
@@ -654,6 +658,8 @@ typedef struct {
 int xrh_zero(void* ptr_dev, int64_t bytes, void* stream);
 int xrh_index_move(int64_t n, const int64_t* idx_dev, const double* src_dev, double* dst_dev, int gather,
                    void* stream);
+int xrh_f64_to_f32(int64_t n, const double* src_dev, float* dst_dev, void* stream);
+int xrh_add_mixed(int64_t n, double alpha, const double* x64_dev, const float* x32_dev, double* y_dev, void* stream);
 int xrh_spin_sum_antisym(int n_sp, int n_spin, const int32_t* so_dev, const double* G_dev, int64_t ldg,
                          double* out_dev, void* stream);
 int xrh_small_mm_grouped(const xrh_small_mm_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);

@@ -86,6 +86,8 @@ _SIGS = {
     "xrh_gather_submatrix": (_i32, [_i32, _vp, _vp, _i64, _vp, _i64, _vp]),
     "xrh_zero": (_i32, [_vp, _i64, _vp]),
     "xrh_index_move": (_i32, [_i64, _vp, _vp, _vp, _i32, _vp]),
+    "xrh_f64_to_f32": (_i32, [_i64, _vp, _vp, _vp]),
+    "xrh_add_mixed": (_i32, [_i64, _dbl, _vp, _vp, _vp, _vp]),
     "xrh_spin_sum_antisym": (_i32, [_i32, _i32, _vp, _vp, _i64, _vp, _vp]),
     "xrh_small_mm_grouped": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_permute_grouped": (_i32, [_vp, _i32, _i64, _vp]),

@@ -164,8 +164,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 return false;
             };
+            // running (segment, chunk-in-segment) cursors of the loads and the MMAs: a tile's
+            // start is located once (its split-K offset), then each chunk advances the cursor
+            // instead of walking the task's segment list from its first segment again
+            int64_t l_si = 0, l_c = 0, m_si = 0, m_c = 0;
             l_ok = seek(tl, L);
             m_ok = seek(tm, Mi);
+            if (l_ok) { l_si = tasks[L.task].seg_begin; l_c = L.cb; }
+            if (m_ok) { m_si = tasks[Mi.task].seg_begin; m_c = Mi.cb; }
             bool ok = true;
             while (m_ok && ok) {
                 // keep the ring full, across tile boundaries
@@ -176,11 +182,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         ok = false;
                         break;
                     }
-                    const xrh_tc_task& T = tasks[L.task];
-                    int64_t c = L.cb + ql, si = T.seg_begin;
-                    while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
-                    const xrh_tc_segment& S = segs[si];
-                    const int kcoord = (int)(c * KCH);
+                    while (l_c >= segs[l_si].kchunks) { l_c -= segs[l_si].kchunks; ++l_si; }
+                    const xrh_tc_segment& S = segs[l_si];
+                    const int kcoord = (int)(l_c * KCH);
+                    ++l_c;
                     const uint32_t b_bytes = (uint32_t)L.BN * 128u;
                     uint8_t* st = stages + (size_t)s * TC_STAGE_BYTES;
                     const uint32_t bar = smem_u32(&full_bar[s]);
@@ -194,6 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         ql = 0;
                         tl += gridDim.x;
                         l_ok = seek(tl, L);
+                        if (l_ok) { l_si = tasks[L.task].seg_begin; l_c = L.cb; }
                     }
                 }
                 if (!ok) break;
@@ -206,10 +212,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                const xrh_tc_task& T = tasks[Mi.task];
-                int64_t c = Mi.cb + qm, si = T.seg_begin;
-                while (c >= segs[si].kchunks) { c -= segs[si].kchunks; ++si; }
-                const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)Mi.BN, segs[si].negate != 0);
+                while (m_c >= segs[m_si].kchunks) { m_c -= segs[m_si].kchunks; ++m_si; }
+                const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)Mi.BN, segs[m_si].negate != 0);
+                ++m_c;
                 const uint32_t b_bytes = (uint32_t)Mi.BN * 128u;
                 const uint32_t st = smem_u32(stages + (size_t)s * TC_STAGE_BYTES);
                 const uint64_t da_hi = umma_desc_sw128(st), da_lo = umma_desc_sw128(st + TC_A_BYTES);
@@ -230,6 +235,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     qm = 0;
                     tm += gridDim.x;
                     m_ok = seek(tm, Mi);
+                    if (m_ok) { m_si = tasks[Mi.task].seg_begin; m_c = Mi.cb; }
                 }
             }
             if (!ok) {

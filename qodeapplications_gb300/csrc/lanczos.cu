@@ -278,8 +278,9 @@ __global__ void __launch_bounds__(256) gemv_rows_grouped_kernel(const xrh_gemv_t
 // reaches (k+1) * gridDim.x; a wait that exceeds wait_limit polls (LC_WAIT_LIMIT unless the
 // caller of xrh_lanczos_coop_bounded gives another) sets XRH_ERR_TIMEOUT in *status and the CTA
 // returns; every later barrier of the other CTAs then returns too.
-constexpr int LC_THREADS = 256;
+constexpr int LC_THREADS = 512;
 constexpr int LC_WARPS = LC_THREADS / 32;
+constexpr int LC_RPW = 4;                        // rows of H a warp multiplies at once
 constexpr int LC_MAX_CTAS = 256;
 constexpr int LC_ROWS_PER_CTA = 4;
 constexpr long long LC_WAIT_LIMIT = 1LL << 22;   // ~ seconds of polls
@@ -346,6 +347,11 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
     double* p1 = part;                                // [m + 2][nb]: pass-1 dots
     double* p2 = part + (int64_t)ms * nb;             // [m + 2][nb]: pass-2 dots, then |w|^2 at row j + 1
     unsigned int bar = 0;
+    // 16-byte loads of H rows and of V[j] (V rows start at multiples of n; the staged copy
+    // follows c, 16-byte aligned when m is even)
+    const bool vec2 = (n % 2 == 0) && (ld % 2 == 0) && (reinterpret_cast<uintptr_t>(H) % 16 == 0) &&
+                      (reinterpret_cast<uintptr_t>(V) % 16 == 0) &&
+                      (!stage_v || reinterpret_cast<uintptr_t>(vst) % 16 == 0);
     for (int r = tid; r < nr; r += LC_THREADS) {
         const double x = v0[r0 + r];
         V[r0 + r] = x;
@@ -358,32 +364,44 @@ __global__ void __launch_bounds__(LC_THREADS) lanczos_coop_kernel(int64_t n, int
             for (int64_t k = tid; k < n; k += LC_THREADS) vst[k] = __ldcg(vj + k);
             __syncthreads();
         }
-        for (int r = warp; r < nr; r += LC_WARPS) {
-            const double* h = H + (r0 + r) * ld;
-            // four independent chains: the FP64 latency, not its rate, bounds a single chain
-            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-            int64_t k = lane;
-            if (stage_v) {
-                for (; k + 96 < n; k += 128) {
-                    s0 = fma(h[k], vst[k], s0);
-                    s1 = fma(h[k + 32], vst[k + 32], s1);
-                    s2 = fma(h[k + 64], vst[k + 64], s2);
-                    s3 = fma(h[k + 96], vst[k + 96], s3);
-                }
-                for (; k < n; k += 32) s0 = fma(h[k], vst[k], s0);
-            } else {
-                for (; k + 96 < n; k += 128) {
-                    s0 = fma(h[k], __ldcg(vj + k), s0);
-                    s1 = fma(h[k + 32], __ldcg(vj + k + 32), s1);
-                    s2 = fma(h[k + 64], __ldcg(vj + k + 64), s2);
-                    s3 = fma(h[k + 96], __ldcg(vj + k + 96), s3);
-                }
-                for (; k < n; k += 32) s0 = fma(h[k], __ldcg(vj + k), s0);
-            }
-            double s = (s0 + s1) + (s2 + s3);
+        // w_R = H_R V[j]: a warp multiplies LC_RPW rows at once, so that one load of V[j] serves
+        // them all, with 16-byte loads when the rows allow it: the loop is bound by the bytes in
+        // flight per SM, which one 8-byte row stream per warp keeps far below what HBM takes
+        for (int rb = warp * LC_RPW; rb < nr; rb += LC_WARPS * LC_RPW) {
+            const int nrow = (nr - rb < LC_RPW) ? nr - rb : LC_RPW;
+            const double* h[LC_RPW];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) w[r] = s;
+            for (int q = 0; q < LC_RPW; ++q) h[q] = H + (r0 + rb + (q < nrow ? q : nrow - 1)) * ld;
+            double s[LC_RPW][2];
+#pragma unroll
+            for (int q = 0; q < LC_RPW; ++q) s[q][0] = s[q][1] = 0.0;
+            if (vec2) {
+                const int64_t n2 = n >> 1;
+                const double2* x2 = stage_v ? reinterpret_cast<const double2*>(vst) : reinterpret_cast<const double2*>(vj);
+#pragma unroll 2
+                for (int64_t k = lane; k < n2; k += 32) {
+                    const double2 x = stage_v ? x2[k] : __ldcg(x2 + k);
+#pragma unroll
+                    for (int q = 0; q < LC_RPW; ++q) {
+                        const double2 y = __ldg(reinterpret_cast<const double2*>(h[q]) + k);
+                        s[q][0] = fma(y.x, x.x, s[q][0]);
+                        s[q][1] = fma(y.y, x.y, s[q][1]);
+                    }
+                }
+            } else {
+                for (int64_t k = lane; k < n; k += 32) {
+                    const double x = stage_v ? vst[k] : __ldcg(vj + k);
+#pragma unroll
+                    for (int q = 0; q < LC_RPW; ++q) s[q][0] = fma(__ldg(h[q] + k), x, s[q][0]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < LC_RPW; ++q) {
+                double t = s[q][0] + s[q][1];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                if (lane == 0 && q < nrow) w[rb + q] = t;
+            }
         }
         double a = 0.0;
         double cc2 = 0.0;

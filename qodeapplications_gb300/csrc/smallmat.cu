@@ -208,8 +208,23 @@ __global__ void index_move_kernel(int64_t n, const int64_t* __restrict__ idx, co
                                   double* __restrict__ dst, int gather) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (gather) dst[i] = src[idx[i]];
+    if (gather == 1) dst[i] = src[idx[i]];
+    else if (gather == 2) atomicAdd(dst + idx[i], src[i]);
     else dst[idx[i]] = src[i];
+}
+
+__global__ void add_mixed_kernel(int64_t n, double alpha, const double* __restrict__ x64,
+                                 const float* __restrict__ x32, double* __restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = x64 ? x64[i] : 0.0;
+    if (x32) v += (double)x32[i];
+    y[i] += alpha * v;
+}
+
+__global__ void f64_to_f32_kernel(int64_t n, const double* __restrict__ src, float* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
 }
 
 __global__ void spin_sum_antisym_kernel(int n_sp, int n_spin, const int32_t* __restrict__ so,
@@ -259,11 +274,30 @@ extern "C" int xrh_zero(void* ptr_dev, int64_t bytes, void* stream) {
 
 extern "C" int xrh_index_move(int64_t n, const int64_t* idx_dev, const double* src_dev, double* dst_dev, int gather,
                               void* stream) {
-    if (n < 0 || (n > 0 && (!idx_dev || !src_dev || !dst_dev))) return XRH_ERR_ARG;
+    if (n < 0 || gather < 0 || gather > 2 || (n > 0 && (!idx_dev || !src_dev || !dst_dev))) return XRH_ERR_ARG;
     if (n == 0) return XRH_OK;
     if ((n + 255) / 256 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     index_move_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, idx_dev, src_dev, dst_dev,
                                                                                    gather);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_add_mixed(int64_t n, double alpha, const double* x64_dev, const float* x32_dev, double* y_dev,
+                             void* stream) {
+    if (n < 0 || (n > 0 && (!y_dev || (!x64_dev && !x32_dev)))) return XRH_ERR_ARG;
+    if (n == 0) return XRH_OK;
+    if ((n + 255) / 256 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    add_mixed_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, alpha, x64_dev, x32_dev, y_dev);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
+extern "C" int xrh_f64_to_f32(int64_t n, const double* src_dev, float* dst_dev, void* stream) {
+    if (n < 0 || (n > 0 && (!src_dev || !dst_dev))) return XRH_ERR_ARG;
+    if (n == 0) return XRH_OK;
+    if ((n + 255) / 256 > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    f64_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, src_dev, dst_dev);
     XRH_CHECK_LAUNCH();
     return XRH_OK;
 }
