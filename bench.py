@@ -38,6 +38,11 @@ CONFIGS = {
                                       "sector (+1,0,-1; 3/4/5 electrons), order-0 XR-H 900x900"),
     3: dict(n_orb=14, n_states=60, name="dimer 2x14 spatial orbitals (28 spin orbitals each), 60 states per charge "
                                        "sector (+1,0,-1), order-0 XR-H 32400x32400"),
+    4: dict(n_orb=14, n_states=100, n_frag=8,
+            name="ring of 8 fragments x 14 spatial orbitals (28 spin orbitals each), 100 states per charge sector "
+                 "(+1,0,-1): all 28 pairs (neutral sectors, 30 000 states, with the state gradient of the pair "
+                 "expansion) and the 8 nearest-neighbour triples (neutral sectors, 7 000 000 states, matrix-free "
+                 "H x v)"),
 }
 SEED = 1234
 METRIC = "XR-H build+grad s/iter vs plain FP64 GPU, at |dE|<=1e-6 Eh vs FP64 oracle"
@@ -55,6 +60,7 @@ def parse():
     p.add_argument("--no-variants", action="store_true")
     p.add_argument("--states", type=int, default=None, help="states per charge sector (default: the config's)")
     p.add_argument("--orbitals", type=int, default=None, help="spatial orbitals per fragment (default: the config's)")
+    p.add_argument("--no-triples", action="store_true", help="ring (config 4): pairs and monomers only")
     return p.parse_args()
 
 
@@ -821,6 +827,151 @@ def run_trimer(args):
     print(json.dumps(line))
 
 
+def run_ring(args):
+    """Ring of 8 fragments: one step = every pair (densities, neutral-sector build, converged
+    FP64 Lanczos, reverse pass into the state gradient of the pair expansion E2), the monomer
+    terms, and every nearest-neighbour triple (densities, pair sectors, trimer stage,
+    restarted matrix-free Lanczos with the Krylov loop as a CUDA graph), each ground state
+    from the same fixed start vector to a residual of 1e-6.  Variant: the FP64 pair phase
+    (E2 and its gradient) for the accuracy and speed of the split form."""
+    import torch
+    from qodeapplications_gb300 import _lib
+    from qodeapplications_gb300.ring import XRRing
+    if int(os.environ.get("RANK", "0")) != 0:
+        return                       # one ring on one GPU: under torchrun rank 0 alone runs it
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    c = dict(CONFIGS[4])
+    n_states = args.states or c["n_states"]
+    n_orb = args.orbitals or c["n_orb"]
+    name = c["name"]
+    if args.states or args.orbitals:
+        name = (f"ring of 8 fragments x {n_orb} spatial orbitals ({2 * n_orb} spin orbitals each), {n_states} "
+                "states per charge sector (+1,0,-1): all 28 pairs (neutral sectors) and the 8 nearest-neighbour "
+                "triples (neutral sectors)")
+    triples = not args.no_triples
+    if not triples:
+        name = name.split(" and the 8 nearest")[0].replace("all 28 pairs", "all 28 pairs and the monomers")
+    head = args.precision if args.precision in ("tf32x3", "bf16x3", "fp64") else "tf32x3"
+    tol = 1e-6
+
+    def log(msg):
+        print(msg, file=sys.stderr, flush=True)
+
+    t_setup = time.time()
+    ring = XRRing(n_frag=c["n_frag"], n_orb=n_orb, n_states=n_states, precision=head, triples=triples, tol=tol,
+                  seed=SEED)
+    log(f"ring set up in {time.time() - t_setup:.1f} s, {torch.cuda.max_memory_allocated() / 1e9:.1f} GB allocated")
+    host = [{q: z.cpu().pin_memory() for q, z in zf.items()} for zf in ring.coeffs]
+    for _ in range(max(args.warmup, 3)):
+        t0 = time.time()
+        ring.iterate()
+        log(f"warm-up iteration {time.time() - t0:.1f} s  phases {ring.phase_ms}")
+    ring.check_status()
+    torch.cuda.synchronize()
+    _lib.LaunchCounter.count = 0
+    ms, outs, phases = [], [], []
+    clock_path = os.path.join(tempfile.gettempdir(), f"xrh_clocks_r_{os.getpid()}.csv")
+    with ClockSampler(clock_path) as cs:
+        torch.cuda.nvtx.range_push("xrh_timed")
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            outs.append(ring.iterate())
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            phases.append(dict(ring.phase_ms))
+        torch.cuda.nvtx.range_pop()
+    launches = _lib.LaunchCounter.count
+    clocks = cs.summary(local)
+    s_per_iter = sum(ms) / 1e3 / args.steps
+    resid_max = max(ring.resid.values())
+    g_split = [{q: g.clone() for q, g in gf.items()} for gf in ring.grad]
+    # e2e: coefficients from pinned host memory in, the two energies out, every step
+    e2e = []
+    for _ in range(args.steps):
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for f, zf in enumerate(ring.coeffs):
+            for q, z in zf.items():
+                z.copy_(host[f][q], non_blocking=True)
+        ring.iterate()
+        t1.record()
+        torch.cuda.synchronize()
+        e2e.append(t0.elapsed_time(t1))
+    h2d = sum(t.numel() * 8 for d in host for t in d.values())
+    # dominant kernel: stage B of the triples' H x v (or the density adjoint without triples)
+    roof = None
+    if triples and head != "fp64":
+        st = ring.slot.stage_b
+        st.run()
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(5):
+            st.run()
+        t1.record()
+        torch.cuda.synchronize()
+        sb_ms = t0.elapsed_time(t1) / 5
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+        peak = float(peaks.get("bf16_tflops", 1900.0))
+        tfl = st.flops / (sb_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": "triple H x v stage B (gemm_tc_kernel)", "achieved": tfl,
+                "unit": "TFLOP/s", "launch_ms": sb_ms, "flops_per_launch": st.flops, "peak": peak,
+                "frac": tfl / peak, "traffic": None,
+                "note": "achieved = algorithmic FLOPs (2 n^4 N^2 per trimer block) / CUDA-event time of the launch; "
+                        "split forms issue 3 MMAs per algorithmic FLOP; peak = MEASURED_PEAKS.json bf16_tflops "
+                        "(of measured)",
+                "hv_gflop": ring.slot.flops_apply / 1e9}
+    rec = {"s_per_iter": s_per_iter, "E2": outs[-1]["E2"], "E3": outs[-1]["E3"], "phases_ms": phases[-1],
+           "max_lanczos_residual": resid_max, "n_pairs": len(ring.pairs), "n_triples": len(ring.triples)}
+    variants = {head: rec}
+    del ring
+    torch.cuda.empty_cache()
+    if not args.no_variants and head != "fp64":
+        # FP64 pair phase: E2 and its gradient, one iteration
+        r64 = XRRing(n_frag=c["n_frag"], n_orb=n_orb, n_states=n_states, precision="fp64", triples=False, tol=tol,
+                     seed=SEED)
+        r64.iterate()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        o64 = r64.iterate()
+        t1.record()
+        torch.cuda.synchronize()
+        num = den = 0.0
+        for f in range(len(g_split)):
+            for q in g_split[f]:
+                num += float((r64.grad[f][q] - g_split[f][q]).norm()) ** 2
+                den += float(r64.grad[f][q].norm()) ** 2
+        variants["fp64_pairs"] = {"s_per_iter_pairs": t0.elapsed_time(t1) / 1e3, "E2": o64["E2"],
+                                  "max_lanczos_residual": max(r64.resid.values())}
+        rec["dE2_vs_fp64"] = abs(rec["E2"] - o64["E2"])
+        rec["state_grad_rel_vs_fp64"] = (num / den) ** 0.5 if den > 0 else None
+        rec["pairs_speedup_vs_fp64"] = variants["fp64_pairs"]["s_per_iter_pairs"] / (rec["phases_ms"]["pairs"] / 1e3)
+        del r64
+        torch.cuda.empty_cache()
+    line = {
+        "metric": "XR ring build + gradient s/iter (pair expansion E2 with its state gradient, nearest-neighbour "
+                  "triple increments E3)",
+        "value": s_per_iter, "unit": "s/iter", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": s_per_iter * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if head == "fp64" else f"{head} (pair builds and triple H x v on tcgen05; FP64 Lanczos)",
+        "data": "synthetic (seeded h ~ N(0,0.1), V = sum_K L L with K=40, Sz-definite QR-orthonormal Gaussian CI "
+                "vectors), the ChainIntegralSource ring",
+        "config": {"workload": name, "lanczos_residual_tol": tol,
+                   "l2": "inputs larger than L2 (pair sector matrices of 7.2 GB, densities of several GB)",
+                   "step": "28 pair builds + Lanczos + reverse passes, 8 monomer ground states, 8 triple builds + "
+                           "restarted matrix-free Lanczos (each from one fixed start vector)"},
+        "e2e": {"value": sum(e2e) / 1e3 / args.steps, "unit": "s/iter", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 16},
+        "gpu_launches": launches, "clocks": clocks, "E2": rec["E2"], "E3": rec["E3"], "roofline": roof,
+        "variants": variants,
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -828,6 +979,10 @@ def run_reference(args):
     if args.config == 2:
         print(json.dumps({"impl": "reference", "unavailable": "the reference diagonalises the dense three-fragment "
                           "H, 1.7 M x 1.7 M at this size (23 TB in FP64); no CPU run of it is possible"}))
+        return
+    if args.config == 4:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference forms the product-basis H of all eight "
+                          "fragments (300^8 states); no CPU run of it is possible"}))
         return
     sysd = make_system(args.config, args.states, args.orbitals)
     times, extra = [], {}
@@ -866,5 +1021,7 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.config == 2:
         run_trimer(a)
+    elif a.config == 4:
+        run_ring(a)
     else:
         run_ours(a)

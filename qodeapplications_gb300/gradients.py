@@ -30,11 +30,19 @@ ORBITAL_FUSED = True  # integral derivatives of the orbital gradient by xrh_orbi
 GAMMA_TC_MIN = 0      # Gamma pair blocks with n * n_K >= this go to the tensor cores (3 x TF32)
 
 class XRDimerAdjoint:
-    def __init__(self, plan, density_adjoint="simt"):
+    def __init__(self, plan, density_adjoint="simt", monomer_terms=False, scratch=None):
         """density_adjoint: 'simt' (the grouped CUDA-core kernel) or 'tc' (tensor cores, split-
         precision plans with at most 64 states per side; exact to the same tolerance but slower
         at 2 x 9 / 10 and 2 x 14 / 60 states: one CTA per SM runs its gather, MMA and atomic
-        phases in sequence)."""
+        phases in sequence).
+        monomer_terms: every monomer block's G gets -dmono[m][c] dmono[m][c]^T added (the
+        vectors self.dmono, zero unless the caller writes them before launch): the reverse pass
+        of E - sum_m u_m^T H1_m u_m with dmono = u_m, so a larger system folds its monomer
+        energy terms (weighted ground vectors of H1_m) into the pair reverse passes.
+        scratch: FP64 device tensors whose memory the transposed density gradients may take
+        (they are written and read inside launch() only): working buffers of another
+        computation that never runs between the launches of one reverse pass, on the same
+        stream; what does not fit is allocated."""
         assert plan.output == "full", "the adjoint differentiates the full H (H2 + H1 x 1 + 1 x H1)"
         self.plan = plan
         self._spatial_cache = {}
@@ -100,18 +108,23 @@ class XRDimerAdjoint:
 
         # the adjoint contractions run in FP32 (FP64 sums) on the split-precision paths
         gprec = "fp64" if plan.dens_precision == "fp64" else "fp32"
+        self.dmono = None
+        if monomer_terms:
+            self.dmono = [{c: torch.zeros(ns[m][c], **f64) for c in plan.H1blk[m]} for m in (0, 1)]
         # ---- launch 1: G blocks, Y and Z per final segment ----
         L1 = GroupedGemm(dev, gprec)
         for m in (0, 1):
             for c in plan.H1blk[m]:
                 n = ns[m][c]
                 gb = G[("gblk", m, c)]
+                # - u u^T of a folded monomer term (one K = 1 segment of the same task)
+                extra = [(self.dmono[m][c], 1, self.dmono[m][c], 1, 1, -1.0)] if monomer_terms else []
                 if m == 0:      # G0[i,j] = sum_b D[off+i, b] D[off+j, b]
                     Dsub = Dflat[off0[c] * tot1:]
-                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot1, 1.0)], gb, n)
+                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot1, 1.0)] + extra, gb, n)
                 else:           # G1[i,j] = sum_a D[a, off+i] D[a, off+j]
                     Dsub = Dflat[off1[c]:]
-                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot0, 1.0, 3, 0, 0)], gb, n)
+                    L1.add(n, n, [(Dsub, tot1, Dsub, tot1, tot0, 1.0, 3, 0, 0)] + extra, gb, n)
         self.final_adj = []
         for i, t in enumerate(plan.final_tasks):
             ci0, ci1, cj0, cj1 = t["key"]
@@ -280,6 +293,19 @@ class XRDimerAdjoint:
         self.gam_reg.upload()
         self.Lgamma_tc = Lgt.finalize().autotune()
 
+        pool = [t.reshape(-1) for t in (scratch or ())]
+        pool_off = [0] * len(pool)
+
+        def take(n):
+            """n FP64 elements from the scratch tensors (256-byte aligned pieces), else new."""
+            n_al = (n + 31) // 32 * 32
+            for i, t_ in enumerate(pool):
+                if t_.dtype == torch.float64 and t_.data_ptr() % 256 == 0 and pool_off[i] + n_al <= t_.numel():
+                    v = t_[pool_off[i]:pool_off[i] + n]
+                    pool_off[i] += n_al
+                    return v
+            return torch.empty(n, **f64)
+
         self.dens_adj = []
         self.mirror_adj = []      # (d rho of a mirrored block, d rho of its partner, partner dims, N, L)
         self.im_adj = []          # intermediate-determinant builders: (builder, density gradients, gzT)
@@ -304,7 +330,7 @@ class XRDimerAdjoint:
                     self.mirror_adj.append((grad_of[rt.data_ptr()], grad_of[b.rho[mir[0]][mir[1:]].data_ptr()],
                                             rt.shape[1], rt.shape[0], plan.N[m], len(op)))
                     continue
-                gT = torch.empty(cp.K * rt.shape[0] * rt.shape[1], **f64)
+                gT = take(cp.K * rt.shape[0] * rt.shape[1])
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
         self.dens_adj_all = list(self.dens_adj)
         # FP32 path: every block of a fragment in one grouped launch, on the tensor cores when
@@ -451,8 +477,9 @@ class XRDimerAdjoint:
         self.Lgamma.run()
         self.Lgamma_tc.run()
         for (m, idx, vals) in self.gam_scatter:
-            # every pair block of the fragment into the N^4 Gamma in one atomic index-add
-            self.G[("Gamma", m)].index_add_(0, idx, vals)
+            # every pair block of the fragment (all charges) into the N^4 Gamma in one atomic
+            # scatter-add
+            call("xrh_index_move", idx.numel(), ptr(idx), ptr(vals), ptr(self.G[("Gamma", m)]), 2, s)
         for (m, c) in self.gamma_old:
             sp = plan.spaces[m]
             call("xrh_ccaa_weighted", _lib.FP32 if self.prec32 else _lib.FP64, sp.n_orbs, ptr(sp.masks[c]),
@@ -636,7 +663,7 @@ class XRDimerAdjoint:
             # with Gbar = B / 8: a t x t result over t^3 terms, split over CTAs by xrh_abt_small
             # (FP32 products on the split-precision paths)
             if self.prec32:
-                b["A"].copy_(V)
+                call("xrh_f64_to_f32", V.numel(), ptr(V), ptr(b["A"]), s)
             K3 = t ** 3
             call("xrh_abt_small", prec, t, t, K3, ptr(b["A"]), K3, ptr(b["B"]), K3, 0.5, ptr(Gso), s)
         if b is None:

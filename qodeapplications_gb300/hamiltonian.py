@@ -341,6 +341,13 @@ class XRDimerPlan:
               sigma vectors through (n-2)-electron pair intermediates, rho^ccaa never
               stored), 'ccaa' (a stored rho^ccaa block per charge, contracted with V as
               SV_1mer_0.py:24 does; for densities handed in by a caller) or 'none'.
+    total_charges: with layout='sector', the total charges whose sectors are built (None: all);
+              H conserves the total charge, so the other sectors are never needed when the
+              eigenvector is sought in one of these (the pairs of a neutral ring).
+    registry: a SplitRegistry shared with other plans over the same density builders (split
+              precision): each builder's densities are split copies held once, in the split
+              group named by the builder (builder.split_group); precontraction outputs and
+              integral matrices stay in groups of this plan.
 
     The inputs are the persistent coefficient buffers self.coeffs[m][charge]
     (n_states x n_conf); launch() enqueues the whole build on the current stream without
@@ -349,9 +356,12 @@ class XRDimerPlan:
 
     def __init__(self, spaces, n_states, charges, ints, output="full", precision="fp64",
                  convention="hermitian", layout="product", dens_precision=None, sigma_precision=None,
-                 autotune=True, builders=None, monomer_2e="sigma"):
+                 autotune=True, builders=None, monomer_2e="sigma", total_charges=None, registry=None):
         if monomer_2e not in ("sigma", "ccaa", "none"):
             raise ValueError("monomer_2e must be 'sigma', 'ccaa' or 'none'")
+        if total_charges is not None and layout == "product":
+            raise ValueError("total_charges needs the sector layout")
+        self.total_charges = None if total_charges is None else set(total_charges)
         self.monomer_2e = monomer_2e
         self.spaces, self.charges = spaces, [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
@@ -525,6 +535,8 @@ class XRDimerPlan:
             for c0 in chg[0]:
                 for c1 in chg[1]:
                     t = c0 + c1
+                    if self.total_charges is not None and t not in self.total_charges:
+                        continue
                     sec = self.sectors.setdefault(t, dict(base={}, dim=0, rows=[]))
                     sec["base"][c0] = sec["dim"]
                     i0 = np.repeat(np.arange(nb[0][c0]), nb[1][c1])
@@ -546,6 +558,8 @@ class XRDimerPlan:
                 for cj0 in chg[0]:
                     for cj1 in chg[1]:
                         if ci0 + ci1 != cj0 + cj1:
+                            continue
+                        if self.total_charges is not None and ci0 + ci1 not in self.total_charges:
                             continue
                         d0 = ci0 - cj0
                         if abs(d0) > 2:
@@ -611,12 +625,30 @@ class XRDimerPlan:
         # ---- split-precision tensor-core variant of both launches ----
         self.tc = self.precision in (_lib.BF16X3, _lib.TF32X3)
         if self.tc:
-            reg = SplitRegistry(precision, dev)
+            reg = registry if registry is not None else SplitRegistry(precision, dev)
+            tag = "%x" % id(self)
+            self._grp_P, self._grp_W = "P" + tag, "W" + tag
             p_ptrs = {t.data_ptr() for t in self.P.values()}
             w_ptrs = {t.data_ptr() for t in W.values()}
+            # every density builder's blocks form one split group, shared by the plans that hold it
+            b_of = {}
+            for b in self.builders:
+                if getattr(b, "split_group", None) is None:
+                    b.split_group = "in%x" % id(b)
+                for blocks in b.rho.values():
+                    for t_ in blocks.values():
+                        b_of[t_.data_ptr()] = b.split_group
+            self._grp_in = set()
 
             def grp(t):
-                return "P" if t.data_ptr() in p_ptrs else ("W" if t.data_ptr() in w_ptrs else "in")
+                p_ = t.data_ptr()
+                if p_ in p_ptrs:
+                    return self._grp_P
+                if p_ in w_ptrs:
+                    return self._grp_W
+                g_ = b_of.get(p_, "in" + tag)
+                self._grp_in.add(g_)
+                return g_
 
             pre_tc = TCGroupedGemm(reg)
             for out, segs_ in self.pre_specs:
@@ -632,7 +664,8 @@ class XRDimerPlan:
                 fin_tc.add(t["M"], t["N"], t["segs"], t["C"], t["ldc"], mode=2, maps=t["maps"], DA=t["DA"],
                            DB=t["DB"], groups=[(grp(a[0]), grp(a[2])) for a in t["segs"]])
             reg.upload()
-            reg.split("W")
+            reg.split(self._grp_W)
+            self._grp_in = sorted(self._grp_in)
             self.reg, self.pre_tc, self.pre64, self.fin_tc = reg, pre_tc.finalize(), pre64.finalize(), fin_tc.finalize()
             if autotune:
                 self.pre_tc.autotune()
@@ -671,8 +704,39 @@ class XRDimerPlan:
                 sg.set_V(ints.V(m, m, m, m))
         self.sigma_batch.refresh_W()
         if self.tc:
-            self.reg.split("W")
+            self.reg.split(self._grp_W)
         self.ints = ints
+
+    def integral_set(self, ints):
+        """Device copies of everything set_integrals writes for these integrals (the integral
+        matrices and each monomer sigma's V and pair-class W), for load_integral_set: one plan
+        then serves many fragment pairs of a larger system, each with its own prepared set."""
+        S = {("W", k): w.contiguous() for k, w in self._integral_matrices(ints).items()}
+        for m in (0, 1):
+            Vm = ints.V(m, m, m, m).contiguous()
+            S[("sV", m)] = Vm.clone()            # never an alias of a cached block
+            for c, sg in self.sigma[m].items():
+                if sg.pl is not None:
+                    for k, (u, v) in enumerate(sg._uv):
+                        S[("sW", m, c, k)] = (4.0 * Vm[u[:, None], v[:, None], u[None, :], v[None, :]]).contiguous()
+        return S
+
+    def load_integral_set(self, S):
+        """set_integrals from a prepared integral_set: device-to-device copies and the operand
+        splits of the split-precision paths, nothing else, on the current stream."""
+        for k, w in self.W.items():
+            w.copy_(S[("W", k)])
+        for m in (0, 1):
+            for c, sg in self.sigma[m].items():
+                sg.V.copy_(S[("sV", m)])
+                if sg.pl is not None:
+                    for k, W in enumerate(sg.W):
+                        W.copy_(S[("sW", m, c, k)])
+                    if sg.reg is not None:
+                        sg.reg.split("sigW")
+        self.sigma_batch.refresh_W()
+        if self.tc:
+            self.reg.split(self._grp_W)
 
     def set_coeffs(self, coeffs):
         """Copy new state coefficients {charge: (n_states, n_conf)} per fragment into the plan."""
@@ -680,9 +744,10 @@ class XRDimerPlan:
             for c in self.charges[m]:
                 self.coeffs[m][c].copy_(coeffs[m][c], non_blocking=True)
 
-    def launch(self, build_densities=True):
+    def launch(self, build_densities=True, split_inputs=True):
         """Enqueue the whole build (densities, sigma, precontractions, final blocks); with
-        build_densities=False the density builders are taken as already built."""
+        build_densities=False the density builders are taken as already built, with
+        split_inputs=False (split precision) their split copies too."""
         for m in (0, 1):
             if build_densities:
                 self.builders[m].build(self.coeffs[m])
@@ -700,10 +765,12 @@ class XRDimerPlan:
             atd, n_a, ctas = self.mono_abt
             call("xrh_abt_grouped", _lib.FP64, ptr(atd), n_a, ctas, s)
         if self.tc:
-            self.reg.split("in")
+            if split_inputs:
+                for g in self._grp_in:
+                    self.reg.split(g)
             self.pre_tc.run()
             self.pre64.run()
-            self.reg.split("P")
+            self.reg.split(self._grp_P)
             self.fin_tc.run()
         else:
             self.pre.run()

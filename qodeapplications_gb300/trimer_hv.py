@@ -84,13 +84,18 @@ class TrimerHvPlan:
     Ns:          spin orbitals per fragment
     avail:       avail(f, op, bra_chg, ket_chg) -> True when fragment f has that density block
     total_charge: None for the whole product space, or one total charge (H conserves it)
+    monomer_scale: factor of the monomer tasks: 1 when the pair blocks are the dimer couplings
+                 alone (XRDimerPlan output 'split'); -1 when they are the full pair
+                 Hamiltonians H1 x 1 + 1 x H1 + H2 (output 'full'), which count every monomer
+                 twice over the three pairs
 
     Buffers are named: 'v', 'w' (the vectors), 'vXYZ'/'wXYZ' (permuted copies for fragment
     order XYZ), 'Pt', 'R3t', 'T1', 'T2', 'T2p' (intermediates, sizes in self.sizes) and external
     keys ('rho', f, op, bc, kc), ('H1', f, c), ('H2', pair, t), ('W', kind, order),
     ('Uq', order), ('eye', n).  A reference is (buffer, element offset)."""
 
-    def __init__(self, charges, n_states, n_elec, Ns, avail, total_charge=None):
+    def __init__(self, charges, n_states, n_elec, Ns, avail, total_charge=None, monomer_scale=1.0):
+        self.monomer_scale = float(monomer_scale)
         self.charges = [list(c) for c in charges]
         self.ns = [dict(n) for n in n_states]
         self.n_elec = list(n_elec)
@@ -131,19 +136,22 @@ class TrimerHvPlan:
     def _monomers(self, avail):
         """H1_f on axis f of every block (build_H.py:38-47); fragment f has a monomer block
         for charge c when it has the rho^ca block (c, c)."""
+        a = self.monomer_scale
         for t in self.triples:
             n0, n1, n2 = self.shape[t]
             o = self.off[t]
             if avail(0, "ca", t[0], t[0]):
                 self.launches[0].append(_task(n0, n1 * n2, ("w", o), n1 * n2,
-                                              [_seg((("H1", 0, t[0]), 0), n0, ("v", o), n1 * n2, n0, flags=2)]))
+                                              [_seg((("H1", 0, t[0]), 0), n0, ("v", o), n1 * n2, n0, alpha=a,
+                                                    flags=2)]))
             if avail(1, "ca", t[1], t[1]):
                 self.launches[0].append(_task(n1, n2, ("w", o), n2,
-                                              [_seg((("H1", 1, t[1]), 0), n1, ("v", o), n2, n1, flags=2, sB=n1 * n2)],
+                                              [_seg((("H1", 1, t[1]), 0), n1, ("v", o), n2, n1, alpha=a, flags=2,
+                                                    sB=n1 * n2)],
                                               batch=n0, sC=n1 * n2))
             if avail(2, "ca", t[2], t[2]):
                 self.launches[0].append(_task(n0 * n1, n2, ("w", o), n2,
-                                              [_seg(("v", o), n2, (("H1", 2, t[2]), 0), n2, n2)]))
+                                              [_seg(("v", o), n2, (("H1", 2, t[2]), 0), n2, n2, alpha=a)]))
 
     def _pairs(self):
         """(H2_ab x 1_s) v for the three pairs, every source block in one task per output block."""
@@ -373,6 +381,13 @@ class XRTrimerHamiltonian:
                   'tf32x3' / 'bf16x3' (the dominant stage on the tensor cores in split precision,
                   the rest with FP32 products and FP64 sums)
     total_charge: restrict the vector to one total charge (None: the whole product space)
+    pair_output:  'split' (pair plans hold the dimer couplings H2) or 'full' (they hold the
+                  full pair Hamiltonians, which then also serve pair energies and their reverse
+                  pass; the monomer terms of the product enter with factor -1)
+    builders:     three DensityBuilder objects to use instead of the object's own
+    pair_terms_tc: split forms only: the pair terms of the product on the tensor cores (True;
+                  the pair sector matrices are then held a second time as split copies) or
+                  with FP32 products and FP64 sums on the CUDA cores (False, no copies)
 
     build(coeffs) runs the three pair builds (densities, monomer and dimer blocks) and the
     per-build trimer stage; apply(x) then returns H x as a device vector in block layout
@@ -381,22 +396,36 @@ class XRTrimerHamiltonian:
     uploaded once, so a build or a product can be captured in a CUDA graph."""
 
     def __init__(self, spaces, n_states, charges, ints, precision="fp64", hv_precision="fp64", total_charge=None,
-                 autotune=True):
+                 autotune=True, pair_output="split", builders=None, pair_terms_tc=True):
         from .densities import DensityBuilder
         from .hamiltonian import XRDimerPlan
+        if pair_output not in ("split", "full"):
+            raise ValueError("pair_output must be 'split' or 'full'")
         dev = spaces[0].device
         self.device = dev
         self.charges = [list(c) for c in charges]
         self.n_states = [dict(n) for n in n_states]
+        self.pair_output = pair_output
         # one density builder per fragment, shared by the two pair plans that hold it (FP32
         # products on the split-precision paths, as XRDimerPlan chooses for its own)
         dens_precision = "fp32" if precision in ("bf16x3", "tf32x3") else "fp64"
-        self.builders = [DensityBuilder(spaces[f], self.n_states[f], precision=dens_precision) for f in range(3)]
+        self.builders = list(builders) if builders is not None else [
+            DensityBuilder(spaces[f], self.n_states[f], precision=dens_precision) for f in range(3)]
+        # pair sectors a restricted vector reaches: total charge minus the spectator's charge
+        pair_sectors = [None] * 3
+        if total_charge is not None:
+            for p, (a, b) in enumerate(PAIRS):
+                s_ = 3 - a - b
+                pair_sectors[p] = sorted({total_charge - c for c in self.charges[s_]})
+        # the three pair plans share one split registry: each fragment's densities are split once
+        from .gemm import SplitRegistry
+        self.pair_registry = SplitRegistry(precision, dev) if precision in ("bf16x3", "tf32x3") else None
         self.plans = [XRDimerPlan([spaces[a], spaces[b]], [self.n_states[a], self.n_states[b]],
-                                  [self.charges[a], self.charges[b]], _PairIntegrals(ints, (a, b)), output="split",
+                                  [self.charges[a], self.charges[b]], _PairIntegrals(ints, (a, b)), output=pair_output,
                                   precision=precision, convention="general", layout="sector", autotune=autotune,
-                                  builders=[self.builders[a], self.builders[b]])
-                      for a, b in PAIRS]
+                                  builders=[self.builders[a], self.builders[b]], total_charges=pair_sectors[p],
+                                  registry=self.pair_registry)
+                      for p, (a, b) in enumerate(PAIRS)]
         # each fragment's coefficient buffers and monomer blocks from one pair plan that holds it
         holder = {0: (0, 0), 1: (0, 1), 2: (1, 1)}
         self.rho = [b.rho for b in self.builders]
@@ -407,12 +436,15 @@ class XRTrimerHamiltonian:
             return (bc, kc) in self.rho[f].get(op, {})
 
         plan = TrimerHvPlan(self.charges, self.n_states, [sp.n_elec_ref for sp in spaces], [sp.N for sp in spaces],
-                            avail, total_charge)
+                            avail, total_charge, monomer_scale=-1.0 if pair_output == "full" else 1.0)
         if plan.dim == 0:
             raise ValueError(f"no product state has total charge {total_charge}")
         self.plan = plan
+        self.total_charge = total_charge
         for p, lay in enumerate(plan.pair_layout):
             for t, (base, dimt) in lay.items():
+                if t not in self.plans[p].sectors:
+                    continue            # a sector the restricted vector never reaches
                 sec = self.plans[p].sectors[t]
                 assert sec["dim"] == dimt and sec["base"] == base, "pair sector layout mismatch"
         f64 = dict(dtype=torch.float64, device=dev)
@@ -447,7 +479,7 @@ class XRTrimerHamiltonian:
         # per build; the monomer terms and the per-build stage keep FP32 products / FP64 sums
         self.tc = hv_precision in ("bf16x3", "tf32x3")
         simt = "fp32" if self.tc else hv_precision
-        tc_roles = ("pair", "A", "B", "C") if self.tc else ()
+        tc_roles = (("pair",) if pair_terms_tc else ()) + ("A", "B", "C") if self.tc else ()
         self.stage1 = self._grouped(plan.build_tasks, simt)
         self.simt = [self._grouped([t for t in L if t.get("role") not in tc_roles], simt) for L in plan.launches]
         self.tcs = [[] for _ in plan.launches]
@@ -518,6 +550,23 @@ class XRTrimerHamiltonian:
         return g.finalize()
 
     # ---------------------------------------------------------------------------------
+    def trimer_integral_set(self, ints):
+        """Device copies of the per-build trimer integral matrices (W, Uq) for these three
+        fragments' integrals, for load_integral_sets."""
+        W, Uq = trimer_integral_matrices(ints.V, ints.U, self.plan.integral_keys, self.plan.Ns)
+        return {"W": {k: w.contiguous().reshape(-1) for k, w in W.items()},
+                "Uq": {k: u.contiguous().reshape(-1) for k, u in Uq.items()}}
+
+    def load_integral_sets(self, pair_sets, trimer_set):
+        """New integrals from prepared sets (XRDimerPlan.integral_set of each pair, in PAIRS
+        order, and trimer_integral_set): device copies and operand splits only."""
+        for pl, S in zip(self.plans, pair_sets):
+            pl.load_integral_set(S)
+        for k, w in self.W.items():
+            w.copy_(trimer_set["W"][k])
+        for k, u in self.Uq.items():
+            u.copy_(trimer_set["Uq"][k])
+
     def set_coeffs(self, coeffs):
         """coeffs: three {charge: CUDA float64 (n_states, n_conf)} dicts."""
         for p, (a, b) in enumerate(PAIRS):
@@ -529,8 +578,11 @@ class XRTrimerHamiltonian:
             self.set_coeffs(coeffs)
         for b, z in zip(self.builders, self.coeffs):
             b.build(z)
+        if self.pair_registry is not None:
+            for b in self.builders:
+                self.pair_registry.split(b.split_group)
         for pl in self.plans:
-            pl.launch(build_densities=False)
+            pl.launch(build_densities=False, split_inputs=False)
         self._run_permutes(self._permutes)
         self.stage1.run()
         for phase in self.tcs:
@@ -589,13 +641,15 @@ class XRTrimerHamiltonian:
         idx, dim = self.plan.product_index()
         return torch.as_tensor(idx, device=self.device), dim
 
-    def lowest(self, k=1, m=60, seed=7, tol=None, max_restarts=30, graph=False):
+    def lowest(self, k=1, m=60, seed=7, tol=None, max_restarts=30, graph=False, v0=None):
         """Lowest k eigenvalues (FP64 Lanczos on the matrix-free product) and the residual
         estimate of the lowest; the ground-state vector is self.lanczos.ground_vector().
         tol: restart the Krylov loop from the current ground Ritz vector until the residual
         of the lowest pair is below tol * max(1, |E0|) (None: one loop of m steps).
         graph: replay the m-step Krylov loop (products and Gram-Schmidt) as one CUDA graph,
-        captured on the first call."""
+        captured on the first call.
+        v0: start vector (device, length self.dim); default: the seeded random start on the
+        first call, the last ground vector on later calls."""
         from .eigen import Lanczos
         if getattr(self, "lanczos", None) is None or self.lanczos.m != min(m, self.dim):
             self.lanczos = Lanczos(self.dim, m=m, device=self.device, seed=seed, mode="steps")
@@ -618,8 +672,12 @@ class XRTrimerHamiltonian:
                 krylov()
             lz.v0.copy_(v0)
             self._krylov_graph = g
+        if v0 is not None:
+            lz.v0.copy_(v0)
         w = resid = None
+        self.lanczos_cycles = 0
         for _ in range(max_restarts if tol is not None else 1):
+            self.lanczos_cycles += 1
             if graph:
                 self._krylov_graph.replay()
             else:
