@@ -47,6 +47,7 @@ constexpr uint32_t TC_TMEM_COLS = 512;             // 2 chunk buffers x (main, c
 constexpr uint32_t TC_A_BYTES = TC_BM * 128;       // 128 rows x 128 B (one swizzle width of K)
 constexpr uint32_t TC_B_MAX_BYTES = 128 * 128;
 constexpr uint32_t TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_MAX_BYTES;
+constexpr long long TC_IDLE_LIMIT = 1LL << 26;     // producer polls without progress before giving up
 
 // Named barrier 1 over the epilogue warps, returning the OR of a predicate over them.
 __device__ __forceinline__ int epi_bar_or(int pred) {
@@ -86,8 +87,16 @@ __device__ __forceinline__ TileInfo tile_info(const xrh_tc_task* __restrict__ ta
     int64_t local = tile - T.tile_begin;
     const int64_t split = local / (tiles_m * tiles_n);
     local -= split * tiles_m * tiles_n;
-    r.m0 = (int)((local / tiles_n) * TC_BM);
-    r.n0 = (int)((local % tiles_n) * r.BN);
+    // the CTAs running at once take consecutive tiles: they walk the M tiles of one N tile when
+    // M < N, so the smaller operand (A, M x K) is the one every CTA re-reads (from L2) and each
+    // tile of the larger one comes from HBM once; else the N tiles of one M tile
+    if (T.M < T.N) {
+        r.m0 = (int)((local % tiles_m) * TC_BM);
+        r.n0 = (int)((local / tiles_m) * r.BN);
+    } else {
+        r.m0 = (int)((local / tiles_n) * TC_BM);
+        r.n0 = (int)((local % tiles_n) * r.BN);
+    }
     int64_t kc_total = 0;
     for (int64_t s = 0; s < T.seg_count; ++s) kc_total += segs[T.seg_begin + s].kchunks;
     const int64_t per = (kc_total + T.splitk - 1) / T.splitk;
@@ -173,15 +182,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (l_ok) { l_si = tasks[L.task].seg_begin; l_c = L.cb; }
             if (m_ok) { m_si = tasks[Mi.task].seg_begin; m_c = Mi.cb; }
             bool ok = true;
+            // one thread drives both queues without blocking on either: a load is issued as soon
+            // as its ring stage is free, the MMAs of a chunk as soon as its operands have landed
+            // and its TMEM buffer is drained, so that the next chunk's MMAs queue behind the
+            // running ones; a stretch of TC_IDLE_LIMIT polls without progress gives up
+            long long idle = 0;
             while (m_ok && ok) {
-                // keep the ring full, across tile boundaries
-                while (l_ok && gl < gm + TC_STAGES && ok) {
+                bool progress = false;
+                while (l_ok && gl < gm + TC_STAGES) {
                     const int s = (int)(gl % TC_STAGES);
-                    if (gl >= TC_STAGES &&
-                        !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((gl / TC_STAGES) - 1) & 1u, &abort_sh)) {
-                        ok = false;
+                    if (gl >= TC_STAGES && !mbar_test(smem_u32(&empty_bar[s]), (uint32_t)((gl / TC_STAGES) - 1) & 1u))
                         break;
-                    }
                     while (l_c >= segs[l_si].kchunks) { l_c -= segs[l_si].kchunks; ++l_si; }
                     const xrh_tc_segment& S = segs[l_si];
                     const int kcoord = (int)(l_c * KCH);
@@ -195,6 +206,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), maps + S.tmB, bar, kcoord, L.n0);
                     tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + b_bytes), maps + S.tmB + 1, bar, kcoord, L.n0);
                     ++gl;
+                    progress = true;
                     if (++ql == L.nk) {
                         ql = 0;
                         tl += gridDim.x;
@@ -202,40 +214,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         if (l_ok) { l_si = tasks[L.task].seg_begin; l_c = L.cb; }
                     }
                 }
-                if (!ok) break;
                 // the MMAs of chunk gm into chunk buffer gm & 1
                 const int s = (int)(gm % TC_STAGES);
                 const uint32_t b = (uint32_t)(gm & 1);
-                if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(gm / TC_STAGES) & 1u, &abort_sh)) { ok = false; break; }
-                if (gm >= 2 && !mbar_wait(smem_u32(&drained_bar[b]), (uint32_t)((gm >> 1) - 1) & 1u, &abort_sh)) {
-                    ok = false;
-                    break;
+                if (gm < gl && mbar_test(smem_u32(&full_bar[s]), (uint32_t)(gm / TC_STAGES) & 1u) &&
+                    (gm < 2 || mbar_test(smem_u32(&drained_bar[b]), (uint32_t)((gm >> 1) - 1) & 1u))) {
+                    tc_fence_after();
+                    while (m_c >= segs[m_si].kchunks) { m_c -= segs[m_si].kchunks; ++m_si; }
+                    const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)Mi.BN, segs[m_si].negate != 0);
+                    ++m_c;
+                    const uint32_t b_bytes = (uint32_t)Mi.BN * 128u;
+                    const uint32_t st = smem_u32(stages + (size_t)s * TC_STAGE_BYTES);
+                    const uint64_t da_hi = umma_desc_sw128(st), da_lo = umma_desc_sw128(st + TC_A_BYTES);
+                    const uint64_t db_hi = umma_desc_sw128(st + 2 * TC_A_BYTES);
+                    const uint64_t db_lo = umma_desc_sw128(st + 2 * TC_A_BYTES + b_bytes);
+                    const uint32_t t_main = tmem + b * 256u, t_corr = t_main + 128u;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)              // 4 MMA K-steps of 32 bytes inside the chunk
+                        umma<KIND>(t_main, da_hi + 2 * j, db_hi + 2 * j, idesc, j > 0 ? 1u : 0u);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_hi + 2 * j, db_lo + 2 * j, idesc, j > 0 ? 1u : 0u);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_lo + 2 * j, db_hi + 2 * j, idesc, 1u);
+                    umma_commit(smem_u32(&empty_bar[s]));
+                    umma_commit(smem_u32(&ready_bar[b]));
+                    ++gm;
+                    progress = true;
+                    if (++qm == Mi.nk) {
+                        qm = 0;
+                        tm += gridDim.x;
+                        m_ok = seek(tm, Mi);
+                        if (m_ok) { m_si = tasks[Mi.task].seg_begin; m_c = Mi.cb; }
+                    }
                 }
-                tc_fence_after();
-                while (m_c >= segs[m_si].kchunks) { m_c -= segs[m_si].kchunks; ++m_si; }
-                const uint32_t idesc = make_idesc(FMT, TC_BM, (uint32_t)Mi.BN, segs[m_si].negate != 0);
-                ++m_c;
-                const uint32_t b_bytes = (uint32_t)Mi.BN * 128u;
-                const uint32_t st = smem_u32(stages + (size_t)s * TC_STAGE_BYTES);
-                const uint64_t da_hi = umma_desc_sw128(st), da_lo = umma_desc_sw128(st + TC_A_BYTES);
-                const uint64_t db_hi = umma_desc_sw128(st + 2 * TC_A_BYTES);
-                const uint64_t db_lo = umma_desc_sw128(st + 2 * TC_A_BYTES + b_bytes);
-                const uint32_t t_main = tmem + b * 256u, t_corr = t_main + 128u;
-#pragma unroll
-                for (int j = 0; j < 4; ++j)              // 4 MMA K-steps of 32 bytes inside the chunk
-                    umma<KIND>(t_main, da_hi + 2 * j, db_hi + 2 * j, idesc, j > 0 ? 1u : 0u);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_hi + 2 * j, db_lo + 2 * j, idesc, j > 0 ? 1u : 0u);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) umma<KIND>(t_corr, da_lo + 2 * j, db_hi + 2 * j, idesc, 1u);
-                umma_commit(smem_u32(&empty_bar[s]));
-                umma_commit(smem_u32(&ready_bar[b]));
-                ++gm;
-                if (++qm == Mi.nk) {
-                    qm = 0;
-                    tm += gridDim.x;
-                    m_ok = seek(tm, Mi);
-                    if (m_ok) { m_si = tasks[Mi.task].seg_begin; m_c = Mi.cb; }
+                if (progress) {
+                    idle = 0;
+                } else if (++idle > TC_IDLE_LIMIT || abort_sh) {
+                    ok = false;
                 }
             }
             if (!ok) {

@@ -101,3 +101,91 @@ def test_tc_gemm_every_tile_policy(prec):
             assert _rel(C2, ref2) < TOL[prec], (cap, div, _rel(C2, ref2))
     tc.autotune()
     assert tc.tuning is not None and tc.policy in [p for p, _ in tc.tuning]
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_tc_gemm_many_short_segments_wide_output(prec):
+    """The shape of the three-fragment H x v's stage B in small: M < N (concurrent tiles walk
+    the M tiles of one N tile), 40 K-concatenated segments of K = 28 (one padded chunk each);
+    stored and split-K accumulated."""
+    from qodeapplications_gb300.gemm import SplitRegistry, TCGroupedGemm
+    g = torch.Generator().manual_seed(5)
+    M, N, K, S_ = 280, 1000, 28, 40
+    As = [torch.randn(M, K, generator=g, dtype=torch.float64).cuda() for _ in range(S_)]
+    Bs = [torch.randn(N, K, generator=g, dtype=torch.float64).cuda() for _ in range(S_)]
+    reg = SplitRegistry(prec)
+    C0 = torch.zeros(M, N, dtype=torch.float64, device="cuda")
+    C1 = torch.zeros(M, N, dtype=torch.float64, device="cuda")
+    tc = TCGroupedGemm(reg)
+    segs = [(A, K, B, K, K, 1.0 if i % 3 else -1.0) for i, (A, B) in enumerate(zip(As, Bs))]
+    tc.add(M, N, segs, C0, N, mode=0)
+    tc.add(M, N, segs, C1, N, mode=1, splitk=4)
+    reg.upload()
+    tc.finalize()
+    reg.split("in")
+    tc.run()
+    torch.cuda.synchronize()
+    tc.check()
+    ref = sum(s[5] * (s[0] @ s[2].t()) for s in segs)
+    assert _rel(C0, ref) < TOL[prec], _rel(C0, ref)
+    assert _rel(C1, ref) < TOL[prec], _rel(C1, ref)
+
+
+def test_tc_gemm_precontraction_shape():
+    """One 3xTF32 launch at the shape of the 2 x 14 / 60-state precontractions (M = 3600 state
+    pairs, N = 784, K = 784) against FP64, and its CUDA-event time (printed): the launch the
+    tensor-pipe counters of the profile summary were taken on."""
+    from qodeapplications_gb300.gemm import SplitRegistry, TCGroupedGemm
+    g = torch.Generator().manual_seed(6)
+    M, N, K = 3600, 784, 784
+    A = torch.randn(M, K, generator=g, dtype=torch.float64).cuda()
+    B = torch.randn(N, K, generator=g, dtype=torch.float64).cuda()
+    C = torch.zeros(M, N, dtype=torch.float64, device="cuda")
+    reg = SplitRegistry("tf32x3")
+    tc = TCGroupedGemm(reg)
+    tc.add(M, N, [(A, K, B, K, K, 1.0)], C, N, mode=0)
+    reg.upload()
+    tc.finalize()
+    reg.split("in")
+    tc.run()
+    torch.cuda.synchronize()
+    tc.check()
+    assert _rel(C, A @ B.t()) < TOL["tf32x3"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        tc.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    print(f"tf32x3 GEMM {M}x{N}x{K}: {ms:.3f} ms, {2.0 * M * N * K / ms / 1e9:.1f} TFLOP/s algorithmic")
+
+
+def test_tc_gemm_stage_b_shape():
+    """One 3xTF32 launch of the three-fragment H x v's stage B at 3 x 14 orbitals / 40 states
+    (M = 40 x 28, N = 40 x 40, 40 K-concatenated segments of K = 28) against FP64, and its
+    CUDA-event time (printed): the launch the stage-B profile summary was taken on."""
+    from qodeapplications_gb300.gemm import SplitRegistry, TCGroupedGemm
+    g = torch.Generator().manual_seed(7)
+    M, N, K, S_ = 1120, 1600, 28, 40
+    A = torch.randn(S_, M, K, generator=g, dtype=torch.float64).cuda()
+    B = torch.randn(S_, N, K, generator=g, dtype=torch.float64).cuda()
+    C = torch.zeros(M, N, dtype=torch.float64, device="cuda")
+    reg = SplitRegistry("tf32x3")
+    tc = TCGroupedGemm(reg)
+    tc.add(M, N, [(A[i], K, B[i], K, K, 1.0) for i in range(S_)], C, N, mode=0)
+    reg.upload()
+    tc.finalize()
+    reg.split("in")
+    tc.run()
+    torch.cuda.synchronize()
+    tc.check()
+    assert _rel(C, torch.einsum("smk,snk->mn", A, B)) < TOL["tf32x3"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        tc.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    print(f"tf32x3 stage-B GEMM {M}x{N}x({S_}x{K}): {ms:.3f} ms, {2.0 * M * N * K * S_ / ms / 1e9:.1f} TFLOP/s algorithmic")
