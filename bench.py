@@ -325,7 +325,7 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from ncu captures of the bench
 # command (the summaries are in profiles/); None where no capture of the current kernel exists
-DENSITY_ADJ_TRAFFIC = {}
+DENSITY_ADJ_TRAFFIC = {(3, "density_adjoint_f32_grouped_kernel"): 1.303e9}
 
 
 def measure_peaks():
@@ -926,18 +926,21 @@ def run_ring(args):
                         "(of measured)",
                 "hv_gflop": ring.slot.flops_apply / 1e9}
     rec = {"s_per_iter": s_per_iter, "E2": outs[-1]["E2"], "E3": outs[-1]["E3"], "phases_ms": phases[-1],
-           "max_lanczos_residual": resid_max, "n_pairs": len(ring.pairs), "n_triples": len(ring.triples)}
+           "max_lanczos_residual": resid_max, "n_pairs": len(ring.pairs), "n_triples": len(ring.triples),
+           "triple_hv_products": sum(ring.products.values())}
+    E_pair, E_mono = dict(ring.E_pair), dict(ring.E_mono)
     variants = {head: rec}
+    triple_products = sum(ring.products.values())
     del ring
     torch.cuda.empty_cache()
     if not args.no_variants and head != "fp64":
-        # FP64 pair phase: E2 and its gradient, one iteration
-        r64 = XRRing(n_frag=c["n_frag"], n_orb=n_orb, n_states=n_states, precision="fp64", triples=False, tol=tol,
-                     seed=SEED)
-        r64.iterate()
+        # FP64: the pair phase (E2 and its gradient) in full, one iteration; the triple phase from
+        # one triple's FP64 build and H x v products timed, times the split run's product count
+        r64 = XRRing(n_frag=c["n_frag"], n_orb=n_orb, n_states=n_states, precision="fp64", triples=triples,
+                     tol=tol, seed=SEED)
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0.record()
-        o64 = r64.iterate()
+        o64 = r64.iterate(with_triples=False)
         t1.record()
         torch.cuda.synchronize()
         num = den = 0.0
@@ -945,11 +948,40 @@ def run_ring(args):
             for q in g_split[f]:
                 num += float((r64.grad[f][q] - g_split[f][q]).norm()) ** 2
                 den += float(r64.grad[f][q].norm()) ** 2
-        variants["fp64_pairs"] = {"s_per_iter_pairs": t0.elapsed_time(t1) / 1e3, "E2": o64["E2"],
-                                  "max_lanczos_residual": max(r64.resid.values())}
+        v64 = {"s_per_iter_pairs": t0.elapsed_time(t1) / 1e3, "E2": o64["E2"],
+               "max_lanczos_residual": max(r64.resid.values())}
         rec["dE2_vs_fp64"] = abs(rec["E2"] - o64["E2"])
+        rec["max_pair_dE_vs_fp64"] = max(abs(E_pair[p] - r64.E_pair[p]) for p in E_pair)
+        rec["max_monomer_dE_vs_fp64"] = max(abs(E_mono[f] - r64.E_mono[f]) for f in E_mono)
         rec["state_grad_rel_vs_fp64"] = (num / den) ** 0.5 if den > 0 else None
-        rec["pairs_speedup_vs_fp64"] = variants["fp64_pairs"]["s_per_iter_pairs"] / (rec["phases_ms"]["pairs"] / 1e3)
+        rec["pairs_speedup_vs_fp64"] = v64["s_per_iter_pairs"] / (rec["phases_ms"]["pairs"] / 1e3)
+        if triples:
+            from qodeapplications_gb300.trimer_hv import PAIRS as _P
+            T = r64.triples[0]
+            S_ = r64.slot
+            S_.set_coeffs([r64.coeffs[f] for f in T])
+            S_.load_integral_sets([r64.pair_sets[(T[a], T[b])] for a, b in _P], r64.triple_sets[T])
+            x = torch.ones(S_.dim, dtype=torch.float64, device="cuda") / S_.dim ** 0.5
+            S_.build()
+            S_.apply(x)
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record()
+            S_.build()
+            e[1].record()
+            for _ in range(2):
+                S_.apply(x)
+            e[2].record()
+            torch.cuda.synchronize()
+            build_s, hv_s = e[0].elapsed_time(e[1]) / 1e3, e[1].elapsed_time(e[2]) / 2e3
+            v64["triple_build_s"], v64["triple_hv_s"] = build_s, hv_s
+            v64["triples_s_extrapolated"] = len(r64.triples) * build_s + triple_products * hv_s
+            v64["s_per_iter_extrapolated"] = v64["s_per_iter_pairs"] + v64["triples_s_extrapolated"]
+            v64["extrapolation"] = ("FP64 pair phase measured in full; FP64 triple phase = 8 FP64 triple builds + "
+                                    "the split run's H x v product count x one FP64 product, each timed on triple "
+                                    f"{T}; the FP64 Lanczos of the triples is not run (about "
+                                    f"{v64['triples_s_extrapolated'] / 60:.0f} min)")
+            rec["speedup_vs_fp64_extrapolated"] = v64["s_per_iter_extrapolated"] / rec["s_per_iter"]
+        variants["fp64"] = v64
         del r64
         torch.cuda.empty_cache()
     line = {
@@ -963,12 +995,15 @@ def run_ring(args):
         "config": {"workload": name, "lanczos_residual_tol": tol,
                    "l2": "inputs larger than L2 (pair sector matrices of 7.2 GB, densities of several GB)",
                    "step": "28 pair builds + Lanczos + reverse passes, 8 monomer ground states, 8 triple builds + "
-                           "restarted matrix-free Lanczos (each from one fixed start vector)"},
+                           "restarted matrix-free Lanczos (Krylov cycles as CUDA graphs), every ground state started "
+                           "from lower orders of the same step plus a fixed random vector"},
         "e2e": {"value": sum(e2e) / 1e3 / args.steps, "unit": "s/iter", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 16},
         "gpu_launches": launches, "clocks": clocks, "E2": rec["E2"], "E3": rec["E3"], "roofline": roof,
         "variants": variants,
     }
+    if "speedup_vs_fp64_extrapolated" in rec:
+        line["speedup_vs_fp64_gpu"] = rec["speedup_vs_fp64_extrapolated"]
     print(json.dumps(line))
 
 

@@ -102,7 +102,7 @@ class XRRing:
     """
 
     def __init__(self, n_frag=8, n_orb=14, n_states=100, charges=(+1, 0, -1), n_elec_ref=4, precision="tf32x3",
-                 hv_precision=None, triples=True, seed=1234, pair_m=60, triple_m=40, tol=1e-6, max_restarts=60,
+                 hv_precision=None, triples=True, seed=1234, pair_m=90, triple_m=100, tol=1e-6, max_restarts=60,
                  graph=True, autotune=True, device="cuda"):
         dev = torch.device(device)
         self.device = dev
@@ -212,6 +212,7 @@ class XRRing:
                      for _ in range(self.n_frag)]
         self.E_mono, self.E_pair, self.E_triple = {}, {}, {}
         self.resid = {}
+        self.products = {}                # H x v products of each triple's last ground state
         self.phase_ms = {}
 
     # ------------------------------------------------------------------------------------
@@ -293,12 +294,14 @@ class XRRing:
                             v0=self.v_triple)
         self.E_triple[T] = float(w[0])
         self.resid[T] = float(resid)
+        self.products[T] = S.lanczos_cycles * S.lanczos.m
         return float(w[0])
 
-    def iterate(self):
+    def iterate(self, with_triples=True):
         """One ring iteration: every pair (build, ground state, reverse pass), the monomer
-        terms, every nearest-neighbour triple (build, ground state).  Returns {'E2', 'E3'};
-        the gradient of E2 is in self.grad[fragment][charge] (n_conf x n_states, dE2/dz^T)."""
+        terms, every nearest-neighbour triple (build, ground state; skipped with
+        with_triples=False).  Returns {'E2', 'E3'}; the gradient of E2 is in
+        self.grad[fragment][charge] (n_conf x n_states, dE2/dz^T)."""
         for g in self.grad:
             for t in g.values():
                 _lib.zero_(t)
@@ -308,13 +311,13 @@ class XRRing:
         for I, J in self.pairs:
             self.run_pair(I, J)
         ev[1].record()
-        for T in self.triples:
+        for T in (self.triples if with_triples else ()):
             self.run_triple(T)
         ev[2].record()
         torch.cuda.current_stream().synchronize()
         self.phase_ms = {"pairs": ev[0].elapsed_time(ev[1]), "triples": ev[1].elapsed_time(ev[2])}
         E2, E3 = mbe_energies(self.E_mono, self.E_pair, self.E_triple, self.n_frag)
-        self.E2, self.E3 = E2, (E3 if self.triples else None)
+        self.E2, self.E3 = E2, (E3 if self.triples and with_triples else None)
         return {"E2": E2, "E3": self.E3}
 
     def check_status(self):
