@@ -25,9 +25,9 @@
 //     rows, 32-column groups alternate between w<4 and w>=4), add into registers, release the
 //     buffer (drained); at the end of the tile, the FP64 epilogue.
 // Every mbarrier wait is bounded; on timeout the kernel records XRH_ERR_TIMEOUT in *status,
-// every warp leaves its loop (the epilogue warps decide together through bar.red.or), the
-// producer waits (bounded) for its copies and MMAs in flight, TMEM is freed and the kernel
-// returns.
+// every warp leaves its loop (the epilogue warps decide together through bar.red.or once per
+// tile), the producer waits (bounded) for its copies and MMAs in flight, TMEM is freed and the
+// kernel returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -291,11 +291,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) acc[i][j] = 0.f;
+            // the warps drain their chunks independently; a wait that gives up raises abort_sh,
+            // so the others' waits give up too, and all decide together once per tile below
+            bool failed = false;
             for (int q = 0; q < I.nk; ++q, ++ge) {
                 const uint32_t b = (uint32_t)(ge & 1);
-                const bool got = mbar_wait(smem_u32(&ready_bar[b]), (uint32_t)(ge >> 1) & 1u, &abort_sh);
-                if (epi_bar_or(!got)) {
-                    aborted = true;
+                if (!mbar_wait(smem_u32(&ready_bar[b]), (uint32_t)(ge >> 1) & 1u, &abort_sh)) {
+                    failed = true;
+                    abort_sh = 1;
                     break;
                 }
                 tc_fence_after();
@@ -315,6 +318,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(&drained_bar[b]));
             }
+            // one collective decision per tile (also the barrier after the column metadata)
+            if (epi_bar_or(failed)) aborted = true;
             if (aborted) {
                 abort_sh = 1;
                 if (tid == 0) atomicExch(status, XRH_ERR_TIMEOUT);
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // FP64 epilogue, one 32-column slice at a time: the 4 warps that hold the slice put it
             // into shared memory (a row per lane), then every warp writes 16 rows with its lanes
             // on consecutive columns, so that stores (and atomics) of a warp touch few cache
-            // lines.  Column metadata came with the chunk barriers; row metadata first:
+            // lines.  Column metadata came before the decision barrier; row metadata first:
             for (int rr = tid; rr < TC_BM; rr += TC_EPI_THREADS) {
                 const int m = m0 + rr;
                 int64_t rb = 0, cb2 = 0;
