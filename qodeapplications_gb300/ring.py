@@ -146,7 +146,7 @@ class XRRing:
                                 autotune=autotune, builders=builders, total_charges=[0], registry=registry)
         # the reverse pass's transposed density gradients live in the triple's H x v
         # intermediates: the two never run inside one another
-        scratch = [self.slot.bufs[k] for k in ("T2", "T2p", "T1") if k in self.slot.bufs] if self.triples else None
+        scratch = [self.slot.bufs[k] for k in ("T2p", "T1") if k in self.slot.bufs] if self.triples else None
         self.adj = XRDimerAdjoint(self.plan, monomer_terms=True, scratch=scratch)
         # integral sets, prepared once: every pair (I < J) and the ordered pairs of the triples
         need = set(self.pairs)

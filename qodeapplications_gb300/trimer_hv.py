@@ -22,8 +22,9 @@ the fragment carrying the two-index density first), the product runs in three GE
 that never touch an n^3 x n^3 object:
 
   A  T1[x',y',z,s]  = sum_z'     v[x',y',z'] R3t[z,s,z']          (R3 transposed once per build)
-  B  T2[x,r,y',z]   = sum_x',s   P[x',x,r,s] T1[x',y',z,s]        (x' as K-concatenated segments)
-     T2p[x,z,y',r]  = a T2[x,r,y',z]                               (factor and phase folded in)
+  B  T2p[x,z,y',r]  = a sum_x',s T1[x',y',z,s] P[x',x,r,s]       (x' as K-concatenated segments;
+                                                                    the GEMM's scatter epilogue
+                                                                    writes the layout of stage C)
   C  w[x,z,y]      += sum_y',r   T2p[x,z,y',r] R2[y,y',r]
 
 each one GEMM with K contiguous in both operands, about 2 n^4 N^2 FLOPs per block instead of
@@ -90,7 +91,7 @@ class TrimerHvPlan:
                  twice over the three pairs
 
     Buffers are named: 'v', 'w' (the vectors), 'vXYZ'/'wXYZ' (permuted copies for fragment
-    order XYZ), 'Pt', 'R3t', 'T1', 'T2', 'T2p' (intermediates, sizes in self.sizes) and external
+    order XYZ), 'Pt', 'R3t', 'T1', 'T2p' (intermediates, sizes in self.sizes) and external
     keys ('rho', f, op, bc, kc), ('H1', f, c), ('H2', pair, t), ('W', kind, order),
     ('Uq', order), ('eye', n).  A reference is (buffer, element offset)."""
 
@@ -226,14 +227,17 @@ class TrimerHvPlan:
                 nz, nzp = ns[z][ci[z]], ns[z][cj[z]]
                 Ny, Nz = N[y], N[z]
                 Kx = N[x] * N[x]
-                # stage 1 (per build): Pt[x'][x][r][s] = sum_k R1[x,x',k] W[(r,s),k] (+ delta U/4)
+                # stage 1 (per build): Pt[x'][x][r][s] = a_k sum_k R1[x,x',k] W[(r,s),k] (+ delta U/4),
+                # a_k = 4 (tex) or 2: the magnitude of the block factor (its sign goes to stage B)
                 pkey = (kind, order, ci[x], cj[x])
+                amag = 4.0 if kind == "tex" else 2.0
                 if pkey not in P_off:
                     self.integral_keys.add((kind, order))
                     P_off[pkey] = self._alloc("Pt", nxp * nx * Ny * Nz)
-                    segs = [_seg((("rho", x, ops[0], ci[x], cj[x]), 0), Kx, (("W", kind, order), 0), Kx, Kx, sA=nxp * Kx)]
+                    segs = [_seg((("rho", x, ops[0], ci[x], cj[x]), 0), Kx, (("W", kind, order), 0), Kx, Kx,
+                                 alpha=amag, sA=nxp * Kx)]
                     if kind == "tex":
-                        segs.append(_seg((("eye", nx), 0), 1, (("Uq", order), 0), 1, 1, sA=nx))
+                        segs.append(_seg((("eye", nx), 0), 1, (("Uq", order), 0), 1, 1, alpha=amag, sA=nx))
                     self.build_tasks.append(_task(nxp, Ny * Nz, ("Pt", P_off[pkey]), nx * Ny * Nz, segs, mode=0,
                                                   batch=nx, sC=Ny * Nz))
                 # R3 as [z][s][z'] (per build)
@@ -249,24 +253,27 @@ class TrimerHvPlan:
                                  [_seg((_vname(order), self.off[cj]), nzp, ("R3t", R3_off[rkey]), nzp, nzp)], mode=0)
                     task["role"] = "A"
                     self.launches[0].append(task)
-                # B: T2[x][r][y'][z] = sum_x' sum_s Pt[x'][x][r][s] T1[x'][y'][z][s]
+                # B: T2p[x][z][y'][r] = sgn sum_x' sum_s T1[x'][y'][z][s] Pt[x'][x][r][s], written by the
+                # GEMM's scatter epilogue (mode 2) straight into the K-contiguous layout of stage C:
+                # output (m = (y', z), n = (x, r)) goes to (z nyp Ny + y' Ny) + (x nz nyp Ny + r), so
+                # the lanes of a warp (consecutive n) store consecutive r
                 s2 = -1.0 if (self.n_elec[1] - ci[1]) % 2 else 1.0
                 s3 = -1.0 if (self.n_elec[2] - ci[2]) % 2 else 1.0
-                alpha = (4.0 if kind == "tex" else 2.0) * _phase(kind, order, s2, s3)
+                sgn = _phase(kind, order, s2, s3)
                 t2key = (pkey, t1key)            # one charge block: (ci[x], ci[z], cj) fix ci[y]
                 if t2key not in T2_off:
-                    T2_off[t2key] = self._alloc("T2", nx * Ny * nyp * nz)
+                    T2_off[t2key] = self._alloc("T2p", nx * Ny * nyp * nz)
                     p0, q0 = P_off[pkey], T1_off[t1key]
-                    segs = [_seg(("Pt", p0 + xp * nx * Ny * Nz), Nz, ("T1", q0 + xp * nyp * nz * Nz), Nz, Nz)
+                    segs = [_seg(("T1", q0 + xp * nyp * nz * Nz), Nz, ("Pt", p0 + xp * nx * Ny * Nz), Nz, Nz,
+                                 alpha=sgn)
                             for xp in range(nxp)]
-                    task = _task(nx * Ny, nyp * nz, ("T2", T2_off[t2key]), nyp * nz, segs, mode=0)
+                    task = _task(nyp * nz, nx * Ny, ("T2p", T2_off[t2key]), 1, segs, mode=2)
+                    yi, zi = np.divmod(np.arange(nyp * nz), nz)
+                    xi, ri = np.divmod(np.arange(nx * Ny), Ny)
+                    task["maps"] = (zi * (nyp * Ny) + yi * Ny, np.zeros(nyp * nz, dtype=np.int64),
+                                    xi * (nz * nyp * Ny) + ri, np.zeros(nx * Ny, dtype=np.int64))
                     task["role"] = "B"
                     self.launches[1].append(task)
-                    # T2p[x][z][y'][r] = a T2[x][r][y'][z] (per product): the K-contiguous operand of
-                    # stage C with the block's factor and phase folded in
-                    self.mid_permutes.append((("T2", T2_off[t2key]), (nx, Ny, nyp, nz), (0, 3, 2, 1),
-                                              ("T2p", T2_off[t2key]), alpha))
-                    self.sizes["T2p"] = self.sizes["T2"]
                 # C: w_xzy[(x z)][y] += sum_(y',r) T2p[(x z)][(y' r)] R2[y][(y' r)]
                 okey = (out_order, ci)
                 if okey not in out_tasks:
@@ -502,7 +509,8 @@ class XRTrimerHamiltonian:
                                          sg["alpha"]))
                             groups.append(tuple("product" if isinstance(r[0], str) and r[0].startswith(per_product)
                                                 else "build" for r in (sg["A"], sg["B"])))
-                        g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], groups=groups)
+                        g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], groups=groups,
+                              maps=self._maps(t))
                     reg.upload()
                     g.finalize()
                     if autotune:
@@ -539,6 +547,16 @@ class XRTrimerHamiltonian:
         t = self._ext(buf)
         return t[off:]
 
+    def _maps(self, t):
+        """Device index maps of a mode-2 (scatter) record: (rowA, colA, rowB, colB) as int32 and
+        zero diagonal flags (no delta terms)."""
+        if t["mode"] != 2:
+            return None
+        dev = self.device
+        rowA, colA, rowB, colB = (torch.as_tensor(np.asarray(a, dtype=np.int32), device=dev) for a in t["maps"])
+        return (rowA, colA, rowB, colB, torch.zeros(t["M"], dtype=torch.uint8, device=dev),
+                torch.zeros(t["N"], dtype=torch.uint8, device=dev))
+
     def _grouped(self, tasks, precision):
         g = GroupedGemm(self.device, precision=precision)
         for t in tasks:
@@ -546,7 +564,8 @@ class XRTrimerHamiltonian:
             for s in t["segs"]:
                 segs.append((self._resolve(s["A"]), s["lda"], self._resolve(s["B"]), s["ldb"], s["K"], s["alpha"],
                              s["flags"], s["sA"], s["sB"]))
-            g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], batch=t["batch"], sC=t["sC"])
+            g.add(t["M"], t["N"], segs, self._resolve(t["C"]), t["ldc"], mode=t["mode"], batch=t["batch"], sC=t["sC"],
+                  maps=self._maps(t))
         return g.finalize()
 
     # ---------------------------------------------------------------------------------

@@ -38,9 +38,13 @@ def _run_task(resolve, t):
             ib = b0 + b * s["sB"] + (k * s["ldb"] + np.arange(N)[:, None] if s["flags"] & 2
                                      else np.arange(N)[:, None] * s["ldb"] + k)
             acc += s["alpha"] * _gather(A, ia) @ _gather(B, ib).T
-        ic = c0 + b * t["sC"] + m * t["ldc"] + n
+        if t["mode"] == 2:         # scatter: C[(rowA[m] + rowB[n]) ldc + colA[m] + colB[n]] = acc
+            rowA, colA, rowB, colB = (np.asarray(a, dtype=np.int64) for a in t["maps"])
+            ic = c0 + (rowA[:, None] + rowB[None, :]) * t["ldc"] + colA[:, None] + colB[None, :]
+        else:
+            ic = c0 + b * t["sC"] + m * t["ldc"] + n
         assert ic.min() >= 0 and ic.max() < C.size, "record writes outside its buffer"
-        if t["mode"] == 0:
+        if t["mode"] in (0, 2):
             C[ic] = acc
         else:
             C[ic] += acc
