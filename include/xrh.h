@@ -178,8 +178,11 @@ int xrh_transpose_grouped(const xrh_transpose_task* tasks_dev, int n_tasks, int6
 int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev,
                        int accumulate, void* stream);
 /* Many mirrors in one launch: task t is one xrh_mirror_density call and owns the launch's CTAs
- * [cta_begin, cta_begin + na * nb * (L == 3 ? N : 1)) (tasks sorted by cta_begin, total_ctas
- * the sum).  The tasks' dst blocks must not overlap. */
+ * [cta_begin, cta_begin + na * nb * xrh_mirror_ctas(N, L)) (tasks sorted by cta_begin,
+ * total_ctas the sum).  The tasks' dst blocks must not overlap.  xrh_mirror_ctas: CTAs per
+ * (a, b) pair (1 for L < 3; for L = 3 one CTA per group of about 4096 / N^2 q planes), 0 for
+ * unsupported N or L. */
+int64_t xrh_mirror_ctas(int N, int L);
 typedef struct {
     const double* src;
     double* dst;

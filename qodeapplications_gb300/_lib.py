@@ -87,6 +87,7 @@ _SIGS = {
     "xrh_zero": (_i32, [_vp, _i64, _vp]),
     "xrh_index_move": (_i32, [_i64, _vp, _vp, _vp, _i32, _vp]),
     "xrh_f64_to_f32": (_i32, [_i64, _vp, _vp, _vp]),
+    "xrh_mirror_ctas": (_i64, [_i32, _i32]),
     "xrh_add_mixed": (_i32, [_i64, _dbl, _vp, _vp, _vp, _vp]),
     "xrh_spin_sum_antisym": (_i32, [_i32, _i32, _vp, _vp, _i64, _vp, _vp]),
     "xrh_small_mm_grouped": (_i32, [_vp, _i32, _i64, _vp]),
@@ -133,7 +134,7 @@ class LaunchCounter:
     multi = {"xrh_orbital_terms": 2, "xrh_gemv_rows_split": 2, "xrh_lanczos_normalize_split": 2}
     host_only = {"xrh_abi_version", "xrh_status_string", "xrh_last_cuda_error", "xrh_tc_chunk_elems", "xrh_zero",
                  "xrh_tc_encode_map", "xrh_state_ctas", "xrh_abt_ctas", "xrh_lanczos_coop_work",
-                 "xrh_lanczos_cluster_fits", "xrh_gemv_split_work"}
+                 "xrh_lanczos_cluster_fits", "xrh_gemv_split_work", "xrh_mirror_ctas"}
     count = 0
 
 
@@ -282,7 +283,7 @@ class Mirrors:
             t = tab[i]
             t["src"], t["dst"], t["na"], t["nb"], t["N"], t["L"] = src.data_ptr(), dst.data_ptr(), na, nb, N, L
             t["accumulate"], t["cta_begin"] = int(acc), cta
-            cta += na * nb * (N if L == 3 else 1)
+            cta += na * nb * int(lib().xrh_mirror_ctas(N, L))
         self.n, self.ctas, self.keep = len(items), cta, items
         self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(items) else None
 

@@ -304,44 +304,27 @@ extern "C" int xrh_sigma2e(int precision, int n_orbs, const double* V_dev, const
 // One CTA per (a, b[, q]) plane: reversing (p, q, r) -> (r, q, p) transposes the (p, r) plane at
 // fixed q, reversing (p, q) -> (q, p) transposes the plane; both go through shared memory so
 // that loads and stores stay coalesced (N <= 64).
-__global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int L, const double* __restrict__ src,
-                                                     double* __restrict__ dst, int accumulate) {
-    __shared__ double tile[64][65];
-    int64_t F = 1;
-    for (int l = 0; l < L; ++l) F *= N;
-    const int64_t blk = blockIdx.x;
-    const int q = (L == 3) ? (int)(blk % N) : 0;
-    const int64_t ab = (L == 3) ? blk / N : blk;
-    const int a = (int)(ab / nb), b = (int)(ab - (int64_t)(ab / nb) * nb);
-    const double* sp = src + ((int64_t)b * na + a) * F;
-    double* dp = dst + ((int64_t)a * nb + b) * F;
-    if (L == 1) {
-        for (int p = threadIdx.x; p < N; p += blockDim.x) dp[p] = (accumulate ? dp[p] : 0.0) + sp[p];
-        return;
-    }
-    const int NN = N * N;
-    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
-        const int p = i / N, r = i - p * N;
-        tile[p][r] = sp[L == 2 ? i : ((int64_t)p * N + q) * N + r];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
-        const int r = i / N, p = i - r * N;
-        const int64_t pos = L == 2 ? i : ((int64_t)r * N + q) * N + p;
-        const double v = tile[p][r];
-        dp[pos] = accumulate ? dp[pos] + v : v;
-    }
-}
-
 // Many mirrors in one launch: CTA -> task by binary search on cta_begin; the tasks' dst
-// blocks are distinct (the host checks), so accumulating tasks do not race.
+// blocks are distinct (the host checks), so accumulating tasks do not race.  For L = 3 a CTA
+// takes mirror_planes(N) consecutive q planes of one (a, b) (about 4096 elements), so that each
+// thread keeps several loads in flight; L = 1, 2: one CTA per (a, b).
+__host__ __device__ __forceinline__ int mirror_planes(int N) {
+    const int q = 4096 / (N * N);
+    return q < 1 ? 1 : (q > N ? N : q);
+}
+__host__ __device__ __forceinline__ int64_t mirror_ctas_per_pair(int N, int L) {
+    return L == 3 ? (N + mirror_planes(N) - 1) / mirror_planes(N) : 1;
+}
+constexpr int kMirrorTile = 4352;      // max over N <= 64 of planes * N * (N + 1) doubles
+
 __device__ __forceinline__ void mirror_plane(int na, int nb, int N, int L, const double* __restrict__ src,
                                              double* __restrict__ dst, int accumulate, int64_t blk,
-                                             double (*tile)[65]) {
+                                             double* __restrict__ tile) {
     int64_t F = 1;
     for (int l = 0; l < L; ++l) F *= N;
-    const int q = (L == 3) ? (int)(blk % N) : 0;
-    const int64_t ab = (L == 3) ? blk / N : blk;
+    const int64_t per = mirror_ctas_per_pair(N, L);
+    const int64_t ab = blk / per;
+    const int qb = (int)(blk - ab * per);
     const int a = (int)(ab / nb), b = (int)(ab - (int64_t)(ab / nb) * nb);
     const double* sp = src + ((int64_t)b * na + a) * F;
     double* dp = dst + ((int64_t)a * nb + b) * F;
@@ -349,22 +332,26 @@ __device__ __forceinline__ void mirror_plane(int na, int nb, int N, int L, const
         for (int p = threadIdx.x; p < N; p += blockDim.x) dp[p] = (accumulate ? dp[p] : 0.0) + sp[p];
         return;
     }
-    const int NN = N * N;
-    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
-        const int p = i / N, r = i - p * N;
-        tile[p][r] = sp[L == 2 ? i : ((int64_t)p * N + q) * N + r];
+    const int NN = N * N, W = N + 1;
+    const int QB = (L == 3) ? mirror_planes(N) : 1;
+    const int q0 = qb * QB;
+    const int nq = (L == 3) ? (N - q0 < QB ? N - q0 : QB) : 1;
+    // load: consecutive threads along r (contiguous in src), store: along p (contiguous in dst)
+    for (int e = threadIdx.x; e < nq * NN; e += blockDim.x) {
+        const int qq = e / NN, rem = e - qq * NN, p = rem / N, r = rem - p * N;
+        tile[(qq * N + p) * W + r] = sp[L == 2 ? rem : ((int64_t)p * N + q0 + qq) * N + r];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
-        const int r = i / N, p = i - r * N;
-        const int64_t pos = L == 2 ? i : ((int64_t)r * N + q) * N + p;
-        const double v = tile[p][r];
+    for (int e = threadIdx.x; e < nq * NN; e += blockDim.x) {
+        const int qq = e / NN, rem = e - qq * NN, r = rem / N, p = rem - r * N;
+        const int64_t pos = L == 2 ? rem : ((int64_t)r * N + q0 + qq) * N + p;
+        const double v = tile[(qq * N + p) * W + r];
         dp[pos] = accumulate ? dp[pos] + v : v;
     }
 }
 
 __global__ void __launch_bounds__(256) mirror_grouped_kernel(const xrh_mirror_task* __restrict__ tasks, int n_tasks) {
-    __shared__ double tile[64][65];
+    __shared__ double tile[kMirrorTile];
     const int64_t cta = blockIdx.x;
     int lo = 0, hi = n_tasks - 1;
     while (lo < hi) {
@@ -376,12 +363,23 @@ __global__ void __launch_bounds__(256) mirror_grouped_kernel(const xrh_mirror_ta
     mirror_plane(T.na, T.nb, T.N, T.L, T.src, T.dst, T.accumulate, cta - T.cta_begin, tile);
 }
 
+__global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int L, const double* __restrict__ src,
+                                                     double* __restrict__ dst, int accumulate) {
+    __shared__ double tile[kMirrorTile];
+    mirror_plane(na, nb, N, L, src, dst, accumulate, blockIdx.x, tile);
+}
+
+extern "C" int64_t xrh_mirror_ctas(int N, int L) {
+    if (N <= 0 || N > 64 || L < 1 || L > 3) return 0;
+    return mirror_ctas_per_pair(N, L);
+}
+
 extern "C" int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, double* dst_dev, int accumulate,
                                   void* stream) {
     if (na <= 0 || nb <= 0 || N <= 0 || L < 1 || L > 3 || !src_dev || !dst_dev || src_dev == dst_dev)
         return XRH_ERR_ARG;
     if (N > 64) return XRH_ERR_CAPACITY;
-    const int64_t blocks = (int64_t)na * nb * (L == 3 ? N : 1);
+    const int64_t blocks = (int64_t)na * nb * mirror_ctas_per_pair(N, L);
     if (blocks > 0x7fffffffLL) return XRH_ERR_CAPACITY;
     mirror_kernel<<<(unsigned)blocks, L == 1 ? 64 : 256, 0, (cudaStream_t)stream>>>(na, nb, N, L, src_dev, dst_dev,
                                                                                       accumulate);
