@@ -183,6 +183,23 @@ int xrh_mirror_density(int na, int nb, int N, int L, const double* src_dev, doub
  * (a, b) pair (1 for L < 3; for L = 3 one CTA per group of about 4096 / N^2 q planes), 0 for
  * unsupported N or L. */
 int64_t xrh_mirror_ctas(int N, int L);
+
+/* Antisymmetric operator pairs (no reference counterpart: the reference's density loops visit
+ * every ordered index tuple, density_tensors.c:283-556).  Two adjacent operators of one kind
+ * anticommute, so rho[.. o_u, o_u+1 ..] = -rho[.. o_u+1, o_u ..] and the density kernels need
+ * the canonical tuples (o_u < o_u+1) only.  Task t covers one block in the transposed layout
+ * rows[idx * R + e] (idx row-major over L indices of N values, R = n_b n_k elements per row)
+ * and owns the launch's CTAs [cta_begin, cta_begin + N^L) (sorted, total_ctas the sum):
+ *   mode 0: rows[idx] = -rows[swap_u(idx)] for every idx with o_u > o_u+1 (fill);
+ *   mode 1: rows[idx] -= rows[swap_u(idx)] for every idx with o_u < o_u+1 (fold, the gradient
+ *           of the canonical rows from the full gradient). */
+typedef struct {
+    double* rows;
+    int64_t R;
+    int32_t N, L, u, mode;
+    int64_t cta_begin;
+} xrh_antisym_task;   /* 40 bytes */
+int xrh_antisym_rows(const xrh_antisym_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
 typedef struct {
     const double* src;
     double* dst;

@@ -88,6 +88,7 @@ _SIGS = {
     "xrh_index_move": (_i32, [_i64, _vp, _vp, _vp, _i32, _vp]),
     "xrh_f64_to_f32": (_i32, [_i64, _vp, _vp, _vp]),
     "xrh_mirror_ctas": (_i64, [_i32, _i32]),
+    "xrh_antisym_rows": (_i32, [_vp, _i32, _i64, _vp]),
     "xrh_add_mixed": (_i32, [_i64, _dbl, _vp, _vp, _vp, _vp]),
     "xrh_spin_sum_antisym": (_i32, [_i32, _i32, _vp, _vp, _i64, _vp, _vp]),
     "xrh_small_mm_grouped": (_i32, [_vp, _i32, _i64, _vp]),
@@ -202,6 +203,9 @@ assert MIRROR_TASK_DTYPE.itemsize == 48
 TRANSPOSE_TASK_DTYPE = np.dtype([("in", np.uint64), ("out", np.uint64), ("rows", np.int64), ("cols", np.int64),
                                  ("tile_begin", np.int64)])
 assert TRANSPOSE_TASK_DTYPE.itemsize == 40
+ANTISYM_TASK_DTYPE = np.dtype([("rows", np.uint64), ("R", np.int64), ("N", np.int32), ("L", np.int32),
+                               ("u", np.int32), ("mode", np.int32), ("cta_begin", np.int64)])
+assert ANTISYM_TASK_DTYPE.itemsize == 40
 COEFF_TASK_DTYPE = np.dtype([("src", np.uint64), ("zT", np.uint64), ("zT32", np.uint64), ("n", np.int64),
                              ("K", np.int64), ("npad", np.int64), ("row_begin", np.int64)])
 assert COEFF_TASK_DTYPE.itemsize == 56
@@ -290,6 +294,28 @@ class Mirrors:
     def run(self, stream=None):
         if self.n:
             call("xrh_mirror_grouped", ptr(self.dev), self.n, self.ctas, stream_ptr(stream))
+
+
+class AntisymRows:
+    """A fixed list of antisymmetric-pair row passes [(rows, R, N, L, u, mode)] run as one
+    xrh_antisym_rows launch (the blocks distinct)."""
+
+    def __init__(self, items, device):
+        import torch
+        tab = np.zeros(len(items), dtype=ANTISYM_TASK_DTYPE)
+        cta = 0
+        for i, (rows, R, N, L, u, mode) in enumerate(items):
+            if not (0 <= u < L - 1) or mode not in (0, 1) or rows.numel() < (N ** L) * R:
+                raise ValueError("bad antisymmetric row task")
+            t = tab[i]
+            t["rows"], t["R"], t["N"], t["L"], t["u"], t["mode"], t["cta_begin"] = rows.data_ptr(), R, N, L, u, mode, cta
+            cta += N ** L
+        self.n, self.ctas, self.keep = len(items), cta, items
+        self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(items) else None
+
+    def run(self, stream=None):
+        if self.n:
+            call("xrh_antisym_rows", ptr(self.dev), self.n, self.ctas, stream_ptr(stream))
 
 
 class PairLaunch:

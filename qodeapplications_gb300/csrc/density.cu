@@ -369,6 +369,51 @@ __global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int 
     mirror_plane(na, nb, N, L, src, dst, accumulate, blockIdx.x, tile);
 }
 
+// ---- antisymmetric operator pairs -------------------------------------------------------
+// Two adjacent operators of one kind anticommute (a_q a_r = -a_r a_q, c+_p c+_q = -c+_q c+_p), so
+// rho[.. o_u, o_u+1 ..] = -rho[.. o_u+1, o_u ..]: the density and adjoint kernels may run over the
+// canonical index tuples (o_u < o_u+1) only, and one pass over the rows of the [K][R] layout
+// (idx row-major over the L operator indices, R = n_b n_k) completes the rest:
+//   mode 0 (fill): row[idx] = -row[swap(idx)] for o_u > o_u+1 (rows with o_u = o_u+1 stay as the
+//                  kernels wrote them: zero, they have no couplings);
+//   mode 1 (fold): row[idx] -= row[swap(idx)] for o_u < o_u+1 (dE/drho of a canonical tuple from
+//                  the full gradient).
+// One CTA per operator index of a task (non-target indices return at once).
+__global__ void __launch_bounds__(256) antisym_rows_kernel(const xrh_antisym_task* __restrict__ tasks, int n_tasks) {
+    const int64_t cta = blockIdx.x;
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const xrh_antisym_task& T = tasks[lo];
+    const int64_t idx = cta - T.cta_begin;
+    int64_t w_lo = 1;                                   // N^(L-2-u): weight of digit u+1
+    for (int t = T.u + 2; t < T.L; ++t) w_lo *= T.N;
+    const int64_t w_hi = w_lo * T.N;                    // weight of digit u
+    const int a = (int)((idx / w_hi) % T.N), b = (int)((idx / w_lo) % T.N);
+    const bool target = T.mode == 0 ? a > b : a < b;
+    if (!target) return;
+    const int64_t partner = idx + (int64_t)(b - a) * w_hi + (int64_t)(a - b) * w_lo;
+    double* dst = T.rows + idx * T.R;
+    const double* src = T.rows + partner * T.R;
+    if (T.mode == 0) {
+        for (int64_t e = threadIdx.x; e < T.R; e += blockDim.x) dst[e] = -src[e];
+    } else {
+        for (int64_t e = threadIdx.x; e < T.R; e += blockDim.x) dst[e] -= src[e];
+    }
+}
+
+extern "C" int xrh_antisym_rows(const xrh_antisym_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream) {
+    if (n_tasks < 0 || total_ctas < 0) return XRH_ERR_ARG;
+    if (n_tasks == 0 || total_ctas == 0) return XRH_OK;
+    if (!tasks_dev) return XRH_ERR_ARG;
+    if (total_ctas > 0x7fffffffLL) return XRH_ERR_CAPACITY;
+    antisym_rows_kernel<<<(unsigned)total_ctas, 256, 0, (cudaStream_t)stream>>>(tasks_dev, n_tasks);
+    XRH_CHECK_LAUNCH();
+    return XRH_OK;
+}
+
 extern "C" int64_t xrh_mirror_ctas(int N, int L) {
     if (N <= 0 || N > 64 || L < 1 || L > 3) return 0;
     return mirror_ctas_per_pair(N, L);

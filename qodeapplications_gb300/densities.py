@@ -37,6 +37,38 @@ class Couplings:
         return int(self.P.numel())
 
 
+# op strings with two adjacent operators of one kind: position u of the anticommuting pair
+# (o_u, o_u+1).  rho[.. o_u, o_u+1 ..] = -rho[.. o_u+1, o_u ..], so the kernels need the
+# canonical tuples (o_u < o_u+1) only and xrh_antisym_rows completes the rest.
+ANTISYM_PAIR = {"aa": 0, "cc": 0, "caa": 1, "cca": 0}
+
+
+def canonical_couplings(space, key):
+    """The couplings of key = (op, bra charge, ket charge) restricted to the canonical index
+    tuples of op's anticommuting pair (about half of them; same order, same CSR over all K
+    indices, empty rows elsewhere), cached on the space; None for other op strings."""
+    op = key[0]
+    if op not in ANTISYM_PAIR or key not in space.couplings:
+        return None
+    cache = space.__dict__.setdefault("_canonical", {})
+    if key not in cache:
+        cp = space.couplings[key]
+        u, L, N = ANTISYM_PAIR[op], len(op), space.N
+        dev = cp.idx_ptr.device
+        counts = cp.idx_ptr[1:] - cp.idx_ptr[:-1]
+        idx_all = torch.arange(cp.K, dtype=torch.int64, device=dev)
+        a = (idx_all // N ** (L - 1 - u)) % N
+        b = (idx_all // N ** (L - 2 - u)) % N
+        keep = a < b
+        per = torch.repeat_interleave(keep, counts)
+        counts_c = torch.where(keep, counts, torch.zeros_like(counts))
+        idx_ptr = torch.zeros(cp.K + 1, dtype=torch.int64, device=dev)
+        idx_ptr[1:] = torch.cumsum(counts_c, 0)
+        cache[key] = Couplings(op, cp.K, idx_ptr, cp.P[per].contiguous(), cp.Q[per].contiguous(),
+                               cp.sign[per].contiguous())
+    return cache[key]
+
+
 def _sort_masks(masks_np):
     order = np.argsort(masks_np, kind="stable")
     return masks_np[order], order.astype(np.int32)
@@ -264,7 +296,7 @@ class DensityBuilder:
     With the same states on both sides (mirror=True, no bra_coeffs) the c, cc and cca
     blocks are mirrored from their a, aa and caa partners instead of accumulated."""
 
-    def __init__(self, space, n_states, precision="fp64", n_states_bra=None, mirror=True):
+    def __init__(self, space, n_states, precision="fp64", n_states_bra=None, mirror=True, antisym=True):
         self.space = space
         self.precision = _lib.PRECISIONS[precision]
         if self.precision not in (_lib.FP64, _lib.FP32):
@@ -300,6 +332,17 @@ class DensityBuilder:
                 arena_off += cp.K * nb * nk
             else:
                 self._tmp[(op, bc, kc)] = torch.empty(cp.K * nb * nk, dtype=torch.float64, device=dev)
+        # canonical lists for the accumulated blocks of op strings with an anticommuting pair (not
+        # the warp-per-unit blocks, whose unit tables index the full lists)
+        self._canon = {}
+        if antisym:
+            for key in space.couplings:
+                if key in self.mirror or key in self._unit_keys:
+                    continue
+                cc = canonical_couplings(space, key)
+                if cc is not None:
+                    self._canon[key] = cc
+        self._fill = None
         self.zT = {c: torch.empty((space.n_conf[c], self.n_states[c]), dtype=torch.float64, device=dev)
                    for c in space.charges}
         # the bra side is the ket side unless separate bra states are built (mirror off)
@@ -321,13 +364,15 @@ class DensityBuilder:
             # operator strings with few indices (K < 1024, e.g. K = N for a/c) spread the couplings
             # of every index over several CTAs, about 256 couplings each
             self.splits = {}
-            for key, cp in space.couplings.items():
+            for key, cp in ((k_, self._canon.get(k_, c_)) for k_, c_ in space.couplings.items()):
                 if cp.K >= 1024:
                     self.splits[key] = 1
                 else:
                     self.splits[key] = int(min(64, max(1, round(cp.count / max(cp.K, 1) / 256))))
-            # every accumulated block of the fragment in one grouped launch (CTA per operator index)
-            direct = [(key, cp) for key, cp in space.couplings.items()
+            # every accumulated block of the fragment in one grouped launch (CTA per operator index);
+            # op strings with an anticommuting pair run over their canonical tuples and are
+            # completed by one xrh_antisym_rows pass
+            direct = [(key, self._canon.get(key, cp)) for key, cp in space.couplings.items()
                       if key not in self.mirror and key not in self._unit_keys]
             tasks = np.zeros(len(direct), dtype=_lib.DENS_TASK_DTYPE)
             begin = 0
@@ -419,9 +464,16 @@ class DensityBuilder:
             for (op, bc, kc), cp in self.space.couplings.items():
                 if (op, bc, kc) in self.mirror:
                     continue
+                cp = self._canon.get((op, bc, kc), cp)
                 nb, nk = self.n_states_bra[bc], self.n_states[kc]
                 call("xrh_density_accumulate", self.precision, cp.K, ptr(cp.idx_ptr), ptr(cp.P), ptr(cp.Q),
                      ptr(cp.sign), ptr(self.zbT[bc]), nb, ptr(self.zT[kc]), nk, ptr(self._tmp[(op, bc, kc)]), s)
+        if self._canon:
+            if self._fill is None:
+                self._fill = _lib.AntisymRows(
+                    [(self._tmp[key], self.n_states_bra[key[1]] * self.n_states[key[2]], self.space.N, len(key[0]),
+                      ANTISYM_PAIR[key[0]], 0) for key in self._canon], self.space.device)
+            self._fill.run()
         if self._tr_direct is None:
             # rho^T [K, nb nk] -> rho [nb nk, K] for the accumulated blocks; the mirrored blocks go
             # the other way after the mirror kernels (their rho^T feeds the reverse pass)

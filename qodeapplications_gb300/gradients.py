@@ -333,6 +333,7 @@ class XRDimerAdjoint:
                 gT = take(cp.K * rt.shape[0] * rt.shape[1])
                 self.dens_adj.append((m, op, bc, kc, cp, rt, grad_of[rt.data_ptr()], gT))
         self.dens_adj_all = list(self.dens_adj)
+        self._fold = None
         # FP32 path: every block of a fragment in one grouped launch, on the tensor cores when
         # every block has at most 64 states per side (else the CUDA-core kernel)
         self.dens_adj_groups = []
@@ -343,6 +344,7 @@ class XRDimerAdjoint:
         if density_adjoint == "tc" and not use_tc:
             raise ValueError("the tensor-core density adjoint needs a split-precision plan and <= 64 states")
         if use_tc:
+            self._canonicalize()
             self.z_split = []
             for m in (0, 1):
                 bld = plan.builders[m]
@@ -393,6 +395,7 @@ class XRDimerAdjoint:
                                                 torch.from_numpy(units.view(np.uint8).copy()).to(dev), len(units),
                                                 max(max(e[5].shape[0], e[5].shape[1]) for e in small)))
                     self.dens_adj = [e for e in self.dens_adj if not any(e is x for x in small)]
+                self._canonicalize(m)
                 entries = [e for e in self.dens_adj if e[0] == m]
                 if not entries:
                     continue
@@ -410,6 +413,30 @@ class XRDimerAdjoint:
                 dev_tasks = torch.from_numpy(tasks.view(np.uint8).copy()).to(dev)
                 self.dens_adj_groups.append((dev_tasks, len(entries), begin,
                                              max(e[5].shape[0] for e in entries), max(e[5].shape[1] for e in entries)))
+        else:
+            self._canonicalize()         # the FP64 per-block adjoint
+
+    def _canonicalize(self, m=None):
+        """Entries of self.dens_adj (of fragment m, or all) whose op string has an anticommuting
+        pair run over the canonical tuples: their coupling list becomes the canonical one and
+        their transposed gradient is folded first (dE/drho_canonical = g - g_swapped)."""
+        from .densities import ANTISYM_PAIR, canonical_couplings
+        plan = self.plan
+        out, fold = [], list(self._fold.keep) if self._fold is not None else []
+        for e in self.dens_adj:
+            (m_, op, bc, kc, cp, rt, grho, gT) = e
+            if (m is None or m_ == m) and op in ANTISYM_PAIR and getattr(self, "_antisym", True):
+                cc = canonical_couplings(plan.spaces[m_], (op, bc, kc))
+                if cc is not None and cc is not cp:
+                    e = (m_, op, bc, kc, cc, rt, grho, gT)
+                    fold.append((gT, rt.shape[0] * rt.shape[1], plan.N[m_], len(op), ANTISYM_PAIR[op], 1))
+            out.append(e)
+        self.dens_adj = out
+        if fold:
+            self._fold = _lib.AntisymRows(fold, plan.device)
+        # the work actually done per launch: the canonical lists where they are used
+        ids = {(e[0],) + e[1:4]: e for e in out}
+        self.dens_adj_all = [ids.get((e[0],) + e[1:4], e) for e in self.dens_adj_all]
 
     # ------------------------------------------------------------------------------------
     def launch_L3(self):
@@ -441,8 +468,12 @@ class XRDimerAdjoint:
         for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             nb, nk = rt.shape[0], rt.shape[1]
             call("xrh_transpose", ptr(grho), nb * nk, cp.K, ptr(gT), s)
+        if self._fold is not None:
+            self._fold.run()
+        for (m, op, bc, kc, cp, rt, grho, gT) in self.dens_adj:
             if self.prec32:
-                continue
+                break
+            nb, nk = rt.shape[0], rt.shape[1]
             bld = plan.builders[m]
             call("xrh_density_adjoint", _lib.PRECISIONS[plan.dens_precision], cp.K, ptr(cp.idx_ptr), ptr(cp.P),
                  ptr(cp.Q), ptr(cp.sign), ptr(bld.zbT[bc]), nb, ptr(bld.zT[kc]), nk, ptr(gT),
