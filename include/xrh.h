@@ -192,13 +192,18 @@ int64_t xrh_mirror_ctas(int N, int L);
  * and owns the launch's CTAs [cta_begin, cta_begin + N^L) (sorted, total_ctas the sum):
  *   mode 0: rows[idx] = -rows[swap_u(idx)] for every idx with o_u > o_u+1 (fill);
  *   mode 1: rows[idx] -= rows[swap_u(idx)] for every idx with o_u < o_u+1 (fold, the gradient
- *           of the canonical rows from the full gradient). */
+ *           of the canonical rows from the full gradient);
+ * and for a Hermitian pair (rho^ca between the same real states, R = nrow^2, rows read as
+ * nrow x nrow matrices M):
+ *   mode 2: M[idx] = M[swap_u(idx)]^T for o_u > o_u+1;   mode 3: M[idx] += M[swap_u(idx)]^T
+ *           for o_u < o_u+1. */
 typedef struct {
     double* rows;
     int64_t R;
     int32_t N, L, u, mode;
+    int32_t nrow, reserved;
     int64_t cta_begin;
-} xrh_antisym_task;   /* 40 bytes */
+} xrh_antisym_task;   /* 48 bytes */
 int xrh_antisym_rows(const xrh_antisym_task* tasks_dev, int n_tasks, int64_t total_ctas, void* stream);
 typedef struct {
     const double* src;

@@ -204,8 +204,9 @@ TRANSPOSE_TASK_DTYPE = np.dtype([("in", np.uint64), ("out", np.uint64), ("rows",
                                  ("tile_begin", np.int64)])
 assert TRANSPOSE_TASK_DTYPE.itemsize == 40
 ANTISYM_TASK_DTYPE = np.dtype([("rows", np.uint64), ("R", np.int64), ("N", np.int32), ("L", np.int32),
-                               ("u", np.int32), ("mode", np.int32), ("cta_begin", np.int64)])
-assert ANTISYM_TASK_DTYPE.itemsize == 40
+                               ("u", np.int32), ("mode", np.int32), ("nrow", np.int32), ("reserved", np.int32),
+                               ("cta_begin", np.int64)])
+assert ANTISYM_TASK_DTYPE.itemsize == 48
 COEFF_TASK_DTYPE = np.dtype([("src", np.uint64), ("zT", np.uint64), ("zT32", np.uint64), ("n", np.int64),
                              ("K", np.int64), ("npad", np.int64), ("row_begin", np.int64)])
 assert COEFF_TASK_DTYPE.itemsize == 56
@@ -297,18 +298,22 @@ class Mirrors:
 
 
 class AntisymRows:
-    """A fixed list of antisymmetric-pair row passes [(rows, R, N, L, u, mode)] run as one
-    xrh_antisym_rows launch (the blocks distinct)."""
+    """A fixed list of operator-pair row passes [(rows, R, N, L, u, mode)] run as one
+    xrh_antisym_rows launch (the blocks distinct); modes 2 and 3 (Hermitian pairs) read the
+    rows as square matrices (R a square)."""
 
     def __init__(self, items, device):
         import torch
         tab = np.zeros(len(items), dtype=ANTISYM_TASK_DTYPE)
         cta = 0
         for i, (rows, R, N, L, u, mode) in enumerate(items):
-            if not (0 <= u < L - 1) or mode not in (0, 1) or rows.numel() < (N ** L) * R:
-                raise ValueError("bad antisymmetric row task")
+            nrow = int(round(R ** 0.5))
+            if (not (0 <= u < L - 1) or mode not in (0, 1, 2, 3) or rows.numel() < (N ** L) * R or
+                    (mode >= 2 and nrow * nrow != R)):
+                raise ValueError("bad operator-pair row task")
             t = tab[i]
             t["rows"], t["R"], t["N"], t["L"], t["u"], t["mode"], t["cta_begin"] = rows.data_ptr(), R, N, L, u, mode, cta
+            t["nrow"] = nrow if mode >= 2 else 0
             cta += N ** L
         self.n, self.ctas, self.keep = len(items), cta, items
         self.dev = torch.from_numpy(tab.view(np.uint8).copy()).to(device) if len(items) else None

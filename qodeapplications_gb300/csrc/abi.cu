@@ -34,7 +34,7 @@ static_assert(sizeof(xrh_dens_adj_tc_task) == 112, "xrh_dens_adj_tc_task layout 
 static_assert(sizeof(xrh_pair_task) == 72, "xrh_pair_task layout is part of the ABI");
 static_assert(sizeof(xrh_orbital_inputs) == 128, "xrh_orbital_inputs layout is part of the ABI");
 static_assert(sizeof(xrh_mirror_task) == 48, "xrh_mirror_task layout is part of the ABI");
-static_assert(sizeof(xrh_antisym_task) == 40, "xrh_antisym_task layout is part of the ABI");
+static_assert(sizeof(xrh_antisym_task) == 48, "xrh_antisym_task layout is part of the ABI");
 static_assert(sizeof(xrh_transpose_task) == 40, "xrh_transpose_task layout is part of the ABI");
 static_assert(sizeof(xrh_coeff_task) == 56, "xrh_coeff_task layout is part of the ABI");
 static_assert(sizeof(xrh_abt_task) == 88, "xrh_abt_task layout is part of the ABI");

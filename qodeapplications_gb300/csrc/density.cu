@@ -378,6 +378,11 @@ __global__ void __launch_bounds__(256) mirror_kernel(int na, int nb, int N, int 
 //                  kernels wrote them: zero, they have no couplings);
 //   mode 1 (fold): row[idx] -= row[swap(idx)] for o_u < o_u+1 (dE/drho of a canonical tuple from
 //                  the full gradient).
+// A creation-annihilation pair between the same states (rho^ca of a diagonal charge block, real
+// states) is Hermitian instead: rho[i, j, p, q] = rho[j, i, q, p], the row of (q, p) the row of
+// (p, q) transposed as an n x n matrix (n = nrow):
+//   mode 2 (fill):  row[idx][i n + j] = row[swap(idx)][j n + i] for o_u > o_u+1;
+//   mode 3 (fold):  row[idx][i n + j] += row[swap(idx)][j n + i] for o_u < o_u+1.
 // One CTA per operator index of a task (non-target indices return at once).
 __global__ void __launch_bounds__(256) antisym_rows_kernel(const xrh_antisym_task* __restrict__ tasks, int n_tasks) {
     const int64_t cta = blockIdx.x;
@@ -392,15 +397,22 @@ __global__ void __launch_bounds__(256) antisym_rows_kernel(const xrh_antisym_tas
     for (int t = T.u + 2; t < T.L; ++t) w_lo *= T.N;
     const int64_t w_hi = w_lo * T.N;                    // weight of digit u
     const int a = (int)((idx / w_hi) % T.N), b = (int)((idx / w_lo) % T.N);
-    const bool target = T.mode == 0 ? a > b : a < b;
+    const bool target = (T.mode == 0 || T.mode == 2) ? a > b : a < b;
     if (!target) return;
     const int64_t partner = idx + (int64_t)(b - a) * w_hi + (int64_t)(a - b) * w_lo;
     double* dst = T.rows + idx * T.R;
     const double* src = T.rows + partner * T.R;
     if (T.mode == 0) {
         for (int64_t e = threadIdx.x; e < T.R; e += blockDim.x) dst[e] = -src[e];
-    } else {
+    } else if (T.mode == 1) {
         for (int64_t e = threadIdx.x; e < T.R; e += blockDim.x) dst[e] -= src[e];
+    } else {
+        const int n = T.nrow;
+        for (int64_t e = threadIdx.x; e < T.R; e += blockDim.x) {
+            const int i = (int)(e / n), j = (int)(e - (int64_t)i * n);
+            const double v = src[(int64_t)j * n + i];
+            dst[e] = T.mode == 2 ? v : dst[e] + v;
+        }
     }
 }
 

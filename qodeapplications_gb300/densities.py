@@ -41,25 +41,39 @@ class Couplings:
 # (o_u, o_u+1).  rho[.. o_u, o_u+1 ..] = -rho[.. o_u+1, o_u ..], so the kernels need the
 # canonical tuples (o_u < o_u+1) only and xrh_antisym_rows completes the rest.
 ANTISYM_PAIR = {"aa": 0, "cc": 0, "caa": 1, "cca": 0}
+# rho^ca between the same real states is Hermitian: rho[i, j, p, q] = rho[j, i, q, p], so the
+# tuples p <= q suffice there (the (q, p) row is the (p, q) row transposed)
+HERMITIAN_PAIR = {"ca": 0}
+
+
+def pair_position(op):
+    """(u, mode_fill, mode_fold) of op's operator pair for xrh_antisym_rows, or None."""
+    if op in ANTISYM_PAIR:
+        return ANTISYM_PAIR[op], 0, 1
+    if op in HERMITIAN_PAIR:
+        return HERMITIAN_PAIR[op], 2, 3
+    return None
 
 
 def canonical_couplings(space, key):
     """The couplings of key = (op, bra charge, ket charge) restricted to the canonical index
-    tuples of op's anticommuting pair (about half of them; same order, same CSR over all K
-    indices, empty rows elsewhere), cached on the space; None for other op strings."""
+    tuples of op's operator pair (o_u < o_u+1 for an anticommuting pair, o_u <= o_u+1 for the
+    Hermitian ca pair; about half of them; same order, same CSR over all K indices, empty rows
+    elsewhere), cached on the space; None for other op strings.  The Hermitian form holds for
+    a block between the same states only: the caller decides."""
     op = key[0]
-    if op not in ANTISYM_PAIR or key not in space.couplings:
+    if pair_position(op) is None or key not in space.couplings:
         return None
     cache = space.__dict__.setdefault("_canonical", {})
     if key not in cache:
         cp = space.couplings[key]
-        u, L, N = ANTISYM_PAIR[op], len(op), space.N
+        u, L, N = pair_position(op)[0], len(op), space.N
         dev = cp.idx_ptr.device
         counts = cp.idx_ptr[1:] - cp.idx_ptr[:-1]
         idx_all = torch.arange(cp.K, dtype=torch.int64, device=dev)
         a = (idx_all // N ** (L - 1 - u)) % N
         b = (idx_all // N ** (L - 2 - u)) % N
-        keep = a < b
+        keep = a < b if op in ANTISYM_PAIR else a <= b
         per = torch.repeat_interleave(keep, counts)
         counts_c = torch.where(keep, counts, torch.zeros_like(counts))
         idx_ptr = torch.zeros(cp.K + 1, dtype=torch.int64, device=dev)
@@ -304,6 +318,8 @@ class DensityBuilder:
         self.n_states = dict(n_states)
         self.n_states_bra = dict(n_states_bra or n_states)
         self.mirror = mirror_pairs(space) if (mirror and self.n_states_bra == self.n_states) else {}
+        # bra states are the ket states (no separate bra coefficients can come in)
+        self.same_bra_states = bool(mirror) and self.n_states_bra == self.n_states
         dev = space.device
         self.rho = {}
         self._tmp = {}
@@ -339,6 +355,8 @@ class DensityBuilder:
             for key in space.couplings:
                 if key in self.mirror or key in self._unit_keys:
                     continue
+                if key[0] in HERMITIAN_PAIR and not (self.same_bra_states and key[1] == key[2]):
+                    continue             # Hermitian only between the same states
                 cc = canonical_couplings(space, key)
                 if cc is not None:
                     self._canon[key] = cc
@@ -472,7 +490,7 @@ class DensityBuilder:
             if self._fill is None:
                 self._fill = _lib.AntisymRows(
                     [(self._tmp[key], self.n_states_bra[key[1]] * self.n_states[key[2]], self.space.N, len(key[0]),
-                      ANTISYM_PAIR[key[0]], 0) for key in self._canon], self.space.device)
+                      pair_position(key[0])[0], pair_position(key[0])[1]) for key in self._canon], self.space.device)
             self._fill.run()
         if self._tr_direct is None:
             # rho^T [K, nb nk] -> rho [nb nk, K] for the accumulated blocks; the mirrored blocks go

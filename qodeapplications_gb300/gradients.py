@@ -420,16 +420,18 @@ class XRDimerAdjoint:
         """Entries of self.dens_adj (of fragment m, or all) whose op string has an anticommuting
         pair run over the canonical tuples: their coupling list becomes the canonical one and
         their transposed gradient is folded first (dE/drho_canonical = g - g_swapped)."""
-        from .densities import ANTISYM_PAIR, canonical_couplings
+        from .densities import HERMITIAN_PAIR, canonical_couplings, pair_position
         plan = self.plan
         out, fold = [], list(self._fold.keep) if self._fold is not None else []
         for e in self.dens_adj:
             (m_, op, bc, kc, cp, rt, grho, gT) = e
-            if (m is None or m_ == m) and op in ANTISYM_PAIR and getattr(self, "_antisym", True):
+            pp = pair_position(op)
+            hermitian_ok = op not in HERMITIAN_PAIR or (bc == kc and getattr(plan.builders[m_], "same_bra_states", False))
+            if (m is None or m_ == m) and pp is not None and hermitian_ok and getattr(self, "_antisym", True):
                 cc = canonical_couplings(plan.spaces[m_], (op, bc, kc))
                 if cc is not None and cc is not cp:
                     e = (m_, op, bc, kc, cc, rt, grho, gT)
-                    fold.append((gT, rt.shape[0] * rt.shape[1], plan.N[m_], len(op), ANTISYM_PAIR[op], 1))
+                    fold.append((gT, rt.shape[0] * rt.shape[1], plan.N[m_], len(op), pp[0], pp[2]))
             out.append(e)
         self.dens_adj = out
         if fold:
