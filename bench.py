@@ -325,7 +325,7 @@ def time_variant(sysd, precision, steps, warmup, l2_flush):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from ncu captures of the bench
 # command (the summaries are in profiles/); None where no capture of the current kernel exists
-DENSITY_ADJ_TRAFFIC = {}
+DENSITY_ADJ_TRAFFIC = {(3, "density_adjoint_f32_grouped_kernel"): 0.675e9}
 
 
 def measure_peaks():
